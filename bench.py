@@ -1,0 +1,374 @@
+#!/usr/bin/env python
+"""Benchmark: Embedding Propagation training throughput on GB300.
+
+A step is one training batch (one optimizer step) of the 10M-node Chung-Lu
+workload (``cl10m``: 10M nodes, ~160M directed edges, degree exponent 2.0,
+degrees clipped to [1, 10^4]; Poisson(6) features over 2M Zipf(1.05) slots;
+dims 256, max_neighbors 25, 10 negatives, StarSpace margin 0.5, batch 8192).
+
+Legs in one run (rank 0, N=1):
+  value        fused BF16 form, inputs resident in HBM, CUDA-event time of the
+               timed batches (a CUDA graph replay per batch)
+  plain_fp32   the plain FP32 form on the same workload and steps
+  cpu_baseline the oracle's CPU restatement of the reference training loop on
+               a bounded sample of the same workload, all host threads
+  e2e          one full pass through the C ABI from pinned host buffers:
+               context creation, graph/feature upload, table init, training,
+               table download, all inside the timed region
+  roofline     algorithmic bytes of the dominant stage / its mean CUDA-event
+               duration from a stage-by-stage profile of the same batches
+
+``--impl reference`` times only the CPU reference restatement (the Rust
+reference cannot be built here) and prints its own line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "EP train nodes/sec & HBM roofline %: fused BF16 vs plain FP32 GPU vs CPU ref"
+UNIT = "nodes/sec"
+L2_NOTE = "inputs larger than L2 (BF16 table ~1 GB, CSR ~1.3 GB, Adam moments ~4 GB per step's random rows)"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3000)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="cl10m")
+    p.add_argument("--scale", type=float, default=1.0, help="shrink the Chung-Lu node count (profiling)")
+    p.add_argument("--loss", default="starspace", choices=["starspace", "margin"])
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--profile-steps", type=int, default=100)
+    return p.parse_args()
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allmax(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def pinned_copy(a: np.ndarray) -> np.ndarray:
+    """A copy of `a` in page-locked host memory (so host->device copies run at
+    full link speed)."""
+    import torch
+
+    t = torch.empty(a.shape, dtype={np.uint64: torch.int64, np.uint32: torch.int32,
+                                    np.float32: torch.float32}[a.dtype.type], pin_memory=True)
+    out = t.numpy().view(a.dtype)
+    out[...] = a
+    out._owner = t  # noqa: keep the pinned tensor alive
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    rows.append((float(p[1]), float(p[2]), p[5:9]))
+                except ValueError:
+                    continue
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        mx = max(r[1] for r in rows)
+        load = [r for r in rows if r[0] >= 0.5 * mx] or rows
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[2]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in load), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic(workload):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
+    summary (profiles/), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(workload)
+    except Exception:
+        return None
+
+
+def make_config(ep, form, loss, passes=1):
+    from cloverleaf_gb300 import _native
+
+    cfg = _native.default_config()
+    cfg.alpha, cfg.dims, cfg.batch_size, cfg.passes = ep["alpha"], ep["dims"], ep["batch_size"], passes
+    cfg.loss = _native.LOSS_STARSPACE if loss == "starspace" else _native.LOSS_MARGIN
+    cfg.gamma, cfg.negatives = ep["gamma"], ep["negatives"]
+    cfg.max_nodes_kind, cfg.max_nodes = _native.SAMPLE_FIXED, float(ep["max_nodes"])
+    cfg.valid_pct = 0.0
+    cfg.form = _native.FORM_FUSED_BF16 if form == "fused" else _native.FORM_PLAIN_FP32
+    cfg.device = int(os.environ.get("LOCAL_RANK", "0"))
+    return cfg
+
+
+def gpu_leg(w, form, loss, steps, warmup, world, sampler_device=None):
+    from cloverleaf_gb300 import _native
+
+    ctx = _native.Context(make_config(w["ep"], form, loss))
+    ctx.upload_graph(w["rows"], w["cols"], w["weights"])
+    ctx.upload_features(w["fptr"], w["fids"], w["n_feat"])
+    ctx.set_table(None)
+    ctx.train_batches(warmup)
+    clocks = None
+    barrier(world)
+    t0 = time.perf_counter()
+    if sampler_device is not None:
+        with ClockSampler(sampler_device) as cs:
+            st = ctx.train_batches(steps)
+        clocks = cs.summary()
+    else:
+        st = ctx.train_batches(steps)
+    wall = time.perf_counter() - t0
+    barrier(world)
+    return ctx, st, wall, clocks
+
+
+def cpu_reference(w, loss, seconds, threads=0, max_batches=None):
+    """The oracle's restatement of the reference loop on host cores, on a
+    bounded number of batches sized to take about `seconds`."""
+    from oracle import ep_oracle as O
+
+    ep = w["ep"]
+    kw = dict(dims=ep["dims"], alpha=ep["alpha"], loss=O.LOSS_STARSPACE if loss == "starspace" else O.LOSS_MARGIN,
+              gamma=ep["gamma"], negatives=ep["negatives"], batch_size=ep["batch_size"], passes=1,
+              max_nodes=(O.SAMPLE_FIXED, float(ep["max_nodes"])), threads=threads)
+    args = (w["rows"], w["cols"], w["weights"], w["fptr"], w["fids"], w["n_feat"])
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    if max_batches is None:
+        _, st = O.train(*args, max_batches=max(2, cores // 4), **kw)
+        rate = st.anchors / max(st.seconds, 1e-9)
+        max_batches = max(cores, int(seconds * rate / ep["batch_size"]))
+    _, st = O.train(*args, max_batches=max_batches, **kw)
+    return st.anchors / st.seconds, st, cores, max_batches
+
+
+def main():
+    args = parse()
+    rank, world = dist_setup(args.gpus)
+    from cloverleaf_gb300 import datagen
+
+    if args.impl == "reference" and rank != 0:
+        return 0
+    t0 = time.time()
+    w = datagen.workload(args.workload, scale=args.scale)
+    ep = w["ep"]
+    n_nodes = len(w["rows"]) - 1
+    if rank == 0:
+        log(f"[bench] {args.workload}: {n_nodes} nodes, {len(w['cols'])} directed edges, "
+            f"{len(w['fids'])} feature occurrences, {w['n_feat']} slots ({time.time() - t0:.1f}s)")
+    wl = (f"{args.workload}: Chung-Lu {n_nodes} nodes / {len(w['cols'])} directed edges, dims {ep['dims']}, "
+          f"max_neighbors {ep['max_nodes']}, {ep['negatives']} negatives, batch {ep['batch_size']}, {args.loss} 0.5")
+    config = {"workload": wl, "nodes": n_nodes, "edges": int(len(w["cols"])), "dims": ep["dims"],
+              "batch": ep["batch_size"], "max_neighbors": ep["max_nodes"], "negatives": ep["negatives"],
+              "loss": args.loss, "table_dtype": "bf16", "moments_dtype": "f32", "l2": L2_NOTE,
+              "parallelism": f"replicas{world}" if world > 1 else "single"}
+
+    if args.impl == "reference":
+        cores = os.cpu_count() or 1
+        _, stw, _, _ = cpu_reference(w, args.loss, 0, max_batches=max(args.warmup, 1))
+        value, st, cores, nb = cpu_reference(w, args.loss, 0, max_batches=max(args.steps, 1))
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": nb, "warmup": args.warmup, "ms_per_step": 1e3 * st.seconds / max(st.batches, 1),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": dict(config, table_dtype="f32"),
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                                 "sample": f"{st.batches} batches of {ep['batch_size']} anchors "
+                                           f"({st.anchors} anchors) of the {args.workload} workload"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+
+    # pinned host copies: the e2e leg uploads from these
+    for k in ("rows", "cols", "weights", "fptr", "fids"):
+        w[k] = pinned_copy(np.ascontiguousarray(w[k]))
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+
+    # --- fused BF16 (headline) ---
+    ctx, st, wall, clocks = gpu_leg(w, "fused", args.loss, args.steps, args.warmup, world,
+                                    sampler_device=dev if rank == 0 else None)
+    ms = allmax(st["ms"], world)
+    anchors = allsum(st["anchors"], world)
+    value = anchors / (ms / 1e3)
+    log(f"[bench] fused: {st['anchors']} anchors in {st['ms']:.1f} ms device / {wall:.2f} s wall "
+        f"-> {value / 1e6:.2f} M nodes/s; loss {st['train_loss']:.4f}")
+    stage_ms, pst = ctx.profile_batches(min(args.profile_steps, args.steps))
+    ctx.close()
+    B = pst["batches"] or 1
+    d, s_el = ep["dims"], 2.0
+    G, U, S, A = pst["gathered_rows"] / B, pst["unique_rows"] / B, pst["sampled_neighbors"] / B, pst["anchors"] / B
+    stage_bytes = {"forward": G * d * s_el + 4 * G + 4 * S + 8 * A * (ep["negatives"] + 2),
+                   "reduce": U * d * (2 * s_el + 16)}
+    dom = max(stage_ms, key=stage_ms.get)
+    peak, peak_kind = load_peaks()
+    rf_stage = "forward" if stage_ms["forward"] >= stage_ms["reduce"] else "reduce"
+    achieved = stage_bytes[rf_stage] / (stage_ms[rf_stage] / 1e3) / 1e9
+    step_bytes = pst["alg_bytes"] / B
+    step_ms = st["ms"] / max(st["batches"], 1)
+    roofline = {"bound": "hbm", "kernel": {"forward": "k_forward", "reduce": "k_reduce+k_fixup"}[rf_stage],
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)",
+                "traffic": load_traffic(args.workload), "alg_bytes_per_launch": stage_bytes[rf_stage],
+                "stage_ms": stage_ms, "dominant_stage": dom,
+                "step": {"achieved": step_bytes / (step_ms / 1e3) / 1e9, "alg_bytes_per_step": step_bytes,
+                         "frac": step_bytes / (step_ms / 1e3) / 1e9 / peak},
+                "per_batch": {"G": G, "U": U, "S": S, "items": pst["items"] / B}}
+    log(f"[bench] stages (ms/batch): " + ", ".join(f"{k} {v:.3f}" for k, v in stage_ms.items()))
+
+    # --- plain FP32 ---
+    plain = None
+    if not args.no_plain:
+        pctx, pst2, pwall, _ = gpu_leg(w, "plain", args.loss, args.steps, args.warmup, world)
+        pctx.close()
+        pms = allmax(pst2["ms"], world)
+        pv = allsum(pst2["anchors"], world) / (pms / 1e3)
+        plain = {"value": pv, "unit": UNIT, "ms_per_step": pms / max(pst2["batches"], 1),
+                 "fused_speedup": value / pv}
+        log(f"[bench] plain fp32: {pv / 1e6:.2f} M nodes/s (fused {value / pv:.2f}x)")
+
+    # --- end to end through the C ABI from pinned host buffers (one pass) ---
+    e2e = None
+    if not args.no_e2e:
+        from cloverleaf_gb300 import _native
+
+        barrier(world)
+        t1 = time.perf_counter()
+        ectx = _native.Context(make_config(ep, "fused", args.loss, passes=1))
+        ectx.upload_graph(w["rows"], w["cols"], w["weights"])
+        ectx.upload_features(w["fptr"], w["fids"], w["n_feat"])
+        ectx.set_table(None)
+        est = ectx.train(1)[0]
+        table = ectx.get_table(w["n_feat"], d)
+        ectx.close()
+        t2 = time.perf_counter()
+        e_sec = allmax(t2 - t1, world)
+        h2d = sum(w[k].nbytes for k in ("rows", "cols", "weights", "fptr", "fids"))
+        nb = max(est["batches"], 1)
+        e2e = {"value": allsum(est["anchors"], world) / e_sec, "unit": UNIT, "h2d_bytes_per_step": h2d / nb,
+               "d2h_bytes_per_step": table.nbytes / nb, "steps": nb, "seconds": e_sec,
+               "note": "one full pass via ep_create/upload/set_table/ep_train/ep_get_table"}
+        log(f"[bench] e2e: {e2e['value'] / 1e6:.2f} M nodes/s over {nb} steps ({e_sec:.2f}s)")
+
+    # --- CPU reference restatement (rank 0) ---
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cv, cst, cores, nb = cpu_reference(w, args.loss, args.cpu_seconds)
+        cpu = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{cst.batches} batches of {ep['batch_size']} anchors ({cst.anchors} anchors) of "
+                         f"{args.workload}, {cst.seconds:.1f}s"}
+        log(f"[bench] cpu reference: {cv / 1e3:.1f} k nodes/s on {cores} threads")
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / max(st["batches"], 1), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(st["launches"]),
+                "clocks": clocks, "plain_fp32": plain,
+                "speedup_vs_cpu": (value / cpu["value"]) if cpu else None}
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,314 @@
+"""ctypes binding of ``include/ep_gb300.h`` and ``include/ep_datagen.h``.
+
+The shared library is the product path: every training call goes through it,
+and loading fails loudly (``NativeError``) when it cannot be built or loaded;
+there is no Python fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import _build
+
+ABI_VERSION = 1
+
+EP_OK = 0
+_STATUS = {
+    -1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "bad call order",
+    -5: "device error flag", -6: "unsupported option", -7: "no CUDA device",
+}
+LOSS_MARGIN, LOSS_STARSPACE, LOSS_CONTRASTIVE = 0, 1, 2
+SAMPLE_ALL, SAMPLE_FIXED, SAMPLE_PROB = 0, 1, 2
+LW_NONE, LW_LOG, LW_EXP = 0, 1, 2
+FORM_PLAIN_FP32, FORM_FUSED_BF16 = 0, 1
+GRAD_REFERENCE, GRAD_TRUE = 0, 1
+
+
+class NativeError(RuntimeError):
+    """A C-ABI call returned an error status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{message} ({_STATUS.get(code, 'error')} {code})")
+        self.code = code
+
+
+class UnsupportedOption(NativeError, NotImplementedError):
+    pass
+
+
+class EpConfig(ctypes.Structure):
+    _fields_ = [
+        ("abi_version", ctypes.c_uint32),
+        ("alpha", ctypes.c_float),
+        ("loss", ctypes.c_int32),
+        ("gamma", ctypes.c_float),
+        ("neg_margin", ctypes.c_float),
+        ("negatives", ctypes.c_uint32),
+        ("batch_size", ctypes.c_uint32),
+        ("dims", ctypes.c_uint32),
+        ("passes", ctypes.c_uint32),
+        ("seed", ctypes.c_uint64),
+        ("max_nodes_kind", ctypes.c_int32),
+        ("max_nodes", ctypes.c_float),
+        ("max_features_kind", ctypes.c_int32),
+        ("max_features", ctypes.c_float),
+        ("weighted_neighbor_sampling", ctypes.c_int32),
+        ("weighted_neighbor_averaging", ctypes.c_int32),
+        ("loss_weighting", ctypes.c_int32),
+        ("loss_weighting_exp", ctypes.c_float),
+        ("valid_pct", ctypes.c_float),
+        ("hard_negatives", ctypes.c_uint32),
+        ("noise", ctypes.c_float),
+        ("form", ctypes.c_int32),
+        ("grad_mode", ctypes.c_int32),
+        ("device", ctypes.c_int32),
+        ("use_graphs", ctypes.c_int32),
+        ("autotune", ctypes.c_int32),
+    ]
+
+
+class EpPassStats(ctypes.Structure):
+    _fields_ = [
+        ("pass_", ctypes.c_uint32),
+        ("batches", ctypes.c_uint32),
+        ("train_loss", ctypes.c_float),
+        ("valid_loss", ctypes.c_float),
+        ("lr_last", ctypes.c_float),
+        ("pad", ctypes.c_uint32),
+        ("anchors", ctypes.c_uint64),
+        ("kept_anchors", ctypes.c_uint64),
+        ("nan_anchors", ctypes.c_uint64),
+        ("items", ctypes.c_uint64),
+        ("gathered_rows", ctypes.c_uint64),
+        ("unique_rows", ctypes.c_uint64),
+        ("sampled_neighbors", ctypes.c_uint64),
+        ("ms", ctypes.c_double),
+        ("alg_bytes", ctypes.c_double),
+        ("launches", ctypes.c_uint64),
+    ]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+        d["pass"] = d.pop("pass_")
+        return d
+
+
+class EpBatchSamples(ctypes.Structure):
+    _fields_ = [
+        ("n_anchors", ctypes.c_uint32),
+        ("anchors", ctypes.c_void_p),
+        ("nbr_ptr", ctypes.c_void_p),
+        ("nbr", ctypes.c_void_p),
+        ("nbr_w", ctypes.c_void_p),
+        ("negatives", ctypes.c_void_p),
+    ]
+
+
+class EpSparseGrad(ctypes.Structure):
+    _fields_ = [
+        ("capacity", ctypes.c_uint32),
+        ("n_rows", ctypes.c_uint32),
+        ("feat_ids", ctypes.c_void_p),
+        ("rows", ctypes.c_void_p),
+        ("loss", ctypes.c_void_p),
+        ("status", ctypes.c_void_p),
+    ]
+
+
+_lock = threading.Lock()
+_lib = None
+
+# name -> (restype, argtypes)
+_P = ctypes.c_void_p
+_U32, _U64, _I32, _F32 = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32, ctypes.c_float
+SIGNATURES = {
+    "ep_config_default": (None, [ctypes.POINTER(EpConfig)]),
+    "ep_create": (ctypes.c_int, [ctypes.POINTER(EpConfig), ctypes.POINTER(_P)]),
+    "ep_upload_graph": (ctypes.c_int, [_P, _U64, _P, _P, _P]),
+    "ep_upload_features": (ctypes.c_int, [_P, _U64, _P, _P, _U32]),
+    "ep_set_table": (ctypes.c_int, [_P, _P]),
+    "ep_train": (ctypes.c_int, [_P, ctypes.POINTER(EpPassStats), _U32]),
+    "ep_train_batches": (ctypes.c_int, [_P, _U32, ctypes.POINTER(EpPassStats)]),
+    "ep_profile_batches": (ctypes.c_int, [_P, _U32, _P, ctypes.POINTER(EpPassStats)]),
+    "ep_batch_grad": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), ctypes.POINTER(EpSparseGrad)]),
+    "ep_batch_step": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), _F32, _U32]),
+    "ep_get_table": (ctypes.c_int, [_P, _P]),
+    "ep_ag_forward": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), ctypes.c_int, _P, _P, _P]),
+    "ep_ag_backward": (ctypes.c_int, [_P, _P, _P, _P]),
+    "ep_synchronize": (ctypes.c_int, [_P]),
+    "ep_last_error": (ctypes.c_char_p, [_P]),
+    "ep_destroy": (None, [_P]),
+    "ep_csr_from_edges": (ctypes.c_int, [_U64, _P, _P, _P, ctypes.c_int, _P, _P, _P, _P, _P]),
+    "ep_cdf_convert": (ctypes.c_int, [_U64, _P, _P]),
+    "epg_sbm": (ctypes.c_int, [_U64, _U32, ctypes.c_double, ctypes.c_double, _U64, _P, _P, _P, _P, _P]),
+    "epg_sbm_tokens": (ctypes.c_int, [_U64, _P, _U32, _U32, _U32, _U32, ctypes.c_double, _U32, _U64, _P, _P,
+                                      _P, _P, _P]),
+    "epg_chung_lu": (ctypes.c_int, [_U64, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, _F32,
+                                    _F32, _U64, _P, _P, _P, _P]),
+    "epg_zipf_features": (ctypes.c_int, [_U64, ctypes.c_double, _U32, _U32, ctypes.c_double, _U32, _U64, _P,
+                                         _P, _P]),
+}
+
+
+def lib():
+    """Loads (building first when needed) the native library."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            try:
+                path = _build.build()
+            except Exception as e:  # no toolchain / compile error
+                if not os.path.exists(_build.LIB_PATH):
+                    raise NativeError(-2, f"cannot build libep_gb300.so: {e}") from e
+                path = _build.LIB_PATH
+            handle = ctypes.CDLL(path)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(handle, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = handle
+        return _lib
+
+
+def ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else ctypes.c_void_p(0)
+
+
+def check(rc: int, ctx=None, what: str = ""):
+    if rc == EP_OK:
+        return
+    msg = lib().ep_last_error(ctx).decode(errors="replace")
+    cls = UnsupportedOption if rc == -6 else NativeError
+    raise cls(rc, f"{what}: {msg}" if what else msg)
+
+
+def default_config() -> EpConfig:
+    cfg = EpConfig()
+    lib().ep_config_default(ctypes.byref(cfg))
+    return cfg
+
+
+class Context:
+    """Owns one ``ep_ctx``; thin RAII wrapper used by the Python API."""
+
+    def __init__(self, cfg: EpConfig):
+        self._h = ctypes.c_void_p()
+        check(lib().ep_create(ctypes.byref(cfg), ctypes.byref(self._h)), None, "ep_create")
+        self.cfg = cfg
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().ep_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload_graph(self, rows, cols, wcdf=None):
+        rows = np.ascontiguousarray(rows, np.uint64)
+        cols = np.ascontiguousarray(cols, np.uint32)
+        w = None if wcdf is None else np.ascontiguousarray(wcdf, np.float32)
+        check(lib().ep_upload_graph(self._h, len(rows) - 1, ptr(rows), ptr(cols), ptr(w)), self._h, "ep_upload_graph")
+
+    def upload_features(self, fptr, fids, n_feat):
+        fptr = np.ascontiguousarray(fptr, np.uint64)
+        fids = np.ascontiguousarray(fids, np.uint32)
+        check(lib().ep_upload_features(self._h, len(fptr) - 1, ptr(fptr), ptr(fids), int(n_feat)), self._h,
+              "ep_upload_features")
+
+    def set_table(self, table=None):
+        t = None if table is None else np.ascontiguousarray(table, np.float32)
+        check(lib().ep_set_table(self._h, ptr(t)), self._h, "ep_set_table")
+
+    def get_table(self, n_feat, dims):
+        out = np.empty((n_feat, dims), np.float32)
+        check(lib().ep_get_table(self._h, ptr(out)), self._h, "ep_get_table")
+        return out
+
+    def train(self, passes):
+        stats = (EpPassStats * max(passes, 1))()
+        check(lib().ep_train(self._h, stats, passes), self._h, "ep_train")
+        return [s.as_dict() for s in stats[:passes]]
+
+    def train_batches(self, n):
+        st = EpPassStats()
+        check(lib().ep_train_batches(self._h, n, ctypes.byref(st)), self._h, "ep_train_batches")
+        return st.as_dict()
+
+    STAGES = ("sample", "forward", "sort", "reduce", "adam", "end")
+
+    def profile_batches(self, n):
+        ms = (ctypes.c_double * len(self.STAGES))()
+        st = EpPassStats()
+        check(lib().ep_profile_batches(self._h, n, ms, ctypes.byref(st)), self._h, "ep_profile_batches")
+        return dict(zip(self.STAGES, list(ms))), st.as_dict()
+
+    @staticmethod
+    def samples(anchors, nbr_ptr, nbr, nbr_w, negatives):
+        arrs = dict(anchors=np.ascontiguousarray(anchors, np.uint32),
+                    nbr_ptr=np.ascontiguousarray(nbr_ptr, np.uint32),
+                    nbr=np.ascontiguousarray(nbr if len(nbr) else [0], np.uint32),
+                    nbr_w=np.ascontiguousarray(nbr_w if len(nbr_w) else [0], np.float32),
+                    negatives=np.ascontiguousarray(negatives, np.uint32).reshape(-1))
+        s = EpBatchSamples(len(arrs["anchors"]), ptr(arrs["anchors"]), ptr(arrs["nbr_ptr"]), ptr(arrs["nbr"]),
+                           ptr(arrs["nbr_w"]), ptr(arrs["negatives"]))
+        return s, arrs   # keep arrays alive with the struct
+
+    def batch_grad(self, samples, n_feat, dims):
+        s, keep = samples
+        B = s.n_anchors
+        ids = np.zeros(n_feat, np.uint32)
+        rows = np.zeros((n_feat, dims), np.float32)
+        loss = np.zeros(B, np.float32)
+        status = np.zeros(B, np.int32)
+        g = EpSparseGrad(n_feat, 0, ptr(ids), ptr(rows), ptr(loss), ptr(status))
+        check(lib().ep_batch_grad(self._h, ctypes.byref(s), ctypes.byref(g)), self._h, "ep_batch_grad")
+        n = g.n_rows
+        return loss, status, ids[:n].copy(), rows[:n].copy()
+
+    def batch_step(self, samples, lr, pass_idx):
+        s, keep = samples
+        check(lib().ep_batch_step(self._h, ctypes.byref(s), float(lr), int(pass_idx)), self._h, "ep_batch_step")
+
+    def ag_forward(self, samples, precision, table_ptr, loss_ptr, stream):
+        s, keep = samples
+        check(lib().ep_ag_forward(self._h, ctypes.byref(s), precision, ctypes.c_void_p(table_ptr),
+                                  ctypes.c_void_p(loss_ptr), ctypes.c_void_p(stream)), self._h, "ep_ag_forward")
+
+    def ag_backward(self, dloss_ptr, grad_ptr, stream):
+        check(lib().ep_ag_backward(self._h, ctypes.c_void_p(dloss_ptr), ctypes.c_void_p(grad_ptr),
+                                   ctypes.c_void_p(stream)), self._h, "ep_ag_backward")
+
+
+def csr_from_edges(src, dst, w, dedup=True):
+    """graph.rs:70-142 through the C ABI.  Returns (rows u64, cols u32, w f32)."""
+    src = np.ascontiguousarray(src, np.uint32)
+    dst = np.ascontiguousarray(dst, np.uint32)
+    w = np.ascontiguousarray(w, np.float32)
+    n = len(src)
+    max_node = int(max(src.max(initial=0), dst.max(initial=0)))
+    rows = np.zeros(max_node + 2, np.uint64)
+    cols = np.zeros(max(n, 1), np.uint32)
+    wo = np.zeros(max(n, 1), np.float32)
+    nn, ne = ctypes.c_uint64(), ctypes.c_uint64()
+    check(lib().ep_csr_from_edges(n, ptr(src), ptr(dst), ptr(w), int(dedup), ptr(rows), ptr(cols), ptr(wo),
+                                  ctypes.byref(nn), ctypes.byref(ne)), None, "ep_csr_from_edges")
+    return rows[: nn.value + 1], cols[: ne.value], wo[: ne.value]
+
+
+def cdf_convert(rows, w):
+    rows = np.ascontiguousarray(rows, np.uint64)
+    w = np.ascontiguousarray(w, np.float32).copy()
+    check(lib().ep_cdf_convert(len(rows) - 1, ptr(rows), ptr(w)), None, "ep_cdf_convert")
+    return w

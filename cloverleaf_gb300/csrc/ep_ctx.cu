@@ -1,0 +1,921 @@
+// ep_ctx.cu -- host driver behind the C ABI declared in include/ep_gb300.h.
+//
+// Owns the device copies of the graph CSR, the feature CSR, the feature table
+// and Adam moments, plus per-batch scratch, and sequences the per-batch
+// kernels (see ep_internal.h) on the context's stream.  In the FUSED form one
+// batch is captured once as a CUDA graph and replayed for every batch of every
+// pass; the kernels read their batch index, step and learning rate from a
+// device-resident BatchState that the last kernel of the batch advances.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ep_gb300.h"
+#include "ep_internal.h"
+
+using namespace ep;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() { if (p) cudaFree(p); }
+    // Grows to at least n bytes (contents not preserved).  Returns false on OOM.
+    bool ensure(size_t n) {
+        if (n <= bytes && p) return true;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (cudaMalloc(&p, n ? n : 16) != cudaSuccess) { cudaGetLastError(); return false; }
+        bytes = n ? n : 16;
+        return true;
+    }
+    template <typename X> X* as() const { return (X*)p; }
+};
+
+uint32_t pick_vpl(uint32_t dims) {
+    const uint32_t need = (dims + 31) / 32;
+    uint32_t v = 1;
+    while (v < need) v <<= 1;
+    return v;
+}
+
+uint32_t bits_for(uint64_t n) {  // bits needed to represent n-1
+    uint32_t b = 0;
+    while (n > 1 && ((n - 1) >> b)) ++b;
+    return b;
+}
+
+}  // namespace
+
+struct ep_ctx {
+    ep_config cfg{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // sizes
+    uint64_t n_nodes = 0, n_edges = 0, n_fids = 0;
+    uint32_t n_feat = 0, max_feat = 0, max_deg = 0;
+    uint32_t dims = 0, dpad = 0, vpl = 1, R = 0, NR = 2, Bcap = 0, Kcap = 0;
+    int tt = TT_F32;
+    bool graph_ok = false, feats_ok = false, table_ok = false, has_w = false;
+
+    // device data
+    DevBuf row, cols, wcdf, fptr, fids, table, m, v, train_ids, valid_ids;
+    uint32_t n_train = 0, n_valid = 0, steps_per_pass = 0;
+    uint64_t total_steps = 0, warmup = 0;
+
+    // per-batch scratch
+    DevBuf st, st_eval, st_inj;
+    DevBuf anchors, nbr, nbr_w, nbr_cnt, neg, occ, dir, scale, valid, loss, status;
+    DevBuf item_f, item_src, item_c, key_alt, idx, idx_alt, hist;
+    DevBuf carry_head, carry_tail, carry_f, carry_flags, gdense, touched, n_touched, packed, xfer, bound;
+    uint64_t items_cap = 0;
+    uint32_t buf_B = 0, buf_K = 0, buf_es = 0;
+    uint32_t chunk = 128;
+    bool prepared = false;
+    cudaGraphExec_t gexec = nullptr;
+    uint32_t* sorted_keys = nullptr;
+    uint32_t* sorted_idx = nullptr;
+    BatchState* h_st = nullptr;   // pinned mirror
+
+    // host-side view of the pass sequence (mirrors the device BatchState)
+    uint32_t host_pass = 1, host_batch = 0;
+    uint64_t launches = 0;   // kernels issued by training batches (graph replays count their kernels)
+    bool state_ok = false;
+
+    // autograd state
+    DevBuf ag_table;
+    int ag_precision = -1;
+    uint32_t ag_n = 0, ag_K = 0;
+    const void* ag_table_ptr = nullptr;
+
+    ~ep_ctx() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (h_st) cudaFreeHost(h_st);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    int fail(int code, const char* fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char* what) {
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? EP_ERR_OOM : EP_ERR_CUDA, "%s: %s", what,
+                    cudaGetErrorString(e));
+    }
+    void drop_graph() {
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    }
+};
+
+static std::string g_create_err;
+
+#define CK(call, what)                                 \
+    do {                                               \
+        cudaError_t e_ = (call);                       \
+        if (e_ != cudaSuccess) return c->cuda_fail(e_, what); \
+    } while (0)
+
+extern "C" void ep_config_default(ep_config* cfg) {
+    if (!cfg) return;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->abi_version = EP_ABI_VERSION;
+    cfg->alpha = 0.9f;
+    cfg->loss = EP_LOSS_MARGIN;
+    cfg->gamma = 1.f;
+    cfg->negatives = 1;
+    cfg->batch_size = 50;
+    cfg->dims = 100;
+    cfg->passes = 100;
+    cfg->seed = 20222022ull;
+    cfg->max_nodes_kind = EP_SAMPLE_ALL;
+    cfg->max_features_kind = EP_SAMPLE_ALL;
+    cfg->loss_weighting = EP_LW_NONE;
+    cfg->loss_weighting_exp = 1.f;
+    cfg->valid_pct = 0.1f;
+    cfg->form = EP_FORM_PLAIN_FP32;
+    cfg->grad_mode = EP_GRAD_REFERENCE;
+    cfg->use_graphs = 1;
+}
+
+extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
+    if (!cfg || !out) { g_create_err = "null argument"; return EP_ERR_INVALID_ARG; }
+    *out = nullptr;
+    if (cfg->abi_version != EP_ABI_VERSION) { g_create_err = "abi_version mismatch"; return EP_ERR_INVALID_ARG; }
+    if (cfg->dims == 0 || cfg->dims > 512) { g_create_err = "dims must be in [1, 512]"; return EP_ERR_INVALID_ARG; }
+    if (cfg->batch_size == 0) { g_create_err = "batch_size must be > 0"; return EP_ERR_INVALID_ARG; }
+    if (cfg->negatives == 0 || cfg->negatives > 1024) { g_create_err = "negatives must be in [1, 1024]"; return EP_ERR_INVALID_ARG; }
+    if (cfg->loss < EP_LOSS_MARGIN || cfg->loss > EP_LOSS_CONTRASTIVE) { g_create_err = "unknown loss"; return EP_ERR_INVALID_ARG; }
+    if (cfg->max_nodes < 0.f || cfg->max_features < 0.f) {
+        g_create_err = "max_nodes / max_features must be either None, or (0, N)";
+        return EP_ERR_INVALID_ARG;
+    }
+    if (cfg->max_nodes_kind == EP_SAMPLE_PROB && !(cfg->max_nodes > 0.f && cfg->max_nodes < 1.f)) {
+        g_create_err = "probability max_nodes must be in (0, 1)";
+        return EP_ERR_INVALID_ARG;
+    }
+    if (cfg->valid_pct < 0.f || cfg->valid_pct >= 1.f) { g_create_err = "valid_pct must be in [0, 1)"; return EP_ERR_INVALID_ARG; }
+    if (cfg->max_features_kind != EP_SAMPLE_ALL) { g_create_err = "max_features sampling is not implemented on the GPU path"; return EP_ERR_UNSUPPORTED; }
+    if (cfg->hard_negatives != 0) { g_create_err = "hard negatives are not implemented on the GPU path"; return EP_ERR_UNSUPPORTED; }
+    if (cfg->noise > 1e-9f) { g_create_err = "gradient noise is not implemented on the GPU path"; return EP_ERR_UNSUPPORTED; }
+    if (cfg->weighted_neighbor_sampling && cfg->weighted_neighbor_averaging) {
+        g_create_err = "weighted neighbour sampling with weighted averaging is not implemented on the GPU path";
+        return EP_ERR_UNSUPPORTED;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        g_create_err = "no CUDA device";
+        return EP_ERR_NO_DEVICE;
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) { g_create_err = "device ordinal out of range"; return EP_ERR_INVALID_ARG; }
+    ep_ctx* c = new ep_ctx();
+    c->cfg = *cfg;
+    c->device = cfg->device;
+    if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost((void**)&c->h_st, sizeof(BatchState)) != cudaSuccess) {
+        g_create_err = std::string("CUDA setup failed: ") + cudaGetErrorString(cudaGetLastError());
+        delete c;
+        return EP_ERR_CUDA;
+    }
+    c->dims = cfg->dims;
+    c->vpl = pick_vpl(cfg->dims);
+    c->dpad = ((cfg->dims + c->vpl - 1) / c->vpl) * c->vpl;
+    c->tt = cfg->form == EP_FORM_FUSED_BF16 ? TT_BF16 : TT_F32;
+    c->R = cfg->negatives;
+    c->NR = c->R + 2;
+    *out = c;
+    return EP_OK;
+}
+
+extern "C" const char* ep_last_error(const ep_ctx* c) { return c ? c->err.c_str() : g_create_err.c_str(); }
+
+extern "C" void ep_destroy(ep_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    delete c;
+}
+
+static int check_csr(ep_ctx* c, uint64_t n, const uint64_t* ptr, const uint32_t* ids, uint64_t id_bound,
+                     const char* what, uint32_t* max_row) {
+    if (ptr[0] != 0) return c->fail(EP_ERR_INVALID_ARG, "%s: row pointer must start at 0", what);
+    uint64_t mx = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        if (ptr[i + 1] < ptr[i]) return c->fail(EP_ERR_INVALID_ARG, "%s: row pointers decrease at row %llu", what, (unsigned long long)i);
+        mx = std::max<uint64_t>(mx, ptr[i + 1] - ptr[i]);
+    }
+    const uint64_t m = ptr[n];
+    for (uint64_t j = 0; j < m; ++j)
+        if (ids[j] >= id_bound) return c->fail(EP_ERR_INVALID_ARG, "%s: id %u at %llu out of range", what, ids[j], (unsigned long long)j);
+    if (mx > 0xffffffffull) return c->fail(EP_ERR_INVALID_ARG, "%s: row too long", what);
+    *max_row = (uint32_t)mx;
+    return EP_OK;
+}
+
+extern "C" int ep_upload_graph(ep_ctx* c, uint64_t n_nodes, const uint64_t* row_ptr, const uint32_t* cols,
+                               const float* w_cdf) {
+    if (!c) return EP_ERR_INVALID_ARG;
+    if (!row_ptr || (!cols && n_nodes && row_ptr[n_nodes])) return c->fail(EP_ERR_INVALID_ARG, "null graph arrays");
+    if (n_nodes == 0 || n_nodes > 0xfffffffeull) return c->fail(EP_ERR_INVALID_ARG, "n_nodes must be in [1, 2^32-1)");
+    if (c->feats_ok && n_nodes != c->n_nodes) return c->fail(EP_ERR_INVALID_ARG, "graph and features disagree on node count");
+    uint32_t mx = 0;
+    int rc = check_csr(c, n_nodes, row_ptr, cols, n_nodes, "graph", &mx);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    const uint64_t E = row_ptr[n_nodes];
+    if (!c->row.ensure((n_nodes + 1) * 8) || !c->cols.ensure(E * 4) || !c->wcdf.ensure(E * 4))
+        return c->fail(EP_ERR_OOM, "graph allocation failed");
+    CK(cudaMemcpyAsync(c->row.p, row_ptr, (n_nodes + 1) * 8, cudaMemcpyHostToDevice, c->stream), "upload row_ptr");
+    if (E) CK(cudaMemcpyAsync(c->cols.p, cols, E * 4, cudaMemcpyHostToDevice, c->stream), "upload cols");
+    if (E && w_cdf) CK(cudaMemcpyAsync(c->wcdf.p, w_cdf, E * 4, cudaMemcpyHostToDevice, c->stream), "upload weights");
+    c->has_w = w_cdf != nullptr;
+    CK(cudaStreamSynchronize(c->stream), "upload graph");
+    c->n_nodes = n_nodes;
+    c->n_edges = E;
+    c->max_deg = mx;
+    c->graph_ok = true;
+    c->prepared = false;
+    c->drop_graph();
+    return EP_OK;
+}
+
+extern "C" int ep_upload_features(ep_ctx* c, uint64_t n_nodes, const uint64_t* fptr, const uint32_t* fids,
+                                  uint32_t n_feat) {
+    if (!c) return EP_ERR_INVALID_ARG;
+    if (!fptr || (!fids && fptr[n_nodes])) return c->fail(EP_ERR_INVALID_ARG, "null feature arrays");
+    if (n_nodes == 0 || n_nodes > 0xfffffffeull) return c->fail(EP_ERR_INVALID_ARG, "n_nodes must be in [1, 2^32-1)");
+    if (c->graph_ok && n_nodes != c->n_nodes) return c->fail(EP_ERR_INVALID_ARG, "graph and features disagree on node count");
+    if (n_feat == 0) return c->fail(EP_ERR_INVALID_ARG, "n_feat must be > 0");
+    uint32_t mx = 0;
+    int rc = check_csr(c, n_nodes, fptr, fids, n_feat, "features", &mx);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    const uint64_t F = fptr[n_nodes];
+    if (!c->fptr.ensure((n_nodes + 1) * 8) || !c->fids.ensure(F * 4)) return c->fail(EP_ERR_OOM, "feature allocation failed");
+    CK(cudaMemcpyAsync(c->fptr.p, fptr, (n_nodes + 1) * 8, cudaMemcpyHostToDevice, c->stream), "upload fptr");
+    if (F) CK(cudaMemcpyAsync(c->fids.p, fids, F * 4, cudaMemcpyHostToDevice, c->stream), "upload fids");
+    CK(cudaStreamSynchronize(c->stream), "upload features");
+    if (c->table_ok && n_feat != c->n_feat) c->table_ok = false;
+    c->n_nodes = n_nodes;
+    c->n_fids = F;
+    c->n_feat = n_feat;
+    c->max_feat = mx;
+    c->feats_ok = true;
+    c->prepared = false;
+    c->drop_graph();
+    return EP_OK;
+}
+
+// Zeroes the Adam moments and restarts the pass sequence at pass 1, step 1.
+static int reset_state(ep_ctx* c) {
+    const size_t mv = (size_t)c->n_feat * c->dpad * sizeof(float);
+    CK(cudaMemsetAsync(c->m.p, 0, mv, c->stream), "reset moments");
+    CK(cudaMemsetAsync(c->v.p, 0, mv, c->stream), "reset moments");
+    BatchState h{};
+    h.pass = 1;
+    h.batch = 0;
+    h.step = 1;
+    *c->h_st = h;
+    if (!c->st.ensure(sizeof(BatchState)) || !c->st_eval.ensure(sizeof(BatchState)) || !c->st_inj.ensure(sizeof(BatchState)))
+        return c->fail(EP_ERR_OOM, "state allocation failed");
+    CK(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(BatchState), cudaMemcpyHostToDevice, c->stream), "reset state");
+    CK(cudaStreamSynchronize(c->stream), "reset state");
+    c->host_pass = 1;
+    c->host_batch = 0;
+    c->state_ok = true;
+    return EP_OK;
+}
+
+extern "C" int ep_set_table(ep_ctx* c, const float* init) {
+    if (!c) return EP_ERR_INVALID_ARG;
+    if (!c->feats_ok) return c->fail(EP_ERR_STATE, "upload features before setting the table");
+    cudaSetDevice(c->device);
+    const size_t es = c->tt == TT_BF16 ? 2 : 4;
+    const size_t rows = (size_t)c->n_feat * c->dpad;
+    if (!c->table.ensure(rows * es) || !c->m.ensure(rows * 4) || !c->v.ensure(rows * 4))
+        return c->fail(EP_ERR_OOM, "table allocation failed (%zu rows)", (size_t)c->n_feat);
+    if (init) {
+        const size_t dense = (size_t)c->n_feat * c->dims * 4;
+        if (!c->xfer.ensure(dense)) return c->fail(EP_ERR_OOM, "staging allocation failed");
+        CK(cudaMemcpyAsync(c->xfer.p, init, dense, cudaMemcpyHostToDevice, c->stream), "upload table");
+        launch_convert_table(c->tt, c->table.p, c->xfer.as<float>(), c->n_feat, c->dims, c->dpad, 1, c->stream);
+    } else {
+        launch_init_table(c->tt, c->table.p, c->n_feat, c->dims, c->dpad, c->cfg.seed, c->stream);
+    }
+    CK(cudaGetLastError(), "table init");
+    c->table_ok = true;
+    c->drop_graph();
+    return reset_state(c);
+}
+
+extern "C" int ep_get_table(ep_ctx* c, float* out) {
+    if (!c || !out) return EP_ERR_INVALID_ARG;
+    if (!c->table_ok) return c->fail(EP_ERR_STATE, "no table");
+    cudaSetDevice(c->device);
+    const size_t dense = (size_t)c->n_feat * c->dims * 4;
+    if (!c->xfer.ensure(dense)) return c->fail(EP_ERR_OOM, "staging allocation failed");
+    launch_convert_table(c->tt, c->table.p, c->xfer.as<float>(), c->n_feat, c->dims, c->dpad, 0, c->stream);
+    CK(cudaGetLastError(), "table download");
+    CK(cudaMemcpyAsync(out, c->xfer.p, dense, cudaMemcpyDeviceToHost, c->stream), "download table");
+    CK(cudaStreamSynchronize(c->stream), "download table");
+    return EP_OK;
+}
+
+// (Re)allocates per-batch scratch for B anchors, K neighbour slots, `items`
+// gradient items and accumulator element size es.
+static int ensure_bufs(ep_ctx* c, uint32_t B, uint32_t K, uint64_t items, uint32_t es, bool dense) {
+    K = std::max<uint32_t>(K, 1);
+    items = std::max<uint64_t>(items, 1);
+    bool grow = B > c->buf_B || K > c->buf_K || items > c->items_cap || es > c->buf_es;
+    if (grow) {
+        B = std::max(B, c->buf_B);
+        K = std::max(K, c->buf_K);
+        items = std::max(items, c->items_cap);
+        es = std::max(es, c->buf_es);
+        const uint64_t NR = c->NR;
+        const uint32_t nch = reduce_chunks(items, c->chunk);
+        bool ok = c->anchors.ensure((size_t)B * 4) && c->nbr.ensure((size_t)B * K * 4) && c->nbr_w.ensure((size_t)B * K * 4) &&
+                  c->nbr_cnt.ensure((size_t)B * 4) && c->neg.ensure((size_t)B * c->R * 4) && c->occ.ensure(((size_t)B + 1) * 4) &&
+                  c->dir.ensure((size_t)B * NR * c->dpad * es) && c->scale.ensure((size_t)B * NR * es) &&
+                  c->valid.ensure((size_t)B * NR) && c->loss.ensure((size_t)B * es) && c->status.ensure((size_t)B * 4) &&
+                  c->item_f.ensure(items * 4) && c->item_src.ensure(items * 4) && c->item_c.ensure(items * 4) &&
+                  c->key_alt.ensure(items * 4) && c->idx.ensure(items * 4) && c->idx_alt.ensure(items * 4) &&
+                  c->hist.ensure(radix_hist_entries(items) * 4) && c->carry_head.ensure((size_t)nch * c->dpad * es) &&
+                  c->carry_tail.ensure((size_t)nch * c->dpad * es) && c->carry_f.ensure((size_t)nch * 4) &&
+                  c->carry_flags.ensure((size_t)nch * 4) && c->n_touched.ensure(4);
+        if (!ok) return c->fail(EP_ERR_OOM, "batch scratch allocation failed (B=%u K=%u items=%llu)", B, K, (unsigned long long)items);
+        c->buf_B = B;
+        c->buf_K = K;
+        c->items_cap = items;
+        c->buf_es = es;
+        c->drop_graph();
+        // the sampling kernel reads nbr_cnt for every anchor slot
+        CK(cudaMemsetAsync(c->nbr_cnt.p, 0, (size_t)B * 4, c->stream), "clear scratch");
+    }
+    if (dense) {
+        const size_t rows = (size_t)c->n_feat * c->dpad * c->buf_es;
+        const size_t tcap = (size_t)std::min<uint64_t>(c->n_feat, c->items_cap) * 4;
+        if (!c->gdense.ensure(rows) || !c->touched.ensure(tcap)) return c->fail(EP_ERR_OOM, "dense gradient allocation failed");
+    }
+    return EP_OK;
+}
+
+static uint32_t feistel_half(uint64_t n) {
+    const uint32_t b = bits_for(n);
+    return (b + 1) / 2 ? (b + 1) / 2 : 1;
+}
+
+static int prepare_train(ep_ctx* c) {
+    if (!c->graph_ok || !c->feats_ok) return c->fail(EP_ERR_STATE, "upload the graph and the features first");
+    if (!c->table_ok) return c->fail(EP_ERR_STATE, "set the table first");
+    if (c->prepared) return EP_OK;
+    const uint32_t n = (uint32_t)c->n_nodes;
+    c->n_valid = (uint32_t)((float)n * c->cfg.valid_pct);   // mod.rs:121
+    c->n_train = n - c->n_valid;
+    if (c->n_train == 0) return c->fail(EP_ERR_INVALID_ARG, "no training nodes");
+    if (!c->train_ids.ensure((size_t)c->n_train * 4) || !c->valid_ids.ensure((size_t)std::max<uint32_t>(c->n_valid, 1) * 4))
+        return c->fail(EP_ERR_OOM, "id allocation failed");
+    if (!c->st.ensure(sizeof(BatchState))) return c->fail(EP_ERR_OOM, "state allocation failed");
+    // split: reuse the error word of the main state (cleared by reset_state)
+    launch_split(c->train_ids.as<uint32_t>(), c->n_train, c->valid_ids.as<uint32_t>(), n, c->cfg.seed,
+                 feistel_half(n), &c->st.as<BatchState>()->error, c->stream);
+    const uint32_t B = c->cfg.batch_size;
+    c->steps_per_pass = (uint32_t)((c->n_train + (uint64_t)B - 1) / B);
+    const uint64_t steps_f = (uint64_t)ceilf((float)c->n_train / (float)B);   // mod.rs:125
+    c->total_steps = steps_f * c->cfg.passes;
+    c->warmup = (uint64_t)((float)c->total_steps / 5.f);                        // mod.rs:134
+    uint32_t K = c->max_deg;
+    if (c->cfg.max_nodes_kind == EP_SAMPLE_FIXED) K = std::min<uint32_t>((uint32_t)c->cfg.max_nodes, c->max_deg);
+    // item bound: sum of the B largest per-anchor bounds
+    if (!c->bound.ensure((size_t)n * 4)) return c->fail(EP_ERR_OOM, "bound allocation failed");
+    launch_node_bound(c->row.as<uint64_t>(), c->cols.as<uint32_t>(), c->fptr.as<uint64_t>(), n, c->cfg.max_nodes_kind,
+                      (uint32_t)c->cfg.max_nodes, c->R, c->max_feat, c->bound.as<uint32_t>(), c->stream);
+    std::vector<uint32_t> hb(n);
+    CK(cudaMemcpyAsync(hb.data(), c->bound.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream), "bounds");
+    CK(cudaStreamSynchronize(c->stream), "bounds");
+    const uint32_t top = std::min<uint32_t>(B, n);
+    std::nth_element(hb.begin(), hb.begin() + (top - 1), hb.end(), std::greater<uint32_t>());
+    uint64_t items = 0;
+    for (uint32_t i = 0; i < top; ++i) items += hb[i];
+    if (items > 0xfffffff0ull) return c->fail(EP_ERR_UNSUPPORTED, "a batch can emit more than 2^32 gradient items");
+    int rc = ensure_bufs(c, B, K, items, 4, c->cfg.form == EP_FORM_PLAIN_FP32);
+    if (rc) return rc;
+    c->Bcap = B;
+    c->Kcap = c->buf_K;
+    c->prepared = true;
+    return EP_OK;
+}
+
+static SampleParams sample_params(ep_ctx* c, BatchState* st, bool eval, bool injected) {
+    SampleParams sp{};
+    sp.st = st;
+    sp.cfg.nodes_kind = c->cfg.max_nodes_kind;
+    sp.cfg.nodes_val = c->cfg.max_nodes;
+    sp.cfg.K = (uint32_t)c->cfg.max_nodes;
+    sp.cfg.Kcap = c->buf_K;
+    sp.cfg.R = c->R;
+    sp.cfg.weighted_avg = c->cfg.weighted_neighbor_averaging;
+    sp.cfg.feat_scalar = 1.f;
+    sp.cfg.seed = c->cfg.seed;
+    sp.row_ptr = c->row.as<uint64_t>();
+    sp.cols = c->cols.as<uint32_t>();
+    sp.wcdf = c->has_w ? c->wcdf.as<float>() : nullptr;
+    sp.fptr = c->fptr.as<uint64_t>();
+    sp.order = eval ? c->valid_ids.as<uint32_t>() : c->train_ids.as<uint32_t>();
+    sp.n_order = eval ? c->n_valid : c->n_train;
+    sp.pool = sp.order;
+    sp.n_pool = sp.n_order;
+    sp.batch_cap = injected ? c->buf_B : c->Bcap;
+    sp.injected = injected;
+    sp.eval = eval;
+    sp.feistel_half = feistel_half(sp.n_order);
+    sp.anchors = c->anchors.as<uint32_t>();
+    sp.nbr = c->nbr.as<uint32_t>();
+    sp.nbr_w = c->nbr_w.as<float>();
+    sp.nbr_cnt = c->nbr_cnt.as<uint32_t>();
+    sp.neg = c->neg.as<uint32_t>();
+    sp.occ = c->occ.as<uint32_t>();
+    return sp;
+}
+
+static ForwardParams forward_params(ep_ctx* c, BatchState* st, const void* table, bool emit, bool eval) {
+    ForwardParams fp{};
+    fp.st = st;
+    fp.loss = c->cfg.loss;
+    fp.gamma = c->cfg.gamma;
+    fp.neg_margin = c->cfg.neg_margin;
+    fp.loss_weighting = eval ? EP_LW_NONE : c->cfg.loss_weighting;   // validation reports the raw loss
+    fp.lw_exp = c->cfg.loss_weighting_exp;
+    fp.feat_scalar = 1.f;
+    fp.R = c->R;
+    fp.Kcap = c->buf_K;
+    fp.dims = c->dims;
+    fp.dpad = c->dpad;
+    fp.row_ptr = c->row.as<uint64_t>();
+    fp.fptr = c->fptr.as<uint64_t>();
+    fp.fids = c->fids.as<uint32_t>();
+    fp.table = table;
+    fp.anchors = c->anchors.as<uint32_t>();
+    fp.nbr = c->nbr.as<uint32_t>();
+    fp.nbr_w = c->nbr_w.as<float>();
+    fp.nbr_cnt = c->nbr_cnt.as<uint32_t>();
+    fp.neg = c->neg.as<uint32_t>();
+    fp.occ_off = c->occ.as<uint32_t>();
+    fp.emit = emit;
+    fp.items_cap = c->items_cap;
+    fp.dir = c->dir.p;
+    fp.scale = c->scale.p;
+    fp.valid = c->valid.as<uint8_t>();
+    fp.loss_out = c->loss.p;
+    fp.status = c->status.as<int32_t>();
+    fp.item_f = c->item_f.as<uint32_t>();
+    fp.item_src = c->item_src.as<uint32_t>();
+    fp.item_c = c->item_c.as<float>();
+    return fp;
+}
+
+static ReduceParams reduce_params(ep_ctx* c, BatchState* st, int out_mode, void* table) {
+    ReduceParams rp{};
+    rp.st = st;
+    rp.NR = c->NR;
+    rp.dpad = c->dpad;
+    rp.chunk = c->chunk;
+    rp.grad_true = c->cfg.grad_mode == EP_GRAD_TRUE;
+    rp.out_mode = out_mode;
+    rp.skey = c->sorted_keys;
+    rp.sidx = c->sorted_idx;
+    rp.item_src = c->item_src.as<uint32_t>();
+    rp.item_c = c->item_c.as<float>();
+    rp.dir = c->dir.p;
+    rp.scale = c->scale.p;
+    rp.valid = c->valid.as<uint8_t>();
+    rp.table = table;
+    rp.m = c->m.as<float>();
+    rp.v = c->v.as<float>();
+    rp.seed = c->cfg.seed;
+    rp.gdense = c->gdense.p;
+    rp.touched = c->touched.as<uint32_t>();
+    rp.n_touched = c->n_touched.as<uint32_t>();
+    rp.carry_head = c->carry_head.p;
+    rp.carry_tail = c->carry_tail.p;
+    rp.carry_f = c->carry_f.as<uint32_t>();
+    rp.carry_flags = c->carry_flags.as<uint32_t>();
+    return rp;
+}
+
+// Sort the emitted items and reduce them; tt selects the kernel family.
+static void sort_and_reduce(ep_ctx* c, BatchState* st, int tt, int out_mode, void* table, cudaStream_t s) {
+    launch_radix_sort(st, c->item_f.as<uint32_t>(), c->key_alt.as<uint32_t>(), c->idx.as<uint32_t>(),
+                      c->idx_alt.as<uint32_t>(), c->hist.as<uint32_t>(), c->items_cap, (int)bits_for(c->n_feat),
+                      &c->sorted_keys, &c->sorted_idx, s);
+    if (out_mode == OUT_DENSE) cudaMemsetAsync(c->n_touched.p, 0, 4, s);
+    ReduceParams rp = reduce_params(c, st, out_mode, table);
+    launch_reduce(tt, (int)c->vpl, rp, c->items_cap, s);
+}
+
+// Kernels launched per training batch.
+static uint32_t kernels_per_batch(const ep_ctx* c) {
+    const uint32_t b = bits_for(c->n_feat);
+    const uint32_t radix = 3 * (b ? (b + 7) / 8 : 1);
+    return 3 /* begin, sample, scan */ + 1 /* forward */ + radix + 2 /* reduce, fixup */ +
+           (c->cfg.form == EP_FORM_PLAIN_FP32 ? 1 : 0) + 1 /* end */;
+}
+
+// Issues one training batch on the context stream; ev (optional) receives an
+// event record after each stage (EP_N_STAGES events).
+static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr) {
+    BatchState* st = c->st.as<BatchState>();
+    cudaStream_t s = c->stream;
+    launch_batch_begin(st, c->n_train, c->Bcap, c->steps_per_pass, c->total_steps, c->warmup, c->cfg.alpha, 0, s);
+    SampleParams sp = sample_params(c, st, false, false);
+    launch_sample(sp, s);
+    launch_scan_occ(st, c->occ.as<uint32_t>(), c->Bcap, c->items_cap, s);
+    if (ev) cudaEventRecord(ev[EP_STAGE_SAMPLE], s);
+    ForwardParams fp = forward_params(c, st, c->table.p, true, false);
+    launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, s);
+    if (ev) cudaEventRecord(ev[EP_STAGE_FORWARD], s);
+    launch_radix_sort(st, c->item_f.as<uint32_t>(), c->key_alt.as<uint32_t>(), c->idx.as<uint32_t>(),
+                      c->idx_alt.as<uint32_t>(), c->hist.as<uint32_t>(), c->items_cap, (int)bits_for(c->n_feat),
+                      &c->sorted_keys, &c->sorted_idx, s);
+    if (ev) cudaEventRecord(ev[EP_STAGE_SORT], s);
+    const bool plain = c->cfg.form == EP_FORM_PLAIN_FP32;
+    if (plain) cudaMemsetAsync(c->n_touched.p, 0, 4, s);
+    ReduceParams rp = reduce_params(c, st, plain ? OUT_DENSE : OUT_ADAM, c->table.p);
+    launch_reduce(c->tt, (int)c->vpl, rp, c->items_cap, s);
+    if (ev) cudaEventRecord(ev[EP_STAGE_REDUCE], s);
+    if (plain)
+        launch_adam_dense(c->tt, (int)c->vpl, st, c->table.p, c->m.as<float>(), c->v.as<float>(), c->gdense.as<float>(),
+                          c->touched.as<uint32_t>(), c->n_touched.as<uint32_t>(), c->dpad,
+                          (uint32_t)std::min<uint64_t>(c->n_feat, c->items_cap), c->cfg.seed, s);
+    if (ev) cudaEventRecord(ev[EP_STAGE_ADAM], s);
+    launch_batch_end(st, c->loss.p, c->status.as<int32_t>(), c->nbr_cnt.as<uint32_t>(), c->Bcap, c->steps_per_pass, 0, 0, s);
+    if (ev) cudaEventRecord(ev[EP_STAGE_END], s);
+    c->launches += kernels_per_batch(c);
+}
+
+static int launch_train_batch(ep_ctx* c) {
+    const bool use_graph = c->cfg.use_graphs && c->cfg.form == EP_FORM_FUSED_BF16;
+    if (use_graph) {
+        if (!c->gexec) {
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+            const uint64_t before = c->launches;
+            issue_train_batch(c);
+            c->launches = before;
+            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+            if (e != cudaSuccess) return c->cuda_fail(e, "graph capture");
+            e = cudaGraphInstantiate(&c->gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { c->gexec = nullptr; return c->cuda_fail(e, "graph instantiate"); }
+        }
+        CK(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
+        c->launches += kernels_per_batch(c);
+    } else {
+        issue_train_batch(c);
+        CK(cudaGetLastError(), "batch launch");
+    }
+    if (++c->host_batch >= c->steps_per_pass) { c->host_batch = 0; ++c->host_pass; }
+    return EP_OK;
+}
+
+// Validation pass over the held-out ids (mod.rs:267-283): forward only, fixed
+// sampling stream, negatives from the validation ids.
+static int run_validation(ep_ctx* c, double* mean_out) {
+    *mean_out = NAN;
+    if (c->n_valid == 0) return EP_OK;
+    BatchState h{};
+    h.pass = 1;
+    h.step = 1;
+    BatchState* st = c->st_eval.as<BatchState>();
+    CK(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream), "eval state");
+    const uint32_t nb = (c->n_valid + c->Bcap - 1) / c->Bcap;
+    for (uint32_t b = 0; b < nb; ++b) {
+        launch_batch_begin(st, c->n_valid, c->Bcap, nb, 1, 0, c->cfg.alpha, 0, c->stream);
+        SampleParams sp = sample_params(c, st, true, false);
+        launch_sample(sp, c->stream);
+        ForwardParams fp = forward_params(c, st, c->table.p, false, true);
+        launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, c->stream);
+        launch_batch_end(st, c->loss.p, c->status.as<int32_t>(), c->nbr_cnt.as<uint32_t>(), c->Bcap, nb, 1, 0, c->stream);
+    }
+    CK(cudaGetLastError(), "validation launch");
+    CK(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "eval state");
+    CK(cudaStreamSynchronize(c->stream), "validation");
+    *mean_out = h.valid_sum / (double)c->n_valid;
+    return EP_OK;
+}
+
+static int clear_accumulators(ep_ctx* c) {
+    c->launches = 0;
+    const size_t off = offsetof(BatchState, pass_err_sum);
+    CK(cudaMemsetAsync((char*)c->st.p + off, 0, sizeof(BatchState) - off, c->stream), "clear counters");
+    return EP_OK;
+}
+
+static int read_state(ep_ctx* c) {
+    CK(cudaMemcpyAsync(c->h_st, c->st.p, sizeof(BatchState), cudaMemcpyDeviceToHost, c->stream), "read state");
+    CK(cudaStreamSynchronize(c->stream), "batch execution");
+    if (c->h_st->error) return c->fail(EP_ERR_DEVICE, "device error flags 0x%x", c->h_st->error);
+    return EP_OK;
+}
+
+static void fill_stats(ep_ctx* c, ep_pass_stats* s, uint32_t pass, double ms, double valid) {
+    const BatchState& h = *c->h_st;
+    memset(s, 0, sizeof(*s));
+    s->pass = pass;
+    s->batches = h.pass_batches;
+    s->train_loss = h.pass_batches ? (float)(h.pass_err_sum / (double)h.pass_batches) : 0.f;
+    s->valid_loss = (float)valid;
+    s->lr_last = h.lr;
+    s->anchors = h.anchors;
+    s->kept_anchors = h.kept;
+    s->nan_anchors = h.nan_anchors;
+    s->items = h.items;
+    s->gathered_rows = h.gathered;
+    s->unique_rows = h.unique_rows;
+    s->sampled_neighbors = h.sampled;
+    s->ms = ms;
+    const double d = c->dims, es = c->tt == TT_BF16 ? 2.0 : 4.0;
+    s->alg_bytes = (double)h.gathered * d * es + (double)h.unique_rows * d * (2 * es + 16) + 4.0 * h.gathered +
+                   4.0 * h.sampled + 8.0 * (double)h.anchors * (c->R + 2);
+    s->launches = c->launches;
+}
+
+extern "C" int ep_train(ep_ctx* c, ep_pass_stats* stats, uint32_t stats_len) {
+    if (!c) return EP_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    int rc = prepare_train(c);
+    if (rc) return rc;
+    rc = reset_state(c);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (uint32_t pass = 1; pass <= c->cfg.passes; ++pass) {
+        if ((rc = clear_accumulators(c))) break;
+        cudaEventRecord(e0, c->stream);
+        for (uint32_t b = 0; b < c->steps_per_pass; ++b)
+            if ((rc = launch_train_batch(c))) break;
+        if (rc) break;
+        cudaEventRecord(e1, c->stream);
+        if ((rc = read_state(c))) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        double valid = NAN;
+        if ((rc = run_validation(c, &valid))) break;
+        if (stats && pass <= stats_len) fill_stats(c, &stats[pass - 1], pass, ms, valid);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+extern "C" int ep_train_batches(ep_ctx* c, uint32_t n_batches, ep_pass_stats* stats) {
+    if (!c) return EP_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    int rc = prepare_train(c);
+    if (rc) return rc;
+    if (!c->state_ok && (rc = reset_state(c))) return rc;
+    if ((rc = clear_accumulators(c))) return rc;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, c->stream);
+    for (uint32_t i = 0; i < n_batches && !rc; ++i) rc = launch_train_batch(c);
+    cudaEventRecord(e1, c->stream);
+    if (!rc) rc = read_state(c);
+    float ms = 0.f;
+    if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!rc && stats) fill_stats(c, stats, c->host_pass, ms, NAN);
+    return rc;
+}
+
+extern "C" int ep_profile_batches(ep_ctx* c, uint32_t n_batches, double* stage_ms, ep_pass_stats* stats) {
+    if (!c || !stage_ms) return EP_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    int rc = prepare_train(c);
+    if (rc) return rc;
+    if (!c->state_ok && (rc = reset_state(c))) return rc;
+    if ((rc = clear_accumulators(c))) return rc;
+    std::vector<cudaEvent_t> ev((size_t)n_batches * EP_N_STAGES + 1);
+    for (auto& e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], c->stream);
+    for (uint32_t b = 0; b < n_batches; ++b) {
+        issue_train_batch(c, &ev[1 + (size_t)b * EP_N_STAGES]);
+        if (++c->host_batch >= c->steps_per_pass) { c->host_batch = 0; ++c->host_pass; }
+    }
+    rc = read_state(c);
+    for (int k = 0; k < EP_N_STAGES; ++k) stage_ms[k] = 0.0;
+    double total = 0.0;
+    if (!rc) {
+        for (uint32_t b = 0; b < n_batches; ++b)
+            for (int k = 0; k < EP_N_STAGES; ++k) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ev[(size_t)b * EP_N_STAGES + k], ev[1 + (size_t)b * EP_N_STAGES + k]);
+                stage_ms[k] += ms;
+                total += ms;
+            }
+        for (int k = 0; k < EP_N_STAGES; ++k) stage_ms[k] /= n_batches ? n_batches : 1;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (!rc && stats) fill_stats(c, stats, c->host_pass, total, NAN);
+    return rc;
+}
+
+extern "C" int ep_synchronize(ep_ctx* c) {
+    if (!c) return EP_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    if (c->state_ok) return read_state(c);
+    return EP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Explicit-sample paths (parity hooks and the autograd binding)
+// ---------------------------------------------------------------------------
+static int stage_samples(ep_ctx* c, const ep_batch_samples* sm, uint32_t es, cudaStream_t s) {
+    if (!sm || !sm->anchors || !sm->nbr_ptr || !sm->negatives) return c->fail(EP_ERR_INVALID_ARG, "null sample arrays");
+    if (!c->graph_ok || !c->feats_ok) return c->fail(EP_ERR_STATE, "upload the graph and the features first");
+    const uint32_t B = sm->n_anchors;
+    if (B == 0) return c->fail(EP_ERR_INVALID_ARG, "empty batch");
+    uint32_t K = 1;
+    for (uint32_t a = 0; a < B; ++a) {
+        if (sm->nbr_ptr[a + 1] < sm->nbr_ptr[a]) return c->fail(EP_ERR_INVALID_ARG, "nbr_ptr decreases at %u", a);
+        K = std::max(K, sm->nbr_ptr[a + 1] - sm->nbr_ptr[a]);
+        if (sm->anchors[a] >= c->n_nodes) return c->fail(EP_ERR_INVALID_ARG, "anchor id out of range");
+    }
+    const uint32_t nn = sm->nbr_ptr[B];
+    if (nn && (!sm->nbr || !sm->nbr_w)) return c->fail(EP_ERR_INVALID_ARG, "null neighbour arrays");
+    for (uint32_t j = 0; j < nn; ++j)
+        if (sm->nbr[j] >= c->n_nodes) return c->fail(EP_ERR_INVALID_ARG, "neighbour id out of range");
+    for (uint64_t j = 0; j < (uint64_t)B * c->R; ++j)
+        if (sm->negatives[j] >= c->n_nodes) return c->fail(EP_ERR_INVALID_ARG, "negative id out of range");
+    const uint64_t items = (uint64_t)B * c->max_feat * (1ull + c->R + K);
+    int rc = ensure_bufs(c, B, K, items, es, true);
+    if (rc) return rc;
+    const uint32_t Ks = c->buf_K;
+    std::vector<uint32_t> nb((size_t)B * Ks, 0u), cnt(B);
+    std::vector<float> nw((size_t)B * Ks, 0.f);
+    for (uint32_t a = 0; a < B; ++a) {
+        cnt[a] = sm->nbr_ptr[a + 1] - sm->nbr_ptr[a];
+        for (uint32_t j = 0; j < cnt[a]; ++j) {
+            nb[(size_t)a * Ks + j] = sm->nbr[sm->nbr_ptr[a] + j];
+            nw[(size_t)a * Ks + j] = sm->nbr_w[sm->nbr_ptr[a] + j];
+        }
+    }
+    CK(cudaMemcpyAsync(c->anchors.p, sm->anchors, (size_t)B * 4, cudaMemcpyHostToDevice, s), "stage anchors");
+    CK(cudaMemcpyAsync(c->nbr.p, nb.data(), nb.size() * 4, cudaMemcpyHostToDevice, s), "stage neighbours");
+    CK(cudaMemcpyAsync(c->nbr_w.p, nw.data(), nw.size() * 4, cudaMemcpyHostToDevice, s), "stage weights");
+    CK(cudaMemcpyAsync(c->nbr_cnt.p, cnt.data(), (size_t)B * 4, cudaMemcpyHostToDevice, s), "stage counts");
+    CK(cudaMemcpyAsync(c->neg.p, sm->negatives, (size_t)B * c->R * 4, cudaMemcpyHostToDevice, s), "stage negatives");
+    CK(cudaStreamSynchronize(s), "stage samples");   // host vectors go out of scope
+    return EP_OK;
+}
+
+// Runs count -> scan -> forward -> sort -> reduce for staged samples.
+static int run_injected(ep_ctx* c, uint32_t B, int tt, const void* table, void* loss_out, const void* dloss,
+                        int out_mode, void* adam_table, float lr, uint32_t pass, cudaStream_t s) {
+    BatchState h{};
+    h.pass = pass;
+    h.step = 1;
+    h.n_anchors = B;
+    h.lr = lr;
+    h.bc1 = 1.f - powf(0.9f, (float)pass + 1.f);
+    h.bc2 = 1.f - powf(0.999f, (float)pass + 1.f);
+    BatchState* st = c->st_inj.as<BatchState>();
+    if (!c->st_inj.ensure(sizeof(BatchState))) return c->fail(EP_ERR_OOM, "state allocation failed");
+    st = c->st_inj.as<BatchState>();
+    CK(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s), "inject state");
+    SampleParams sp = sample_params(c, st, false, true);
+    launch_sample(sp, s);
+    launch_scan_occ(st, c->occ.as<uint32_t>(), B, c->items_cap, s);
+    ForwardParams fp = forward_params(c, st, table, true, false);
+    fp.loss_out = loss_out;
+    fp.dloss = (const float*)dloss;
+    fp.dloss_f64 = tt == TT_F64;
+    launch_forward(tt, (int)c->vpl, fp, B, s);
+    sort_and_reduce(c, st, tt, out_mode, adam_table, s);
+    if (out_mode == OUT_DENSE && adam_table)
+        launch_adam_dense(tt, (int)c->vpl, st, adam_table, c->m.as<float>(), c->v.as<float>(), c->gdense.as<float>(),
+                          c->touched.as<uint32_t>(), c->n_touched.as<uint32_t>(), c->dpad,
+                          (uint32_t)std::min<uint64_t>(c->n_feat, c->items_cap), c->cfg.seed, s);
+    CK(cudaGetLastError(), "injected batch launch");
+    CK(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s), "read state");
+    CK(cudaStreamSynchronize(s), "injected batch");
+    if (h.error) return c->fail(EP_ERR_DEVICE, "device error flags 0x%x", h.error);
+    return EP_OK;
+}
+
+extern "C" int ep_batch_grad(ep_ctx* c, const ep_batch_samples* sm, ep_sparse_grad* out) {
+    if (!c || !out) return EP_ERR_INVALID_ARG;
+    if (!c->table_ok) return c->fail(EP_ERR_STATE, "set the table first");
+    cudaSetDevice(c->device);
+    int rc = stage_samples(c, sm, 4, c->stream);
+    if (rc) return rc;
+    const uint32_t B = sm->n_anchors;
+    rc = run_injected(c, B, c->tt, c->table.p, c->loss.p, nullptr, OUT_DENSE, nullptr, 0.f, 1, c->stream);
+    if (rc) return rc;
+    uint32_t nt = 0;
+    CK(cudaMemcpy(&nt, c->n_touched.p, 4, cudaMemcpyDeviceToHost), "read touched count");
+    out->n_rows = nt;
+    if (out->loss) CK(cudaMemcpy(out->loss, c->loss.p, (size_t)B * 4, cudaMemcpyDeviceToHost), "read loss");
+    if (out->status) CK(cudaMemcpy(out->status, c->status.p, (size_t)B * 4, cudaMemcpyDeviceToHost), "read status");
+    if (nt > out->capacity) return c->fail(EP_ERR_INVALID_ARG, "gradient has %u rows, capacity %u", nt, out->capacity);
+    if (nt == 0) return EP_OK;
+    if (!c->packed.ensure((size_t)nt * c->dims * 4)) return c->fail(EP_ERR_OOM, "pack allocation failed");
+    launch_pack_rows(4, c->gdense.p, c->touched.as<uint32_t>(), c->n_touched.as<uint32_t>(), c->dpad, c->dims, c->packed.p,
+                     0, nt, c->stream);
+    std::vector<uint32_t> ids(nt);
+    std::vector<float> rows((size_t)nt * c->dims);
+    CK(cudaMemcpyAsync(ids.data(), c->touched.p, (size_t)nt * 4, cudaMemcpyDeviceToHost, c->stream), "read ids");
+    CK(cudaMemcpyAsync(rows.data(), c->packed.p, rows.size() * 4, cudaMemcpyDeviceToHost, c->stream), "read rows");
+    CK(cudaStreamSynchronize(c->stream), "read gradient");
+    // ascending feature order (the device list order depends on scheduling)
+    std::vector<uint32_t> ord(nt);
+    for (uint32_t i = 0; i < nt; ++i) ord[i] = i;
+    std::sort(ord.begin(), ord.end(), [&](uint32_t x, uint32_t y) { return ids[x] < ids[y]; });
+    for (uint32_t i = 0; i < nt; ++i) {
+        out->feat_ids[i] = ids[ord[i]];
+        memcpy(out->rows + (size_t)i * c->dims, rows.data() + (size_t)ord[i] * c->dims, (size_t)c->dims * 4);
+    }
+    return EP_OK;
+}
+
+extern "C" int ep_batch_step(ep_ctx* c, const ep_batch_samples* sm, float lr, uint32_t pass) {
+    if (!c) return EP_ERR_INVALID_ARG;
+    if (!c->table_ok) return c->fail(EP_ERR_STATE, "set the table first");
+    cudaSetDevice(c->device);
+    int rc = stage_samples(c, sm, 4, c->stream);
+    if (rc) return rc;
+    if (c->cfg.form == EP_FORM_PLAIN_FP32)
+        return run_injected(c, sm->n_anchors, c->tt, c->table.p, c->loss.p, nullptr, OUT_DENSE, c->table.p, lr, pass, c->stream);
+    return run_injected(c, sm->n_anchors, c->tt, c->table.p, c->loss.p, nullptr, OUT_ADAM, c->table.p, lr, pass, c->stream);
+}
+
+// autograd: the caller's dense table (n_feat x dims) is copied into the padded
+// device layout when dims is not a multiple of the lane width.
+static int ag_prepare(ep_ctx* c, const ep_batch_samples* sm, int precision, const void* table_dev, cudaStream_t s) {
+    if (!c->graph_ok || !c->feats_ok) return c->fail(EP_ERR_STATE, "upload the graph and the features first");
+    if (precision != 0 && precision != 1) return c->fail(EP_ERR_INVALID_ARG, "precision must be 0 or 1");
+    const uint32_t es = precision ? 8 : 4;
+    int rc = stage_samples(c, sm, es, s);
+    if (rc) return rc;
+    c->ag_precision = precision;
+    c->ag_n = sm->n_anchors;
+    if (c->dims == c->dpad && ((uintptr_t)table_dev % 16) == 0) {
+        c->ag_table_ptr = table_dev;
+    } else {
+        if (!c->ag_table.ensure((size_t)c->n_feat * c->dpad * es)) return c->fail(EP_ERR_OOM, "table staging failed");
+        CK(cudaMemsetAsync(c->ag_table.p, 0, (size_t)c->n_feat * c->dpad * es, s), "table staging");
+        CK(cudaMemcpy2DAsync(c->ag_table.p, (size_t)c->dpad * es, table_dev, (size_t)c->dims * es, (size_t)c->dims * es,
+                             c->n_feat, cudaMemcpyDeviceToDevice, s), "table staging");
+        c->ag_table_ptr = c->ag_table.p;
+    }
+    return EP_OK;
+}
+
+extern "C" int ep_ag_forward(ep_ctx* c, const ep_batch_samples* sm, int precision, const void* table_dev, void* loss_dev,
+                             void* stream) {
+    if (!c || !table_dev || !loss_dev) return c ? c->fail(EP_ERR_INVALID_ARG, "null pointer") : EP_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+    int rc = ag_prepare(c, sm, precision, table_dev, s);
+    if (rc) return rc;
+    return run_injected(c, c->ag_n, precision ? TT_F64 : TT_F32, c->ag_table_ptr, loss_dev, nullptr, OUT_DENSE, nullptr, 0.f,
+                        1, s);
+}
+
+extern "C" int ep_ag_backward(ep_ctx* c, const void* dloss_dev, void* grad_dev, void* stream) {
+    if (!c || !dloss_dev || !grad_dev) return c ? c->fail(EP_ERR_INVALID_ARG, "null pointer") : EP_ERR_INVALID_ARG;
+    if (c->ag_precision < 0) return c->fail(EP_ERR_STATE, "call ep_ag_forward first");
+    cudaSetDevice(c->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+    const int tt = c->ag_precision ? TT_F64 : TT_F32;
+    const size_t es = c->ag_precision ? 8 : 4;
+    int rc = run_injected(c, c->ag_n, tt, c->ag_table_ptr, c->loss.p, dloss_dev, OUT_DENSE, nullptr, 0.f, 1, s);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(grad_dev, 0, (size_t)c->n_feat * c->dims * es, s), "clear gradient");
+    launch_pack_rows(es, c->gdense.p, c->touched.as<uint32_t>(), c->n_touched.as<uint32_t>(), c->dpad, c->dims, grad_dev, 1,
+                     (uint32_t)std::min<uint64_t>(c->n_feat, c->items_cap), s);
+    CK(cudaGetLastError(), "gradient scatter");
+    CK(cudaStreamSynchronize(s), "autograd backward");
+    return EP_OK;
+}

@@ -1,0 +1,166 @@
+// ep_device.cuh -- device building blocks: counter-based Philox RNG, warp
+// primitives, and vectorised access to one table row split across a warp.
+//
+// Row layout in HBM: a table of n_feat rows, each padded to `dpad` elements
+// (dpad = VPL * ceil(dims / VPL), VPL = values per lane).  Lane l of a warp
+// owns elements [l*VPL, l*VPL + VPL) of every row, so one row is read by one
+// coalesced warp-wide access of VPL*sizeof(T) bytes per lane (16 B for BF16
+// at d=256).  Padding elements are zero and stay zero under training.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ep {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+// as 1, 2, 3", SC 2011).  Counter-based: every draw is a pure function of
+// (key, counter), so sampling is reproducible and needs no RNG state.
+// ---------------------------------------------------------------------------
+struct u32x4 { uint32_t x, y, z, w; };
+
+__host__ __device__ __forceinline__ void mulhilo32(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo) {
+    uint64_t p = (uint64_t)a * (uint64_t)b;
+    hi = (uint32_t)(p >> 32);
+    lo = (uint32_t)p;
+}
+
+__host__ __device__ __forceinline__ u32x4 philox(u32x4 c, uint64_t key) {
+    uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0, lo0, hi1, lo1;
+        mulhilo32(0xD2511F53u, c.x, hi0, lo0);
+        mulhilo32(0xCD9E8D57u, c.z, hi1, lo1);
+        c = u32x4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Stream ids (third counter word, top byte).
+enum : uint32_t { ST_NBR = 1u, ST_NEG = 2u, ST_NSEL = 3u, ST_ROUND = 4u, ST_INIT = 5u };
+
+__host__ __device__ __forceinline__ uint32_t rand_u32(uint64_t seed, uint32_t a, uint32_t b,
+                                                      uint32_t stream, uint32_t i) {
+    u32x4 r = philox(u32x4{a, b, (stream << 24) | (i >> 2), 0x5bd1e995u}, seed);
+    switch (i & 3u) { case 0: return r.x; case 1: return r.y; case 2: return r.z; default: return r.w; }
+}
+
+// Uniform integer in [0, n) by multiply-high (bias < n / 2^32).
+__host__ __device__ __forceinline__ uint32_t below(uint32_t r, uint32_t n) {
+    return (uint32_t)(((uint64_t)r * (uint64_t)n) >> 32);
+}
+__host__ __device__ __forceinline__ float unit_f32(uint32_t r) {   // [0, 1)
+    return (float)(r >> 8) * (1.0f / 16777216.0f);
+}
+
+// ---------------------------------------------------------------------------
+// Warp primitives
+// ---------------------------------------------------------------------------
+template <typename A>
+__device__ __forceinline__ A warp_sum(A v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    return v;
+}
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+template <typename A> __device__ __forceinline__ bool is_finite(A x) { return isfinite(x); }
+
+// ---------------------------------------------------------------------------
+// Row I/O.  RowIO<T, VPL>::load reads this lane's VPL elements of a row as A.
+// ---------------------------------------------------------------------------
+template <int BYTES> struct VecT;
+template <> struct VecT<2> { using type = unsigned short; };
+template <> struct VecT<4> { using type = unsigned int; };
+template <> struct VecT<8> { using type = uint2; };
+template <> struct VecT<16> { using type = uint4; };
+
+template <typename T> __device__ __forceinline__ float to_f(T x);
+template <> __device__ __forceinline__ float to_f<float>(float x) { return x; }
+template <> __device__ __forceinline__ float to_f<__nv_bfloat16>(__nv_bfloat16 x) { return __bfloat162float(x); }
+
+template <typename A, typename T> __device__ __forceinline__ A cvt_in(T x) { return (A)to_f<T>(x); }
+template <> __device__ __forceinline__ double cvt_in<double, double>(double x) { return x; }
+template <> __device__ __forceinline__ float cvt_in<float, double>(double x) { return (float)x; }
+
+template <typename T, int VPL>
+struct RowIO {
+    static constexpr int BYTES = VPL * (int)sizeof(T);
+    static constexpr int VB = BYTES >= 16 ? 16 : BYTES;
+    static constexpr int NV = BYTES / VB;
+    using V = typename VecT<VB>::type;
+
+    // Read-only path (ld.global.nc): valid while no kernel writes the row
+    // concurrently, which holds for the table inside one forward kernel.
+    template <typename A>
+    static __device__ __forceinline__ void load(const T* __restrict__ row, int lane, A (&out)[VPL]) {
+        union { V v[NV]; T t[VPL]; } u;
+        const V* src = reinterpret_cast<const V*>(row + lane * VPL);
+#pragma unroll
+        for (int i = 0; i < NV; ++i) u.v[i] = __ldg(src + i);
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) out[k] = cvt_in<A, T>(u.t[k]);
+    }
+    // Coherent load (rows written earlier in the same kernel).
+    template <typename A>
+    static __device__ __forceinline__ void load_cg(const T* row, int lane, A (&out)[VPL]) {
+        union { V v[NV]; T t[VPL]; } u;
+        const V* src = reinterpret_cast<const V*>(row + lane * VPL);
+#pragma unroll
+        for (int i = 0; i < NV; ++i) u.v[i] = __ldcg(src + i);
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) out[k] = cvt_in<A, T>(u.t[k]);
+    }
+    static __device__ __forceinline__ void store_raw(T* row, int lane, const T (&in)[VPL]) {
+        union { V v[NV]; T t[VPL]; } u;
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) u.t[k] = in[k];
+        V* dst = reinterpret_cast<V*>(row + lane * VPL);
+#pragma unroll
+        for (int i = 0; i < NV; ++i) dst[i] = u.v[i];
+    }
+};
+
+template <typename T> struct FromA;
+template <> struct FromA<float> {
+    template <typename A> static __device__ __forceinline__ float cvt(A x) { return (float)x; }
+};
+template <> struct FromA<double> {
+    template <typename A> static __device__ __forceinline__ double cvt(A x) { return (double)x; }
+};
+
+// Stores VPL accumulator values into a row of T (float/double: exact cast).
+template <typename T, int VPL, typename A>
+__device__ __forceinline__ void store_row(T* row, int lane, const A (&in)[VPL]) {
+    T t[VPL];
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) t[k] = FromA<T>::cvt(in[k]);
+    RowIO<T, VPL>::store_raw(row, lane, t);
+}
+
+// FP32 -> BF16 with stochastic rounding: adds uniform 16-bit noise below the
+// BF16 mantissa before truncation, so E[bf16(x)] = x and small Adam updates
+// are not lost to round-to-nearest.  NaN/Inf pass through unchanged.
+__device__ __forceinline__ __nv_bfloat16 bf16_stochastic(float x, uint32_t r16) {
+    uint32_t b = __float_as_uint(x);
+    if ((b & 0x7f800000u) == 0x7f800000u) return __float2bfloat16_rn(x);
+    b += (r16 & 0xffffu);
+    b &= 0xffff0000u;
+    return __ushort_as_bfloat16((unsigned short)(b >> 16));
+}
+
+}  // namespace ep

@@ -1,0 +1,753 @@
+// ep_fwd.cu -- sampling, gather-mean + loss + gradient-direction kernel, and
+// the per-batch bookkeeping kernels.
+//
+// Reference behaviour restated here (cloverleaf, Rust):
+//   anchor order per pass      src/algos/ep/mod.rs:172-174 (shuffle, chunks)
+//   neighbour reconstruction   src/algos/ep/model.rs:342-386, utils.rs:193-216
+//   negatives                  src/algos/grad_utils/node_sampler.rs:243-246
+//   role means                 src/algos/ep/model.rs:257-301, 388-416, 448-463
+//   losses                     src/algos/ep/loss.rs:56-129, 229-243
+//   loss weighting             src/algos/ep/mod.rs:190-200
+//   learning rate              src/algos/grad_utils/scheduler.rs:120-137
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "ep_device.cuh"
+#include "ep_internal.h"
+
+namespace ep {
+
+enum { LOSS_MARGIN = 0, LOSS_STARSPACE = 1, LOSS_CONTRASTIVE = 2 };
+enum { S_ALL = 0, S_FIXED = 1, S_PROB = 2 };
+enum { LW_NONE = 0, LW_LOG = 1, LW_EXP = 2 };
+
+// ---------------------------------------------------------------------------
+// Per-pass anchor order: a keyed Feistel bijection on [0, 2^(2h)) restricted
+// to [0, n) by cycle walking.  Replaces the host shuffle of mod.rs:173 with an
+// O(1)-per-position permutation that needs no buffer and no sort.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t fmix32(uint32_t x) {
+    x ^= x >> 16; x *= 0x85ebca6bu; x ^= x >> 13; x *= 0xc2b2ae35u; x ^= x >> 16;
+    return x;
+}
+
+__device__ __forceinline__ uint32_t feistel(uint32_t x, uint32_t h, const uint32_t* k) {
+    const uint32_t mask = h >= 32 ? 0xffffffffu : ((1u << h) - 1u);
+    uint32_t L = (h >= 32) ? 0 : (x >> h), Rr = x & mask;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        uint32_t F = fmix32(Rr ^ k[r]) & mask;
+        uint32_t nL = Rr;
+        Rr = L ^ F;
+        L = nL;
+    }
+    return (L << h) | Rr;
+}
+
+__device__ __forceinline__ uint32_t permute(uint32_t pos, uint32_t n, uint32_t h, const uint32_t* k,
+                                            uint32_t* err) {
+    uint32_t x = pos;
+    for (int it = 0; it < 128; ++it) {
+        x = feistel(x, h, k);
+        if (x < n) return x;
+    }
+    atomicOr(err, ERR_FEISTEL);
+    return pos % n;
+}
+
+// ---------------------------------------------------------------------------
+// k_batch_begin: batch range, learning rate and Adam bias corrections.
+// ---------------------------------------------------------------------------
+__global__ void k_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, uint64_t total,
+                              uint64_t warmup, float alpha, int injected) {
+    if (threadIdx.x != 0) return;
+    if (!injected) {
+        uint32_t b0 = st->batch * cap;
+        st->b0 = b0;
+        st->n_anchors = b0 < n_order ? min(cap, n_order - b0) : 0;
+    }
+    // LRScheduler::CosDecay(alpha/100, alpha, warmup, total) (mod.rs:133-137)
+    const float min_alpha = alpha / 100.f;
+    const uint64_t s = st->step;
+    float lr;
+    if (s > warmup) {
+        float ratio = (float)s / (float)total;
+        lr = min_alpha + 0.5f * (alpha - min_alpha) * (1.f + cosf(3.14159265358979323846f * ratio));
+    } else {
+        float ratio = (float)s / (float)warmup;
+        lr = min_alpha + ratio * (alpha - min_alpha);
+    }
+    st->lr = lr;
+    const float t = (float)st->pass + 1.f;
+    st->bc1 = 1.f - powf(0.9f, t);
+    st->bc2 = 1.f - powf(0.999f, t);
+    st->n_items = 0;
+}
+
+// ---------------------------------------------------------------------------
+// k_sample: one warp per anchor.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_sample(SampleParams p) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    BatchState* st = p.st;
+    const uint32_t n = st->n_anchors;
+    if (a >= n) return;
+    const SampleCfg& c = p.cfg;
+    const uint32_t salt = p.eval ? 0xffffffffu : (uint32_t)st->step;
+    uint32_t v;
+    if (p.injected) {
+        v = p.anchors[a];
+    } else {
+        const uint32_t pos = st->b0 + a;
+        uint32_t idx = pos;
+        if (!p.eval) {
+            uint32_t k[4];
+            u32x4 kk = philox(u32x4{st->pass, 0x9e3779b9u, 0x7f4a7c15u, 0x1234567u}, c.seed);
+            k[0] = kk.x; k[1] = kk.y; k[2] = kk.z; k[3] = kk.w;
+            idx = permute(pos, p.n_order, p.feistel_half, k, &st->error);
+        }
+        v = p.order[idx];
+        if (lane == 0) p.anchors[a] = v;
+
+        // --- neighbours (reconstruct_node_embedding, model.rs:342-386) ---
+        const uint64_t rs = p.row_ptr[v];
+        const uint32_t deg = (uint32_t)(p.row_ptr[v + 1] - rs);
+        uint32_t* out = p.nbr + (uint64_t)a * c.Kcap;
+        float* outw = p.nbr_w + (uint64_t)a * c.Kcap;
+        uint32_t cnt = 0;
+        float sw = 1.f;
+        int take_all = 0;
+        if (c.nodes_kind == S_ALL) {
+            take_all = 1;
+        } else if (c.nodes_kind == S_FIXED) {
+            const uint32_t r = min(c.K, deg);
+            sw = (float)deg / (float)r;
+            if (r == deg) {
+                take_all = 1;
+            } else if (r <= 32) {
+                // Floyd's algorithm: a uniform r-subset of [0, deg); lane i
+                // holds the i-th chosen position.
+                uint32_t mine = 0xffffffffu;
+                for (uint32_t it = 0; it < r; ++it) {
+                    const uint32_t j = deg - r + it;
+                    const uint32_t tpos = below(rand_u32(c.seed, v, salt, ST_NBR, it), j + 1);
+                    const unsigned hit = __ballot_sync(FULL, mine == tpos);
+                    const uint32_t pick = hit ? j : tpos;
+                    if (lane == (int)it) mine = pick;
+                }
+                if ((uint32_t)lane < r) { out[lane] = p.cols[rs + mine]; outw[lane] = __uint_as_float(mine); }
+                cnt = r;
+            } else if (r <= c.Kcap) {
+                // Floyd with the chosen set kept in the output slots.
+                for (uint32_t it = 0; it < r; ++it) {
+                    const uint32_t j = deg - r + it;
+                    const uint32_t tpos = below(rand_u32(c.seed, v, salt, ST_NBR, it), j + 1);
+                    bool found = false;
+                    for (uint32_t b = 0; b < it; b += 32) {
+                        const uint32_t q = b + lane;
+                        const bool m = q < it && out[q] == tpos;
+                        if (__any_sync(FULL, m)) { found = true; break; }
+                    }
+                    if (lane == 0) out[it] = found ? j : tpos;
+                    __syncwarp();
+                }
+                for (uint32_t q = lane; q < r; q += 32) {
+                    const uint32_t pos2 = out[q];
+                    outw[q] = __uint_as_float(pos2);
+                    out[q] = p.cols[rs + pos2];
+                }
+                cnt = r;
+            } else {
+                if (lane == 0) atomicOr(&st->error, ERR_NBR_OVERFLOW);
+                cnt = 0;
+            }
+            __syncwarp();
+        } else {  // S_PROB: independent Bernoulli(p) per neighbour == Binomial count + uniform subset
+            const float pr = c.nodes_val;
+            uint32_t sel_total = 0;
+            for (uint32_t b = 0; b < deg; b += 32) {
+                uint32_t q = b + lane;
+                bool s = q < deg && unit_f32(rand_u32(c.seed, v, salt, ST_NSEL, q)) < pr;
+                unsigned bm = __ballot_sync(FULL, s);
+                uint32_t off = sel_total + __popc(bm & ((1u << lane) - 1u));
+                if (s && off < c.Kcap) { out[off] = p.cols[rs + q]; outw[off] = __uint_as_float(q); }
+                sel_total += __popc(bm);
+            }
+            if (sel_total > c.Kcap) {
+                if (lane == 0) atomicOr(&st->error, ERR_NBR_OVERFLOW);
+                sel_total = c.Kcap;
+            }
+            if (sel_total == 0 && deg > 0) {
+                uint32_t q = below(rand_u32(c.seed, v, salt, ST_NSEL, deg), deg);
+                if (lane == 0) { out[0] = p.cols[rs + q]; outw[0] = __uint_as_float(q); }
+                sel_total = 1;
+                sw = (1.f - powf(pr, (float)deg)) / pr;
+            } else {
+                sw = 1.f / pr;
+            }
+            if (sel_total == deg) take_all = 1;
+            else cnt = sel_total;
+            __syncwarp();
+        }
+        if (take_all) {
+            if (deg > c.Kcap) {
+                if (lane == 0) atomicOr(&st->error, ERR_NBR_OVERFLOW);
+                cnt = 0;
+            } else {
+                for (uint32_t q = lane; q < deg; q += 32) { out[q] = p.cols[rs + q]; outw[q] = __uint_as_float(q); }
+                cnt = deg;
+            }
+        }
+        __syncwarp();
+        // weights: scale_weight, or scale * p_j * deg when averaging by edge
+        // weight (CDFtoP, graph.rs:630-661)
+        for (uint32_t q = lane; q < cnt; q += 32) {
+            float w = sw;
+            if (c.weighted_avg && p.wcdf) {
+                const uint32_t pos2 = __float_as_uint(outw[q]);
+                float pj = p.wcdf[rs + pos2] - (pos2 ? p.wcdf[rs + pos2 - 1] : 0.f);
+                w = sw * pj * (float)deg;
+            }
+            outw[q] = w;
+        }
+        if (lane == 0) p.nbr_cnt[a] = cnt;
+        // --- negatives: uniform over the pool, with replacement ---
+        for (uint32_t i = lane; i < c.R; i += 32)
+            p.neg[(uint64_t)a * c.R + i] = p.pool[below(rand_u32(c.seed, v, salt, ST_NEG, i), p.n_pool)];
+        __syncwarp();
+    }
+    // --- item count of this anchor: sum of feature counts over its roles ---
+    const uint32_t cnt = p.nbr_cnt[a];
+    uint64_t occ = 0;
+    if (lane == 0) occ += p.fptr[v + 1] - p.fptr[v];
+    const uint32_t* nb = p.nbr + (uint64_t)a * c.Kcap;
+    for (uint32_t q = lane; q < cnt; q += 32) { uint32_t u = nb[q]; occ += p.fptr[u + 1] - p.fptr[u]; }
+    const uint32_t* ng = p.neg + (uint64_t)a * c.R;
+    for (uint32_t q = lane; q < c.R; q += 32) { uint32_t u = ng[q]; occ += p.fptr[u + 1] - p.fptr[u]; }
+    occ = warp_sum<unsigned long long>((unsigned long long)occ);
+    if (lane == 0) p.occ[a] = (uint32_t)min(occ, (uint64_t)0xffffffffu);
+}
+
+// ---------------------------------------------------------------------------
+// k_scan_occ: exclusive scan of the per-anchor item counts (one CTA).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_scan_occ(BatchState* st, uint32_t* occ, uint64_t items_cap) {
+    __shared__ unsigned long long warp_tot[32];
+    __shared__ unsigned long long carry;
+    const uint32_t n = st->n_anchors;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < n; base += 1024) {
+        uint32_t i = base + tid;
+        unsigned long long x = i < n ? occ[i] : 0;
+        unsigned long long incl = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long t = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) warp_tot[w] = incl;
+        __syncthreads();
+        if (w == 0) {
+            unsigned long long s = warp_tot[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned long long t = __shfl_up_sync(FULL, s, o);
+                if (lane >= o) s += t;
+            }
+            warp_tot[lane] = s;
+        }
+        __syncthreads();
+        unsigned long long excl = carry + (w ? warp_tot[w - 1] : 0) + incl - x;
+        if (i < n) occ[i] = (uint32_t)min(excl, (unsigned long long)0xffffffffu);
+        __syncthreads();
+        if (tid == 1023) carry = excl + x;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        unsigned long long total = carry;
+        if (total > items_cap) {
+            atomicOr(&st->error, ERR_ITEMS_OVERFLOW);
+            total = 0;
+        }
+        occ[n] = (uint32_t)total;
+        st->n_items = (uint32_t)total;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_forward: one warp per anchor.
+// ---------------------------------------------------------------------------
+template <typename T, typename A, int VPL>
+__device__ __forceinline__ void fma_row(A (&acc)[VPL], A c, const A (&r)[VPL]) {
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) acc[k] += c * r[k];
+}
+
+// Gathers one role: the (weighted) mean numerator over every feature
+// occurrence of `count` nodes, returning the weight total.  Emits one item
+// per occurrence at item positions pos, pos+1, ... (role-major, node order,
+// feature order), which keeps items ordered by (anchor, role).
+template <typename T, typename A, int VPL>
+__device__ A gather_role(const ForwardParams& p, const T* __restrict__ table, const uint32_t* nodes,
+                         const float* w, uint32_t count, uint32_t src, uint64_t& pos, bool emit,
+                         A (&acc)[VPL], int lane, bool lane_on) {
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) acc[k] = 0;
+    A ntot = 0;
+    const uint32_t dpad = p.dpad;
+    for (uint32_t base = 0; base < count; base += 32) {
+        const uint32_t q = base + lane;
+        uint64_t fs = 0;
+        uint32_t fn = 0;
+        float c = 0.f;
+        if (q < count) {
+            const uint32_t u = nodes[q];
+            fs = p.fptr[u];
+            fn = (uint32_t)(p.fptr[u + 1] - fs);
+            c = (w ? w[q] : 1.f) + p.feat_scalar;
+        }
+        const uint32_t incl = warp_incl_scan(fn, lane);
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        ntot += warp_sum<A>((A)c * (A)fn);
+        for (uint32_t ob = 0; ob < total; ob += 32) {
+            const uint32_t o = ob + lane;
+            int qq = 0;
+#pragma unroll
+            for (int s = 16; s >= 1; s >>= 1) {
+                uint32_t iv = __shfl_sync(FULL, incl, qq + s - 1);
+                if (iv <= o) qq += s;
+            }
+            const int qs = qq > 31 ? 31 : qq;
+            const uint32_t excl_q = __shfl_sync(FULL, incl - fn, qs);
+            const uint32_t fs_lo = __shfl_sync(FULL, (uint32_t)fs, qs);
+            const uint32_t fs_hi = __shfl_sync(FULL, (uint32_t)(fs >> 32), qs);
+            const float cq = __shfl_sync(FULL, c, qs);
+            const bool active = o < total;
+            uint32_t f = 0;
+            if (active) f = p.fids[(((uint64_t)fs_hi << 32) | fs_lo) + (o - excl_q)];
+            if (emit && active) {
+                p.item_f[pos + o] = f;
+                p.item_src[pos + o] = src;
+                p.item_c[pos + o] = cq;
+            }
+            const uint32_t m = min(32u, total - ob);
+            uint32_t j = 0;
+            for (; j + 4 <= m; j += 4) {
+                const uint32_t f0 = __shfl_sync(FULL, f, j), f1 = __shfl_sync(FULL, f, j + 1);
+                const uint32_t f2 = __shfl_sync(FULL, f, j + 2), f3 = __shfl_sync(FULL, f, j + 3);
+                const A c0 = (A)__shfl_sync(FULL, cq, j), c1 = (A)__shfl_sync(FULL, cq, j + 1);
+                const A c2 = (A)__shfl_sync(FULL, cq, j + 2), c3 = (A)__shfl_sync(FULL, cq, j + 3);
+                if (lane_on) {
+                    A r0[VPL], r1[VPL], r2[VPL], r3[VPL];
+                    RowIO<T, VPL>::load(table + (uint64_t)f0 * dpad, lane, r0);
+                    RowIO<T, VPL>::load(table + (uint64_t)f1 * dpad, lane, r1);
+                    RowIO<T, VPL>::load(table + (uint64_t)f2 * dpad, lane, r2);
+                    RowIO<T, VPL>::load(table + (uint64_t)f3 * dpad, lane, r3);
+                    fma_row<T, A, VPL>(acc, c0, r0);
+                    fma_row<T, A, VPL>(acc, c1, r1);
+                    fma_row<T, A, VPL>(acc, c2, r2);
+                    fma_row<T, A, VPL>(acc, c3, r3);
+                }
+            }
+            for (; j < m; ++j) {
+                const uint32_t f0 = __shfl_sync(FULL, f, j);
+                const A c0 = (A)__shfl_sync(FULL, cq, j);
+                if (lane_on) {
+                    A r0[VPL];
+                    RowIO<T, VPL>::load(table + (uint64_t)f0 * dpad, lane, r0);
+                    fma_row<T, A, VPL>(acc, c0, r0);
+                }
+            }
+        }
+        pos += total;
+    }
+    return ntot;
+}
+
+template <typename A, int VPL>
+__device__ __forceinline__ A warp_dot(const A (&x)[VPL], const A (&y)[VPL]) {
+    A s = 0;
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) s += x[k] * y[k];
+    return warp_sum<A>(s);
+}
+
+template <typename A, int VPL>
+__device__ __forceinline__ bool warp_all_finite(const A (&x)[VPL]) {
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) ok = ok && isfinite(x[k]);
+    return __all_sync(FULL, ok);
+}
+
+template <typename T, typename A, int VPL>
+__global__ void __launch_bounds__(256) k_forward(ForwardParams p) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t n = p.st->n_anchors;
+    if (a >= n) return;
+    const uint32_t R = p.R, NR = R + 2, dpad = p.dpad;
+    const bool lane_on = (uint32_t)(lane * VPL) < dpad;
+    const T* __restrict__ table = (const T*)p.table;
+    A* dir = (A*)p.dir;
+    A* scale = (A*)p.scale;
+    const uint32_t v = p.anchors[a];
+    const bool emit = p.emit && p.st->n_items > 0;
+    uint64_t pos = emit ? p.occ_off[a] : 0;
+    const uint64_t sbase = (uint64_t)a * NR;
+
+    A hv[VPL], tv[VPL], u[VPL];
+    const A n_h = gather_role<T, A, VPL>(p, table, &v, nullptr, 1, (uint32_t)sbase, pos, emit, hv, lane, lane_on);
+    const uint32_t cnt = p.nbr_cnt[a];
+    const A n_t = gather_role<T, A, VPL>(p, table, p.nbr + (uint64_t)a * p.Kcap, p.nbr_w + (uint64_t)a * p.Kcap,
+                                         cnt, (uint32_t)(sbase + 1), pos, emit, tv, lane, lane_on);
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) { hv[k] /= n_h; tv[k] /= n_t; }
+
+    // loss weighting divisor (mod.rs:190-200)
+    A wdiv = 1;
+    if (p.loss_weighting != LW_NONE) {
+        const A deg = (A)(p.row_ptr[v + 1] - p.row_ptr[v]);
+        wdiv = p.loss_weighting == LW_LOG ? (A)log((double)(1 + deg)) : (A)pow((double)deg, (double)p.lw_exp);
+    }
+
+    A gsum[VPL];
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) gsum[k] = 0;
+    A lsum = 0;
+    uint32_t P = 0;
+
+    A na = 0, d1 = 0, nt = 0, nh = 0, rd = 0;
+    A xa[VPL];  // margin: t - h; cosine losses: normalised t
+    A xh[VPL];  // cosine losses: normalised h
+    if (p.loss == LOSS_MARGIN) {
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) xa[k] = tv[k] - hv[k];
+        na = sqrt(warp_dot<A, VPL>(xa, xa));
+        d1 = (A)p.gamma + na;
+    } else {
+        nt = sqrt(warp_dot<A, VPL>(tv, tv));
+        nh = sqrt(warp_dot<A, VPL>(hv, hv));
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) { xa[k] = tv[k] / nt; xh[k] = hv[k] / nh; }
+        rd = warp_dot<A, VPL>(xa, xh);
+    }
+
+    for (uint32_t i = 0; i < R; ++i) {
+        const uint32_t src = (uint32_t)(sbase + 2 + i);
+        const A n_u = gather_role<T, A, VPL>(p, table, p.neg + (uint64_t)a * R + i, nullptr, 1, src, pos, emit, u,
+                                             lane, lane_on);
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) u[k] /= n_u;
+        A d[VPL];
+        bool kept;
+        if (p.loss == LOSS_MARGIN) {
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) d[k] = tv[k] - u[k];
+            const A nb = sqrt(warp_dot<A, VPL>(d, d));
+            const A li = d1 - nb;
+            kept = li > 0;
+            if (kept) {
+                ++P;
+                lsum += li;
+#pragma unroll
+                for (int k = 0; k < VPL; ++k) { d[k] = d[k] / nb; gsum[k] += d[k]; }
+            }
+        } else {
+            const A nu = sqrt(warp_dot<A, VPL>(u, u));
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) u[k] /= nu;
+            const A cs = warp_dot<A, VPL>(xh, u);
+            const A li = p.loss == LOSS_STARSPACE ? (A)p.gamma - (rd - cs) : cs - (A)p.neg_margin;
+            kept = li > 0;
+            if (kept) {
+                ++P;
+                lsum += li;
+#pragma unroll
+                for (int k = 0; k < VPL; ++k) { gsum[k] += u[k]; d[k] = (xh[k] - u[k] * cs) / nu; }
+            }
+        }
+        bool fin = kept ? warp_all_finite<A, VPL>(d) : false;
+        if (kept && lane_on) store_row<A, VPL, A>(dir + (uint64_t)src * dpad, lane, d);
+        if (lane == 0) {
+            p.valid[src] = (uint8_t)(kept && fin);
+            scale[src] = kept ? (A)1 / n_u : (A)0;   // finalised below
+        }
+    }
+
+    // --- loss value and role-0/1 directions ---
+    uint32_t n_terms = P;
+    int pos_kept = 0;
+    if (p.loss == LOSS_CONTRASTIVE) {
+        const A pos_l = (A)p.gamma - rd;
+        if (pos_l > 0) { pos_kept = 1; ++n_terms; lsum += pos_l; }
+    }
+    A L = n_terms ? lsum / (A)n_terms : (A)0;
+    L = L / wdiv;
+    const bool is_nan = L != L;
+    const bool ok = !is_nan && L > 0;
+    A up = 1;
+    if (p.dloss) up = p.dloss_f64 ? (A)((const double*)p.dloss)[a] : (A)p.dloss[a];
+    const A inv = n_terms ? (A)1 / (A)n_terms : (A)0;
+
+    A dh[VPL], dt[VPL];
+    bool reach_t = true;
+    if (p.loss == LOSS_MARGIN) {
+        const A invP = P ? (A)1 / (A)P : (A)0;
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+            const A ak = xa[k] / na;   // NaN when t == h, dropped by the extraction rule
+            dh[k] = -ak;
+            dt[k] = ak - gsum[k] * invP;
+        }
+    } else {
+        const A cnt_t = p.loss == LOSS_STARSPACE ? (A)P : (A)pos_kept;
+        reach_t = p.loss == LOSS_STARSPACE ? true : pos_kept != 0;
+        A gtn[VPL], ghn[VPL];
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+            gtn[k] = -xh[k] * cnt_t * inv;
+            ghn[k] = (gsum[k] - xa[k] * cnt_t) * inv;
+        }
+        const A st_ = warp_dot<A, VPL>(xa, gtn);
+        const A sh_ = warp_dot<A, VPL>(xh, ghn);
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+            dt[k] = (gtn[k] - xa[k] * st_) / nt;
+            dh[k] = (ghn[k] - xh[k] * sh_) / nh;
+        }
+    }
+    const bool fin_h = warp_all_finite<A, VPL>(dh);
+    const bool fin_t = warp_all_finite<A, VPL>(dt);
+    if (lane_on) {
+        store_row<A, VPL, A>(dir + sbase * dpad, lane, dh);
+        store_row<A, VPL, A>(dir + (sbase + 1) * dpad, lane, dt);
+    }
+    if (lane == 0) {
+        p.valid[sbase] = (uint8_t)(ok && fin_h);
+        p.valid[sbase + 1] = (uint8_t)(ok && reach_t && fin_t);
+        scale[sbase] = up / (n_h * wdiv);
+        scale[sbase + 1] = up / (n_t * wdiv);
+        if (p.loss_out) ((A*)p.loss_out)[a] = L;
+        p.status[a] = is_nan ? 2 : (ok ? 0 : 1);
+    }
+    // negatives: scale = upstream * (1/terms) / (n_u * wdiv); clear when the anchor is dropped
+    __syncwarp();
+    const A neg_f = p.loss == LOSS_MARGIN ? (P ? (A)1 / (A)P : (A)0) : inv;
+    for (uint32_t i = lane; i < R; i += 32) {
+        const uint64_t src = sbase + 2 + i;
+        if (!ok) p.valid[src] = 0;
+        scale[src] = scale[src] * up * neg_f / wdiv;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_batch_end: deterministic per-batch loss sums and counters (one CTA).
+// ---------------------------------------------------------------------------
+template <typename A>
+__global__ void __launch_bounds__(1024) k_batch_end(BatchState* st, const A* loss, const int32_t* status,
+                                                    const uint32_t* nbr_cnt, uint32_t steps_per_pass, int eval) {
+    __shared__ double s_sum[32];
+    __shared__ unsigned long long s_cnt[32], s_nan[32], s_smp[32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const uint32_t n = st->n_anchors;
+    double sum = 0;
+    unsigned long long cnt = 0, nan = 0, smp = 0;
+    for (uint32_t i = tid; i < n; i += 1024) {
+        const int s = status[i];
+        const double l = (double)loss[i];
+        if (eval) sum += l;
+        else if (s == 0) { sum += l; ++cnt; }
+        nan += (s == 2);
+        smp += nbr_cnt[i];
+    }
+    sum = warp_sum<double>(sum);
+    cnt = warp_sum<unsigned long long>(cnt);
+    nan = warp_sum<unsigned long long>(nan);
+    smp = warp_sum<unsigned long long>(smp);
+    if (lane == 0) { s_sum[w] = sum; s_cnt[w] = cnt; s_nan[w] = nan; s_smp[w] = smp; }
+    __syncthreads();
+    if (tid == 0) {
+        double ts = 0;
+        unsigned long long tc = 0, tn = 0, tsm = 0;
+        for (int i = 0; i < 32; ++i) { ts += s_sum[i]; tc += s_cnt[i]; tn += s_nan[i]; tsm += s_smp[i]; }
+        if (eval) {
+            st->valid_sum += ts;
+            st->batch += 1;
+            return;
+        }
+        float be = (tc > 0 && n > 0) ? (float)(ts / (double)n) : 0.f;
+        if (isinf(be)) be = 0.f;
+        st->batch_err = be;
+        st->batch_kept = (uint32_t)tc;
+        st->pass_err_sum += be;
+        st->pass_batches += 1;
+        st->anchors += n;
+        st->kept += tc;
+        st->nan_anchors += tn;
+        st->sampled += tsm;
+        st->items += st->n_items;
+        st->step += 1;
+        st->batch += 1;
+        if (st->batch >= steps_per_pass) { st->batch = 0; st->pass += 1; }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Table initialisation (mod.rs:381-392): U(-1, 1) rows, L2-normalised.  One
+// warp per row; Philox draws keyed by (row, element).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_init_table(T* table, uint64_t n_feat, uint32_t dims, uint32_t dpad, uint64_t seed) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t row = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (row >= n_feat) return;
+    float ss = 0.f;
+    for (uint32_t k = lane; k < dims; k += 32) {
+        float x = 2.f * unit_f32(rand_u32(seed, (uint32_t)row, (uint32_t)(row >> 32), ST_INIT, k)) - 1.f;
+        ss += x * x;
+    }
+    ss = warp_sum<float>(ss);
+    const float nrm = sqrtf(ss);
+    for (uint32_t k = lane; k < dpad; k += 32) {
+        float x = 0.f;
+        if (k < dims) x = (2.f * unit_f32(rand_u32(seed, (uint32_t)row, (uint32_t)(row >> 32), ST_INIT, k)) - 1.f) / nrm;
+        if constexpr (sizeof(T) == 2) table[row * dpad + k] = __float2bfloat16_rn(x);
+        else table[row * dpad + k] = (T)x;
+    }
+}
+
+// Dense FP32 [n_feat x dims] <-> device layout [n_feat x dpad] of type T.
+template <typename T>
+__global__ void k_convert(T* dev, float* host_layout, uint64_t n_feat, uint32_t dims, uint32_t dpad, int to_dev) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_feat * dpad) return;
+    const uint64_t r = i / dpad;
+    const uint32_t k = (uint32_t)(i % dpad);
+    if (to_dev) {
+        float x = k < dims ? host_layout[r * dims + k] : 0.f;
+        if constexpr (sizeof(T) == 2) dev[i] = __float2bfloat16_rn(x);
+        else dev[i] = (T)x;
+    } else if (k < dims) {
+        if constexpr (sizeof(T) == 2) host_layout[r * dims + k] = __bfloat162float(dev[i]);
+        else host_layout[r * dims + k] = (float)dev[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Set-up kernels.
+// k_node_bound: an upper bound on the items one anchor can emit:
+//   F(v) + R * maxF + (neighbour part): the exact sum of the neighbours'
+//   feature counts when all of them can be taken (All / Prob), else
+//   min(K, deg) * (largest neighbour feature count).
+// k_split: train / validation ids as the first n_train / remaining positions
+//   of a seeded permutation of all nodes (mod.rs:118-122).
+// ---------------------------------------------------------------------------
+__global__ void k_node_bound(const uint64_t* row_ptr, const uint32_t* cols, const uint64_t* fptr, uint32_t n,
+                             int nodes_kind, uint32_t K, uint32_t R, uint32_t max_feat, uint32_t* bound) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const uint64_t rs = row_ptr[v], re = row_ptr[v + 1];
+    const uint64_t deg = re - rs;
+    uint64_t nb = 0;
+    if (nodes_kind == S_FIXED && deg > K) {
+        uint64_t mx = 0;
+        for (uint64_t j = rs; j < re; ++j) { const uint32_t u = cols[j]; mx = max(mx, fptr[u + 1] - fptr[u]); }
+        nb = (uint64_t)K * mx;
+    } else {
+        for (uint64_t j = rs; j < re; ++j) { const uint32_t u = cols[j]; nb += fptr[u + 1] - fptr[u]; }
+    }
+    const uint64_t b = (fptr[v + 1] - fptr[v]) + (uint64_t)R * max_feat + nb;
+    bound[v] = (uint32_t)min(b, (uint64_t)0xffffffffu);
+}
+
+__global__ void k_split(uint32_t* train, uint32_t n_train, uint32_t* valid, uint32_t n, uint64_t seed,
+                        uint32_t half, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t k[4];
+    const u32x4 kk = philox(u32x4{0u, 0x51ed270bu, 0x2545f491u, 0x9e3779b9u}, seed);
+    k[0] = kk.x; k[1] = kk.y; k[2] = kk.z; k[3] = kk.w;
+    const uint32_t node = permute(i, n, half, k, err);
+    if (i < n_train) train[i] = node;
+    else valid[i - n_train] = node;
+}
+
+void launch_node_bound(const uint64_t* row_ptr, const uint32_t* cols, const uint64_t* fptr, uint32_t n,
+                       int nodes_kind, uint32_t K, uint32_t R, uint32_t max_feat, uint32_t* bound, cudaStream_t s) {
+    k_node_bound<<<(n + 255) / 256, 256, 0, s>>>(row_ptr, cols, fptr, n, nodes_kind, K, R, max_feat, bound);
+}
+
+void launch_split(uint32_t* train, uint32_t n_train, uint32_t* valid, uint32_t n, uint64_t seed, uint32_t half,
+                  uint32_t* err, cudaStream_t s) {
+    k_split<<<(n + 255) / 256, 256, 0, s>>>(train, n_train, valid, n, seed, half, err);
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+void launch_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, uint32_t steps_per_pass,
+                        uint64_t total, uint64_t warmup, float alpha, int injected, cudaStream_t s) {
+    (void)steps_per_pass;
+    k_batch_begin<<<1, 32, 0, s>>>(st, n_order, cap, total, warmup, alpha, injected);
+}
+
+void launch_sample(const SampleParams& p, cudaStream_t s) {
+    const uint32_t blocks = (p.batch_cap + 7) / 8;
+    k_sample<<<blocks, 256, 0, s>>>(p);
+}
+
+void launch_scan_occ(BatchState* st, uint32_t* occ, uint32_t cap, uint64_t items_cap, cudaStream_t s) {
+    (void)cap;
+    k_scan_occ<<<1, 1024, 0, s>>>(st, occ, items_cap);
+}
+
+template <typename T, typename A>
+static void fwd_dispatch(int vpl, const ForwardParams& p, uint32_t cap, cudaStream_t s) {
+    const uint32_t blocks = (cap + 7) / 8;
+    switch (vpl) {
+        case 1: k_forward<T, A, 1><<<blocks, 256, 0, s>>>(p); break;
+        case 2: k_forward<T, A, 2><<<blocks, 256, 0, s>>>(p); break;
+        case 4: k_forward<T, A, 4><<<blocks, 256, 0, s>>>(p); break;
+        case 8: k_forward<T, A, 8><<<blocks, 256, 0, s>>>(p); break;
+        default: k_forward<T, A, 16><<<blocks, 256, 0, s>>>(p); break;
+    }
+}
+
+void launch_forward(int tt, int vpl, const ForwardParams& p, uint32_t cap, cudaStream_t s) {
+    if (tt == TT_F32) fwd_dispatch<float, float>(vpl, p, cap, s);
+    else if (tt == TT_BF16) fwd_dispatch<__nv_bfloat16, float>(vpl, p, cap, s);
+    else fwd_dispatch<double, double>(vpl, p, cap, s);
+}
+
+void launch_batch_end(BatchState* st, const void* loss, const int32_t* status, const uint32_t* nbr_cnt,
+                      uint32_t cap, uint32_t steps_per_pass, int eval, int loss_f64, cudaStream_t s) {
+    (void)cap;
+    if (loss_f64) k_batch_end<double><<<1, 1024, 0, s>>>(st, (const double*)loss, status, nbr_cnt, steps_per_pass, eval);
+    else k_batch_end<float><<<1, 1024, 0, s>>>(st, (const float*)loss, status, nbr_cnt, steps_per_pass, eval);
+}
+
+void launch_init_table(int tt, void* table, uint64_t n_feat, uint32_t dims, uint32_t dpad, uint64_t seed,
+                       cudaStream_t s) {
+    const uint64_t blocks = (n_feat * 32 + 255) / 256;
+    if (tt == TT_F32) k_init_table<float><<<(unsigned)blocks, 256, 0, s>>>((float*)table, n_feat, dims, dpad, seed);
+    else if (tt == TT_BF16)
+        k_init_table<__nv_bfloat16><<<(unsigned)blocks, 256, 0, s>>>((__nv_bfloat16*)table, n_feat, dims, dpad, seed);
+    else k_init_table<double><<<(unsigned)blocks, 256, 0, s>>>((double*)table, n_feat, dims, dpad, seed);
+}
+
+void launch_convert_table(int tt, void* dst, const float* src, uint64_t n_feat, uint32_t dims, uint32_t dpad,
+                          int to_dev, cudaStream_t s) {
+    const uint64_t n = n_feat * dpad;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (!n) return;
+    float* hl = const_cast<float*>(src);
+    if (tt == TT_F32) k_convert<float><<<blocks, 256, 0, s>>>((float*)dst, hl, n_feat, dims, dpad, to_dev);
+    else if (tt == TT_BF16) k_convert<__nv_bfloat16><<<blocks, 256, 0, s>>>((__nv_bfloat16*)dst, hl, n_feat, dims, dpad, to_dev);
+    else k_convert<double><<<blocks, 256, 0, s>>>((double*)dst, hl, n_feat, dims, dpad, to_dev);
+}
+
+}  // namespace ep

@@ -1,0 +1,187 @@
+// ep_internal.h -- structures shared by the host driver (ep_ctx.cu) and the
+// kernel translation units (ep_fwd.cu, ep_sort.cu, ep_red.cu).
+//
+// Per-batch data flow on the device (one CUDA stream, replayable as a graph):
+//   k_batch_begin  -> BatchState (batch range, lr, Adam bias corrections)
+//   k_sample       -> anchors, sampled neighbours, negatives, occurrence counts
+//   k_scan_occ     -> exclusive item offsets per anchor
+//   k_forward      -> role means, loss, per-role gradient directions and
+//                     scales, one item (feature, role-src, count) per feature
+//                     occurrence, written at deterministic offsets
+//   radix sort     -> items stably ordered by feature id
+//   k_reduce       -> per-feature gradient = sum over kept items, with the
+//                     first-occurrence rule; fused Adam (FUSED) or a dense
+//                     gradient row + touched list (PLAIN / parity hooks)
+//   k_fixup        -> features whose items span reducer chunks
+//   k_adam         -> (PLAIN) Adam over the touched list
+//   k_batch_end    -> deterministic loss sums, counters, state advance
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ep {
+
+// Device error bits (BatchState::error).  A kernel that detects a condition
+// it cannot handle sets a bit and skips the offending work; the host reads
+// the word after each pass / synchronisation and reports EP_ERR_DEVICE.
+enum : uint32_t {
+    ERR_ITEMS_OVERFLOW = 1u << 0,   // a batch emitted more items than allocated
+    ERR_FEISTEL = 1u << 1,          // permutation cycle walk exceeded its cap
+    ERR_NBR_OVERFLOW = 1u << 2,     // sampled neighbours exceeded capacity
+};
+
+enum OutMode : int { OUT_ADAM = 0, OUT_DENSE = 1 };
+enum TableType : int { TT_F32 = 0, TT_BF16 = 1, TT_F64 = 2 };
+
+struct BatchState {
+    uint32_t pass;          // 1-based pass index
+    uint32_t batch;         // batch index within the pass
+    uint64_t step;          // global optimizer step, starts at 1 (mod.rs:153)
+    uint32_t b0;            // first position of this batch in the pass order
+    uint32_t n_anchors;     // anchors in this batch
+    float lr;               // cos-decay learning rate for `step`
+    float bc1, bc2;         // 1 - beta^t with t = pass + 1 (optimizer.rs:50)
+    uint32_t error;         // ERR_* bits, sticky
+    uint32_t n_items;       // items emitted by this batch
+    // per-batch outputs of k_batch_end
+    float batch_err;        // sum(loss kept) / n_anchors (0 when none kept)
+    uint32_t batch_kept;
+    // pass accumulators (reset by the host at a pass start)
+    double pass_err_sum;
+    uint32_t pass_batches;
+    uint32_t pad0;
+    unsigned long long anchors, kept, nan_anchors, items, gathered, unique_rows, sampled;
+    double valid_sum;
+};
+
+struct SampleCfg {
+    int nodes_kind;         // EP_SAMPLE_*
+    float nodes_val;
+    uint32_t K;             // Fixed(k)
+    uint32_t Kcap;          // neighbour slots per anchor
+    uint32_t R;             // negatives
+    int weighted_avg;       // weighted_neighbor_averaging
+    float feat_scalar;      // s_u for Sample::All features
+    uint64_t seed;
+};
+
+struct SampleParams {
+    BatchState* st;
+    SampleCfg cfg;
+    const uint64_t* row_ptr;
+    const uint32_t* cols;
+    const float* wcdf;
+    const uint64_t* fptr;
+    const uint32_t* order;  // anchor source (train or valid ids)
+    uint32_t n_order;
+    const uint32_t* pool;   // negative pool (train or valid ids)
+    uint32_t n_pool;
+    uint32_t batch_cap;     // anchors per batch
+    int injected;           // samples provided by the host: only count
+    int eval;               // validation: fixed sampling stream, no shuffle
+    uint32_t feistel_half;  // half-width in bits of the permutation domain
+    uint32_t feistel_key[4];
+    // outputs
+    uint32_t* anchors;
+    uint32_t* nbr;
+    float* nbr_w;
+    uint32_t* nbr_cnt;
+    uint32_t* neg;
+    uint32_t* occ;          // per-anchor item counts
+};
+
+struct ForwardParams {
+    BatchState* st;
+    int loss;               // EP_LOSS_*
+    float gamma, neg_margin;
+    int loss_weighting;
+    float lw_exp;
+    float feat_scalar;
+    uint32_t R, Kcap, dims, dpad;
+    const uint64_t* row_ptr;
+    const uint64_t* fptr;
+    const uint32_t* fids;
+    const void* table;      // T[n_feat * dpad]
+    const uint32_t* anchors;
+    const uint32_t* nbr;
+    const float* nbr_w;
+    const uint32_t* nbr_cnt;
+    const uint32_t* neg;
+    const uint32_t* occ_off;  // exclusive offsets, [n_anchors] = total
+    const float* dloss;       // optional per-anchor upstream gradient (autograd)
+    int dloss_f64;
+    int emit;                 // 0: forward only (validation)
+    uint64_t items_cap;
+    // outputs
+    void* dir;              // A[n_anchors * NR * dpad]
+    void* scale;            // A[n_anchors * NR]
+    uint8_t* valid;         // [n_anchors * NR]
+    void* loss_out;         // A[n_anchors]
+    int32_t* status;        // [n_anchors]
+    uint32_t* item_f;
+    uint32_t* item_src;
+    float* item_c;
+};
+
+struct ReduceParams {
+    BatchState* st;
+    uint32_t NR, dpad, chunk;
+    int grad_true;          // EP_GRAD_TRUE
+    int out_mode;           // OutMode
+    const uint32_t* skey;   // sorted feature ids
+    const uint32_t* sidx;   // item index of each sorted position
+    const uint32_t* item_src;
+    const float* item_c;
+    const void* dir;        // A
+    const void* scale;      // A
+    const uint8_t* valid;
+    // OUT_ADAM
+    void* table;            // T
+    float* m;
+    float* v;
+    uint64_t seed;
+    // OUT_DENSE
+    void* gdense;           // A[n_feat * dpad]
+    uint32_t* touched;      // list of touched features
+    uint32_t* n_touched;
+    // carries
+    void* carry_head;       // A[n_chunks * dpad]
+    void* carry_tail;
+    uint32_t* carry_f;
+    uint32_t* carry_flags;
+};
+
+// ---- launchers (defined in the kernel translation units) -----------------
+void launch_batch_begin(BatchState* st, uint32_t n_order, uint32_t batch_cap,
+                        uint32_t steps_per_pass, uint64_t total_steps, uint64_t warmup,
+                        float alpha, int injected, cudaStream_t s);
+void launch_sample(const SampleParams& p, cudaStream_t s);
+void launch_scan_occ(BatchState* st, uint32_t* occ, uint32_t cap, uint64_t items_cap,
+                     cudaStream_t s);
+void launch_forward(int tt, int vpl, const ForwardParams& p, uint32_t cap, cudaStream_t s);
+void launch_radix_sort(BatchState* st, uint32_t* keys, uint32_t* keys_alt, uint32_t* idx,
+                       uint32_t* idx_alt, uint32_t* hist, uint64_t cap, int key_bits,
+                       uint32_t** sorted_keys, uint32_t** sorted_idx, cudaStream_t s);
+void launch_reduce(int tt, int vpl, const ReduceParams& p, uint64_t items_cap, cudaStream_t s);
+void launch_adam_dense(int tt, int vpl, BatchState* st, void* table, float* m, float* v,
+                       const float* g, const uint32_t* touched, const uint32_t* n_touched,
+                       uint32_t dpad, uint32_t max_rows, uint64_t seed, cudaStream_t s);
+void launch_batch_end(BatchState* st, const void* loss, const int32_t* status,
+                      const uint32_t* nbr_cnt, uint32_t cap, uint32_t steps_per_pass,
+                      int eval, int loss_f64, cudaStream_t s);
+void launch_init_table(int tt, void* table, uint64_t n_feat, uint32_t dims, uint32_t dpad,
+                       uint64_t seed, cudaStream_t s);
+void launch_convert_table(int tt_dst, void* dst, const float* src, uint64_t n_feat,
+                          uint32_t dims, uint32_t dpad, int to_device_layout, cudaStream_t s);
+void launch_node_bound(const uint64_t* row_ptr, const uint32_t* cols, const uint64_t* fptr, uint32_t n,
+                       int nodes_kind, uint32_t K, uint32_t R, uint32_t max_feat, uint32_t* bound,
+                       cudaStream_t s);
+void launch_split(uint32_t* train, uint32_t n_train, uint32_t* valid, uint32_t n, uint64_t seed,
+                  uint32_t half, uint32_t* err, cudaStream_t s);
+void launch_pack_rows(size_t es, const void* dense, const uint32_t* rows, const uint32_t* n_rows,
+                      uint32_t dpad, uint32_t dims, void* out, int scatter, uint32_t max_rows,
+                      cudaStream_t s);
+size_t radix_hist_entries(uint64_t cap);
+uint32_t reduce_chunks(uint64_t cap, uint32_t chunk);
+
+}  // namespace ep

@@ -1,0 +1,368 @@
+// ep_red.cu -- deterministic per-feature gradient reduction, fused with Adam.
+//
+// Input: items sorted stably by feature id (ep_sort.cu), so the items of one
+// feature are contiguous and ordered by (anchor, role).  For feature f the
+// batch gradient is
+//     G[f] = sum over kept items i of c_i * scale[src_i] * dir[src_i]
+// where src = anchor * NR + role, c_i is the occurrence's count weight,
+// scale folds 1/n_role, the loss-term normaliser, loss weighting and any
+// upstream gradient, and dir is the role's gradient direction.
+//
+// Kept items (src/algos/ep/mod.rs:361-378): in REFERENCE mode, within one
+// (feature, anchor) group only the items of the first role whose gradient is
+// present and finite are kept ("first occurrence wins"); in TRUE mode every
+// item of a valid role is kept.
+//
+// Work split: the sorted range is cut into fixed-size chunks, one warp per
+// chunk, walking its items in order (so no atomics on gradient rows).  A
+// feature entirely inside a chunk is finished in place: Adam on the row
+// (optimizer.rs:43-81) or a dense gradient row.  A feature spanning chunks
+// leaves partial sums (carries); k_fixup adds them in chunk order and
+// finishes the row, so the summation order is fixed and results are
+// bit-reproducible.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <type_traits>
+
+#include "ep_device.cuh"
+#include "ep_internal.h"
+
+namespace ep {
+
+constexpr uint32_t NONE = 0xffffffffu;
+enum : uint32_t { CF_HEAD = 1u, CF_THROUGH = 2u, CF_OWNER = 4u };
+constexpr int RED_THREADS = 256;
+constexpr uint32_t RED_MAX_CTAS = 152 * 8;
+
+uint32_t reduce_chunks(uint64_t cap, uint32_t chunk) { return (uint32_t)((cap + chunk - 1) / chunk); }
+
+// Adam on one row (optimizer.rs:43-81): t = pass + 1, beta1 0.9, beta2 0.999,
+// eps 1e-8; rows containing NaN are skipped (optimizer.rs:56).
+template <typename T, int VPL, typename A>
+__device__ __forceinline__ void adam_row(T* __restrict__ table, float* __restrict__ m, float* __restrict__ v,
+                                         uint32_t f, uint32_t dpad, const A (&g)[VPL], float lr, float bc1, float bc2,
+                                         uint64_t seed, uint32_t step, int lane, bool lane_on) {
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) bad = bad || (g[k] != g[k]);
+    if (__any_sync(FULL, bad) || !lane_on) return;
+    if constexpr (std::is_same<T, double>::value) {
+        return;  // FP64 tables exist only for gradient checks
+    } else {
+        const uint64_t o = (uint64_t)f * dpad;
+        float mm[VPL], vv[VPL], ee[VPL];
+        RowIO<float, VPL>::load_cg(m + o, lane, mm);
+        RowIO<float, VPL>::load_cg(v + o, lane, vv);
+        RowIO<T, VPL>::load_cg(table + o, lane, ee);
+        const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+            const float gk = (float)g[k];
+            mm[k] = b1 * mm[k] + (1.f - b1) * gk;
+            vv[k] = b2 * vv[k] + (1.f - b2) * (gk * gk);
+            const float mh = mm[k] / bc1;
+            const float vh = vv[k] / bc2;
+            ee[k] -= lr * (mh / (sqrtf(vh) + eps));
+        }
+        RowIO<float, VPL>::store_raw(m + o, lane, mm);
+        RowIO<float, VPL>::store_raw(v + o, lane, vv);
+        if constexpr (std::is_same<T, float>::value) {
+            RowIO<float, VPL>::store_raw(table + o, lane, ee);
+        } else {
+            // BF16 table: stochastic rounding, 16 random bits per element from
+            // one Philox block per 8 elements.
+            __nv_bfloat16 out[VPL];
+#pragma unroll
+            for (int k0 = 0; k0 < VPL; k0 += 8) {
+                const u32x4 r = philox(u32x4{f, step, (ST_ROUND << 24) | (uint32_t)lane, (uint32_t)k0}, seed);
+                const uint32_t w[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+                for (int k = k0; k < k0 + 8 && k < VPL; ++k) {
+                    const uint32_t bits = (k & 1) ? (w[(k - k0) >> 1] >> 16) : (w[(k - k0) >> 1] & 0xffffu);
+                    out[k] = bf16_stochastic(ee[k], bits);
+                }
+            }
+            RowIO<__nv_bfloat16, VPL>::store_raw(table + o, lane, out);
+        }
+    }
+}
+
+template <typename T, typename A, int VPL>
+__device__ __forceinline__ void finish_row(const ReduceParams& p, uint32_t f, const A (&acc)[VPL], int lane,
+                                           bool lane_on, float lr, float bc1, float bc2, uint32_t step) {
+    if (p.out_mode == OUT_DENSE) {
+        if (lane_on) store_row<A, VPL, A>((A*)p.gdense + (uint64_t)f * p.dpad, lane, acc);
+        if (lane == 0) p.touched[atomicAdd(p.n_touched, 1u)] = f;
+        return;
+    }
+    adam_row<T, VPL, A>((T*)p.table, p.m, p.v, f, p.dpad, acc, lr, bc1, bc2, p.seed, step, lane, lane_on);
+}
+
+template <typename A, int VPL>
+__device__ __forceinline__ void flush_pending(const ReduceParams& p, uint32_t& pend, A& pend_c, A (&acc)[VPL],
+                                              int lane, bool lane_on) {
+    if (pend == NONE) return;
+    const A sc = ((const A*)p.scale)[pend];
+    if (lane_on) {
+        A d[VPL];
+        RowIO<A, VPL>::load((const A*)p.dir + (uint64_t)pend * p.dpad, lane, d);
+        const A w = pend_c * sc;
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) acc[k] += w * d[k];
+    }
+    pend = NONE;
+    pend_c = 0;
+}
+
+template <typename T, typename A, int VPL>
+__global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t M = p.st->n_items;
+    const uint32_t C = p.chunk;
+    const uint32_t nchunks = (M + C - 1) / C;
+    const uint32_t NR = p.NR;
+    const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
+    const float lr = p.st->lr, bc1 = p.st->bc1, bc2 = p.st->bc2;
+    const uint32_t step = (uint32_t)p.st->step;
+    unsigned long long g_cnt = 0, u_cnt = 0;
+    for (uint32_t c = gw; c < nchunks; c += nw) {
+        const uint32_t i0 = c * C, i1 = min(i0 + C, M);
+        uint32_t cur_f = p.skey[i0];
+        const bool head_partial = i0 > 0 && p.skey[i0 - 1] == cur_f;
+        uint32_t cur_anchor = p.item_src[p.sidx[i0]] / NR;
+        uint32_t chosen = NONE;
+        if (!p.grad_true && head_partial) {
+            // The (feature, anchor) group may have started in an earlier
+            // chunk: find its first valid role by walking back.
+            int64_t j = (int64_t)i0 - 1;
+            for (;;) {
+                const int64_t jj = j - lane;
+                bool in = false;
+                uint32_t s = 0;
+                if (jj >= 0 && p.skey[jj] == cur_f) {
+                    s = p.item_src[p.sidx[jj]];
+                    in = (s / NR) == cur_anchor;
+                }
+                const unsigned inm = __ballot_sync(FULL, in);
+                const unsigned run = (~inm) ? ((1u << (__ffs(~inm) - 1)) - 1u) : FULL;
+                const bool vv = in && ((run >> lane) & 1u) && p.valid[s];
+                const unsigned vm = __ballot_sync(FULL, vv);
+                if (vm) chosen = __shfl_sync(FULL, s, 31 - __clz(vm));
+                if (run != FULL) break;
+                j -= 32;
+            }
+        }
+        A acc[VPL];
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) acc[k] = 0;
+        uint32_t pend = NONE;
+        A pend_c = 0;
+        bool started_here = !head_partial;
+        uint32_t flags = 0;
+        for (uint32_t ib = i0; ib < i1; ib += 32) {
+            const uint32_t i = ib + lane;
+            uint32_t f_l = 0, s_l = 0, v_l = 0;
+            float c_l = 0.f;
+            if (i < i1) {
+                f_l = p.skey[i];
+                const uint32_t ix = p.sidx[i];
+                s_l = p.item_src[ix];
+                c_l = p.item_c[ix];
+                v_l = p.valid[s_l];
+                const bool newrun = (i == 0) || (p.skey[i - 1] != f_l) || (p.item_src[p.sidx[i - 1]] != s_l);
+                g_cnt += newrun;
+            }
+            const uint32_t m = min(32u, i1 - ib);
+            for (uint32_t j = 0; j < m; ++j) {
+                const uint32_t f = __shfl_sync(FULL, f_l, j);
+                const uint32_t s = __shfl_sync(FULL, s_l, j);
+                const A cc = (A)__shfl_sync(FULL, c_l, j);
+                const uint32_t vv = __shfl_sync(FULL, v_l, j);
+                if (f != cur_f) {
+                    flush_pending<A, VPL>(p, pend, pend_c, acc, lane, lane_on);
+                    if (started_here) {
+                        finish_row<T, A, VPL>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step);
+                        ++u_cnt;
+                    } else {
+                        if (lane_on) store_row<A, VPL, A>((A*)p.carry_head + (uint64_t)c * p.dpad, lane, acc);
+                        flags |= CF_HEAD;
+                    }
+#pragma unroll
+                    for (int k = 0; k < VPL; ++k) acc[k] = 0;
+                    cur_f = f;
+                    started_here = true;
+                    cur_anchor = s / NR;
+                    chosen = NONE;
+                } else if (s / NR != cur_anchor) {
+                    cur_anchor = s / NR;
+                    chosen = NONE;
+                }
+                bool keep;
+                if (p.grad_true) {
+                    keep = vv != 0;
+                } else {
+                    if (vv && chosen == NONE) chosen = s;
+                    keep = vv && s == chosen;
+                }
+                if (keep) {
+                    if (s == pend) {
+                        pend_c += cc;
+                    } else {
+                        flush_pending<A, VPL>(p, pend, pend_c, acc, lane, lane_on);
+                        pend = s;
+                        pend_c = cc;
+                    }
+                }
+            }
+        }
+        flush_pending<A, VPL>(p, pend, pend_c, acc, lane, lane_on);
+        const bool cont = i1 < M && p.skey[i1] == cur_f;
+        if (started_here && !cont) {
+            finish_row<T, A, VPL>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step);
+            ++u_cnt;
+        } else if (!started_here) {
+            if (lane_on) store_row<A, VPL, A>((A*)p.carry_head + (uint64_t)c * p.dpad, lane, acc);
+            flags |= CF_HEAD | (cont ? CF_THROUGH : 0u);
+        } else {
+            if (lane_on) store_row<A, VPL, A>((A*)p.carry_tail + (uint64_t)c * p.dpad, lane, acc);
+            if (lane == 0) p.carry_f[c] = cur_f;
+            flags |= CF_OWNER;
+            ++u_cnt;
+        }
+        if (lane == 0) p.carry_flags[c] = flags;
+    }
+    g_cnt = warp_sum<unsigned long long>(g_cnt);
+    if (lane == 0) {
+        if (g_cnt) atomicAdd(&p.st->gathered, g_cnt);
+        if (u_cnt) atomicAdd(&p.st->unique_rows, u_cnt);
+    }
+}
+
+template <typename T, typename A, int VPL>
+__global__ void __launch_bounds__(RED_THREADS) k_fixup(ReduceParams p) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t M = p.st->n_items;
+    const uint32_t nchunks = (M + p.chunk - 1) / p.chunk;
+    const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
+    const float lr = p.st->lr, bc1 = p.st->bc1, bc2 = p.st->bc2;
+    const uint32_t step = (uint32_t)p.st->step;
+    for (uint32_t c = gw; c < nchunks; c += nw) {
+        if (!(p.carry_flags[c] & CF_OWNER)) continue;
+        const uint32_t f = p.carry_f[c];
+        A acc[VPL];
+        if (lane_on) RowIO<A, VPL>::load_cg((const A*)p.carry_tail + (uint64_t)c * p.dpad, lane, acc);
+        else {
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) acc[k] = 0;
+        }
+        for (uint32_t j = c + 1; j < nchunks; ++j) {
+            if (lane_on) {
+                A h[VPL];
+                RowIO<A, VPL>::load_cg((const A*)p.carry_head + (uint64_t)j * p.dpad, lane, h);
+#pragma unroll
+                for (int k = 0; k < VPL; ++k) acc[k] += h[k];
+            }
+            if (!(p.carry_flags[j] & CF_THROUGH)) break;
+        }
+        finish_row<T, A, VPL>(p, f, acc, lane, lane_on, lr, bc1, bc2, step);
+    }
+}
+
+// PLAIN form: Adam over the touched list, reading the dense gradient rows.
+template <typename T, int VPL>
+__global__ void __launch_bounds__(RED_THREADS) k_adam_dense(BatchState* st, T* table, float* m, float* v,
+                                                            const float* g, const uint32_t* touched,
+                                                            const uint32_t* n_touched, uint32_t dpad, uint64_t seed) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t n = *n_touched;
+    const bool lane_on = (uint32_t)(lane * VPL) < dpad;
+    const float lr = st->lr, bc1 = st->bc1, bc2 = st->bc2;
+    const uint32_t step = (uint32_t)st->step;
+    for (uint32_t r = gw; r < n; r += nw) {
+        const uint32_t f = touched[r];
+        float gg[VPL];
+        if (lane_on) RowIO<float, VPL>::load_cg(g + (uint64_t)f * dpad, lane, gg);
+        else {
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) gg[k] = 0.f;
+        }
+        adam_row<T, VPL, float>(table, m, v, f, dpad, gg, lr, bc1, bc2, seed, step, lane, lane_on);
+    }
+}
+
+template <typename T, typename A>
+static void red_dispatch(int vpl, const ReduceParams& p, uint64_t cap, cudaStream_t s) {
+    const uint32_t nch = reduce_chunks(cap, p.chunk);
+    const uint32_t warps = nch ? nch : 1;
+    uint32_t ctas = (warps + RED_THREADS / 32 - 1) / (RED_THREADS / 32);
+    if (ctas > RED_MAX_CTAS) ctas = RED_MAX_CTAS;
+    switch (vpl) {
+        case 1: k_reduce<T, A, 1><<<ctas, RED_THREADS, 0, s>>>(p); k_fixup<T, A, 1><<<ctas, RED_THREADS, 0, s>>>(p); break;
+        case 2: k_reduce<T, A, 2><<<ctas, RED_THREADS, 0, s>>>(p); k_fixup<T, A, 2><<<ctas, RED_THREADS, 0, s>>>(p); break;
+        case 4: k_reduce<T, A, 4><<<ctas, RED_THREADS, 0, s>>>(p); k_fixup<T, A, 4><<<ctas, RED_THREADS, 0, s>>>(p); break;
+        case 8: k_reduce<T, A, 8><<<ctas, RED_THREADS, 0, s>>>(p); k_fixup<T, A, 8><<<ctas, RED_THREADS, 0, s>>>(p); break;
+        default: k_reduce<T, A, 16><<<ctas, RED_THREADS, 0, s>>>(p); k_fixup<T, A, 16><<<ctas, RED_THREADS, 0, s>>>(p); break;
+    }
+}
+
+void launch_reduce(int tt, int vpl, const ReduceParams& p, uint64_t cap, cudaStream_t s) {
+    if (tt == TT_F32) red_dispatch<float, float>(vpl, p, cap, s);
+    else if (tt == TT_BF16) red_dispatch<__nv_bfloat16, float>(vpl, p, cap, s);
+    else red_dispatch<double, double>(vpl, p, cap, s);
+}
+
+template <typename T>
+static void adam_dispatch(int vpl, BatchState* st, T* table, float* m, float* v, const float* g,
+                          const uint32_t* touched, const uint32_t* n_touched, uint32_t dpad, uint32_t max_rows,
+                          uint64_t seed, cudaStream_t s) {
+    uint32_t ctas = (max_rows + RED_THREADS / 32 - 1) / (RED_THREADS / 32);
+    if (ctas > RED_MAX_CTAS) ctas = RED_MAX_CTAS;
+    if (ctas == 0) ctas = 1;
+    switch (vpl) {
+        case 1: k_adam_dense<T, 1><<<ctas, RED_THREADS, 0, s>>>(st, table, m, v, g, touched, n_touched, dpad, seed); break;
+        case 2: k_adam_dense<T, 2><<<ctas, RED_THREADS, 0, s>>>(st, table, m, v, g, touched, n_touched, dpad, seed); break;
+        case 4: k_adam_dense<T, 4><<<ctas, RED_THREADS, 0, s>>>(st, table, m, v, g, touched, n_touched, dpad, seed); break;
+        case 8: k_adam_dense<T, 8><<<ctas, RED_THREADS, 0, s>>>(st, table, m, v, g, touched, n_touched, dpad, seed); break;
+        default: k_adam_dense<T, 16><<<ctas, RED_THREADS, 0, s>>>(st, table, m, v, g, touched, n_touched, dpad, seed); break;
+    }
+}
+
+void launch_adam_dense(int tt, int vpl, BatchState* st, void* table, float* m, float* v, const float* g,
+                       const uint32_t* touched, const uint32_t* n_touched, uint32_t dpad, uint32_t max_rows,
+                       uint64_t seed, cudaStream_t s) {
+    if (tt == TT_F32) adam_dispatch<float>(vpl, st, (float*)table, m, v, g, touched, n_touched, dpad, max_rows, seed, s);
+    else if (tt == TT_BF16)
+        adam_dispatch<__nv_bfloat16>(vpl, st, (__nv_bfloat16*)table, m, v, g, touched, n_touched, dpad, max_rows, seed, s);
+}
+
+// Packs touched rows of a padded dense buffer into out[r * dims] (scatter=0),
+// or writes them back into a dense [n_feat x dims] buffer (scatter=1).
+template <typename E>
+__global__ void k_pack_rows(const E* dense, const uint32_t* rows, const uint32_t* n_rows, uint32_t dpad,
+                            uint32_t dims, E* out, int scatter) {
+    const uint32_t n = *n_rows;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (uint64_t)n * dims;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t r = (uint32_t)(i / dims), k = (uint32_t)(i % dims);
+        const uint32_t f = rows[r];
+        if (scatter) out[(uint64_t)f * dims + k] = dense[(uint64_t)f * dpad + k];
+        else out[i] = dense[(uint64_t)f * dpad + k];
+    }
+}
+
+void launch_pack_rows(size_t es, const void* dense, const uint32_t* rows, const uint32_t* n_rows, uint32_t dpad,
+                      uint32_t dims, void* out, int scatter, uint32_t max_rows, cudaStream_t s) {
+    uint64_t total = (uint64_t)max_rows * dims;
+    unsigned blocks = (unsigned)std::min<uint64_t>((total + 255) / 256, 152 * 16);
+    if (!blocks) blocks = 1;
+    if (es == 8) k_pack_rows<double><<<blocks, 256, 0, s>>>((const double*)dense, rows, n_rows, dpad, dims, (double*)out, scatter);
+    else k_pack_rows<float><<<blocks, 256, 0, s>>>((const float*)dense, rows, n_rows, dpad, dims, (float*)out, scatter);
+}
+
+}  // namespace ep

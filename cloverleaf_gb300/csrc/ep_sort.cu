@@ -1,0 +1,162 @@
+// ep_sort.cu -- stable LSD radix sort of gradient items by feature id.
+//
+// Replaces the per-batch std::HashMap merge of src/algos/ep/mod.rs:223-233
+// and the racy Hogwild row writes (src/hogwild.rs:15-60): after a stable sort
+// by feature id the items of one feature are contiguous and keep their
+// emission order (anchor, role, occurrence), so the reduction that follows is
+// deterministic and can apply the reference's first-occurrence rule.
+//
+// One pass per 8-bit digit, three kernels per pass:
+//   k_radix_hist     per-tile digit counts -> hist[digit * ntiles + tile]
+//   k_radix_scan     exclusive scan of hist (digit-major = stable tile order)
+//   k_radix_scatter  per-tile stable ranks (warp match + per-warp counters)
+// The item count lives in device memory (BatchState::n_items), so the same
+// launches replay inside a CUDA graph for any batch.
+#include <cuda_runtime.h>
+
+#include "ep_device.cuh"
+#include "ep_internal.h"
+
+namespace ep {
+
+constexpr int SORT_THREADS = 256;          // 8 warps
+constexpr int SORT_ROUNDS = 8;             // rounds of 32 items per warp
+constexpr int SORT_TILE = SORT_THREADS * SORT_ROUNDS;   // 2048 items
+constexpr int SORT_MAX_GRID = 152 * 4;
+
+size_t radix_hist_entries(uint64_t cap) {
+    const uint64_t tiles = (cap + SORT_TILE - 1) / SORT_TILE;
+    return (size_t)(256 * (tiles ? tiles : 1));
+}
+
+__global__ void __launch_bounds__(SORT_THREADS) k_radix_hist(const uint32_t* __restrict__ keys, const BatchState* st,
+                                                             int shift, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[256];
+    const uint32_t n = st->n_items;
+    const uint32_t ntiles = (n + SORT_TILE - 1) / SORT_TILE;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        h[threadIdx.x] = 0;
+        __syncthreads();
+        const uint32_t base = tile * SORT_TILE;
+        const uint32_t end = min(base + SORT_TILE, n);
+        for (uint32_t i = base + threadIdx.x; i < end; i += SORT_THREADS)
+            atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+        __syncthreads();
+        hist[threadIdx.x * ntiles + tile] = h[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_radix_scan(const BatchState* st, uint32_t* hist) {
+    __shared__ uint32_t wsum[32];
+    const uint32_t n = st->n_items;
+    const uint32_t ntiles = (n + SORT_TILE - 1) / SORT_TILE;
+    const uint32_t len = 256 * ntiles;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    // each thread owns a contiguous run of `per` entries
+    const uint32_t per = (len + 1023) / 1024;
+    const uint32_t b = tid * per, e = min(b + per, len);
+    uint32_t local = 0;
+    for (uint32_t i = b; i < e; ++i) local += hist[i];
+    uint32_t incl = warp_incl_scan(local, lane);
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t s = warp_incl_scan(wsum[lane], lane);
+        wsum[lane] = s;
+    }
+    __syncthreads();
+    uint32_t run = (w ? wsum[w - 1] : 0) + incl - local;
+    for (uint32_t i = b; i < e; ++i) {
+        const uint32_t x = hist[i];
+        hist[i] = run;
+        run += x;
+    }
+}
+
+__global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(const uint32_t* __restrict__ keys_in,
+                                                                const uint32_t* __restrict__ vals_in,
+                                                                uint32_t* __restrict__ keys_out,
+                                                                uint32_t* __restrict__ vals_out,
+                                                                const BatchState* st, int shift,
+                                                                const uint32_t* __restrict__ hist) {
+    __shared__ uint32_t wcount[SORT_THREADS / 32][256];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t n = st->n_items;
+    const uint32_t ntiles = (n + SORT_TILE - 1) / SORT_TILE;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        for (int i = threadIdx.x; i < (SORT_THREADS / 32) * 256; i += SORT_THREADS) (&wcount[0][0])[i] = 0;
+        __syncthreads();
+        const uint32_t base = tile * SORT_TILE + w * (32 * SORT_ROUNDS);
+        uint32_t key[SORT_ROUNDS], val[SORT_ROUNDS], rank[SORT_ROUNDS];
+#pragma unroll
+        for (int r = 0; r < SORT_ROUNDS; ++r) {
+            const uint32_t i = base + r * 32 + lane;
+            const bool ok = i < n;
+            key[r] = ok ? keys_in[i] : 0u;
+            val[r] = ok ? (vals_in ? vals_in[i] : i) : 0u;
+            const uint32_t dig = ok ? ((key[r] >> shift) & 255u) : 256u;
+            const unsigned peers = __match_any_sync(FULL, dig);
+            const uint32_t before = ok ? wcount[w][dig] : 0u;
+            __syncwarp();
+            const int leader = __ffs(peers) - 1;
+            if (ok && lane == leader) wcount[w][dig] = before + __popc(peers);
+            __syncwarp();
+            rank[r] = before + __popc(peers & ((1u << lane) - 1u));
+        }
+        __syncthreads();
+        // exclusive prefix over warps, per digit
+        if (threadIdx.x < 256) {
+            uint32_t s = 0;
+#pragma unroll
+            for (int ww = 0; ww < SORT_THREADS / 32; ++ww) {
+                const uint32_t c = wcount[ww][threadIdx.x];
+                wcount[ww][threadIdx.x] = s;
+                s += c;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < SORT_ROUNDS; ++r) {
+            const uint32_t i = base + r * 32 + lane;
+            if (i < n) {
+                const uint32_t dig = (key[r] >> shift) & 255u;
+                const uint32_t pos = hist[dig * ntiles + tile] + wcount[w][dig] + rank[r];
+                keys_out[pos] = key[r];
+                vals_out[pos] = val[r];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Sorts keys[0, n_items) with values = original positions.  Ping-pongs
+// between (keys, keys_alt) and (idx, idx_alt); returns where the result is.
+void launch_radix_sort(BatchState* st, uint32_t* keys, uint32_t* keys_alt, uint32_t* idx, uint32_t* idx_alt,
+                       uint32_t* hist, uint64_t cap, int key_bits, uint32_t** sorted_keys, uint32_t** sorted_idx,
+                       cudaStream_t s) {
+    const uint64_t tiles = (cap + SORT_TILE - 1) / SORT_TILE;
+    const unsigned grid = (unsigned)(tiles < SORT_MAX_GRID ? (tiles ? tiles : 1) : SORT_MAX_GRID);
+    const int passes = key_bits <= 0 ? 1 : (key_bits + 7) / 8;
+    // pass p reads K[p % 2] and writes K[(p + 1) % 2]; values start as the
+    // identity (vals_in == nullptr) and then alternate between idx / idx_alt.
+    uint32_t* K[2] = {keys, keys_alt};
+    uint32_t* V[2] = {idx, idx_alt};
+    uint32_t *kin = nullptr, *vin = nullptr;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        kin = K[p & 1];
+        uint32_t* kout = K[(p + 1) & 1];
+        vin = p == 0 ? nullptr : V[(p - 1) & 1];
+        uint32_t* vout = V[p & 1];
+        k_radix_hist<<<grid, SORT_THREADS, 0, s>>>(kin, st, shift, hist);
+        k_radix_scan<<<1, 1024, 0, s>>>(st, hist);
+        k_radix_scatter<<<grid, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, st, shift, hist);
+        kin = kout;
+        vin = vout;
+    }
+    *sorted_keys = kin;
+    *sorted_idx = vin;
+}
+
+}  // namespace ep

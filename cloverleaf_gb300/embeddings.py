@@ -1,0 +1,282 @@
+"""NodeEmbeddings, Distance, FeatureAggregator and NodeEmbedder.
+
+Mirrors ``src/lib.rs:2009-2207`` (NodeEmbedder), ``:2536-2900``
+(NodeEmbeddings), ``src/embeddings.rs:24-173`` (EmbeddingStore),
+``src/distance.rs:132-198`` (distances) and ``src/algos/aggregator.rs:17-120``
+(Averaged / Weighted aggregators).  These run on the host with numpy: they
+are the inputs and outputs around the GPU training path, not part of it.
+"""
+from __future__ import annotations
+
+import enum
+from typing import Iterator, List, Optional, Sequence, Tuple, Union
+
+import numpy as np
+
+from .graph import FQNode, Graph, Vocab, _node_id
+
+
+class Distance(enum.Enum):
+    ALT = 0
+    Cosine = 1
+    Dot = 2
+    Euclidean = 3
+    Hamming = 4
+    Jaccard = 5
+
+    def compute(self, e1, e2) -> float:
+        """distance.rs:132-198: zero means identical."""
+        a = np.asarray(e1, np.float32)
+        b = np.asarray(e2, np.float32)
+        if self is Distance.Cosine:
+            d = float(np.dot(a, b)) / (float(np.sqrt(np.dot(a, a))) * float(np.sqrt(np.dot(b, b))))
+            return float("inf") if d != d else 1.0 - d
+        if self is Distance.Euclidean:
+            return float(np.sqrt(np.sum((a - b) ** 2)))
+        if self is Distance.Dot:
+            return -float(np.dot(a, b))
+        if self is Distance.ALT:
+            return float(np.max(np.abs(a - b))) if len(a) else 0.0
+        if self is Distance.Hamming:
+            return float(np.sum(a != b)) / len(a)
+        # Jaccard over sorted non-negative ids
+        i = j = m = 0
+        while i < len(a) and j < len(b) and a[i] >= 0 and b[j] >= 0:
+            if a[i] == b[j]:
+                m += 1; i += 1; j += 1
+            elif a[i] < b[j]:
+                i += 1
+            else:
+                j += 1
+        while i < len(a) and a[i] >= 0:
+            i += 1
+        while j < len(b) and b[j] >= 0:
+            j += 1
+        total = m + (i - m) + (j - m)
+        return 1.0 - m / total
+
+    def matrix(self, q: np.ndarray, X: np.ndarray) -> np.ndarray:
+        """Distances from query q to every row of X (Cosine/Euclidean/Dot
+        vectorised; others row by row)."""
+        if self is Distance.Cosine:
+            qn = np.sqrt(np.dot(q, q))
+            xn = np.sqrt(np.einsum("ij,ij->i", X, X))
+            with np.errstate(divide="ignore", invalid="ignore"):
+                s = (X @ q) / (xn * qn)
+            out = 1.0 - s
+            out[~np.isfinite(out)] = np.inf
+            return out
+        if self is Distance.Euclidean:
+            return np.sqrt(np.sum((X - q) ** 2, axis=1))
+        if self is Distance.Dot:
+            return -(X @ q)
+        return np.array([self.compute(q, x) for x in X], np.float32)
+
+
+class NodeEmbeddings:
+    """Dense row-major embeddings keyed by a vocabulary."""
+
+    def __init__(self, vocab: Vocab, table: np.ndarray, distance: Distance = Distance.Cosine):
+        self.vocab_ = vocab
+        self.table = np.ascontiguousarray(table, np.float32)
+        self.distance = distance
+
+    @classmethod
+    def new(cls, graph: Graph, dims: int, distance: Distance) -> "NodeEmbeddings":
+        return cls(graph.vocab_, np.zeros((graph.nodes(), dims), np.float32), distance)
+
+    @staticmethod
+    def new_from_list(lst: Sequence[Tuple[FQNode, Sequence[float]]], distance: Distance) -> "NodeEmbeddings":
+        v = Vocab()
+        rows = []
+        for (nt, nn), emb in lst:
+            v.get_or_insert(nt, nn)
+            rows.append(list(emb))
+        d = max((len(r) for r in rows), default=0)
+        t = np.zeros((len(v), d), np.float32)
+        for (nt, nn), emb in lst:
+            t[v.get_node_id(nt, nn), : len(emb)] = emb
+        return NodeEmbeddings(v, t, distance)
+
+    def __repr__(self) -> str:
+        return f"NodeEmbeddings<Nodes={self.len()}, Dims={self.dims()}, Distance={self.distance.name}>"
+
+    def contains(self, node: FQNode) -> bool:
+        return self.vocab_.get_node_id(node[0], node[1]) is not None
+
+    def get_embedding(self, node: FQNode) -> List[float]:
+        return self.table[_node_id(self.vocab_, node)].tolist()
+
+    def set_embedding(self, node: FQNode, embedding: Sequence[float]) -> None:
+        self.table[_node_id(self.vocab_, node), : len(embedding)] = embedding
+
+    def vocab(self) -> Iterator[FQNode]:
+        return iter(self.vocab_)
+
+    def get_distance(self) -> Distance:
+        return self.distance
+
+    def dims(self) -> int:
+        return self.table.shape[1]
+
+    def len(self) -> int:
+        return self.table.shape[0]
+
+    def __len__(self) -> int:
+        return self.len()
+
+    def __getitem__(self, idx: int):
+        n = self.len()
+        if idx < 0:
+            idx += n
+        if idx < 0 or idx >= n:
+            raise IndexError("Index larger than embedding store!")
+        return self.vocab_.get_name(idx), self.table[idx].tolist()
+
+    def l2norm(self) -> None:
+        """Row-wise L2 normalisation; zero rows untouched (lib.rs:2804-2814)."""
+        n = np.sqrt(np.einsum("ij,ij->i", self.table, self.table))
+        nz = n > 0
+        self.table[nz] /= n[nz, None]
+
+    def compute_distance(self, e1, e2) -> float:
+        def look(e):
+            if isinstance(e, tuple) and len(e) == 2 and isinstance(e[0], str):
+                return self.table[_node_id(self.vocab_, e)]
+            return np.asarray(e, np.float32)
+        return self.distance.compute(look(e1), look(e2))
+
+    def nearest_neighbor(self, emb, k: int, filter_type: Optional[Union[str, Sequence[str]]] = None):
+        """Brute-force top-k by the store's distance (embeddings.rs:149-173)."""
+        q = np.asarray(emb, np.float32)
+        d = self.distance.matrix(q, self.table).astype(np.float32)
+        if filter_type is not None:
+            types = {filter_type} if isinstance(filter_type, str) else set(filter_type)
+            mask = np.array([self.vocab_.get_node_type(i) in types for i in range(self.len())])
+            d = np.where(mask, d, np.float32(np.finfo(np.float32).max))
+        k = min(k, len(d))
+        idx = np.argpartition(d, k - 1)[:k] if k < len(d) else np.arange(len(d))
+        idx = idx[np.argsort(d[idx], kind="stable")]
+        return [(self.vocab_.get_name(int(i)), float(d[i])) for i in idx]
+
+    def save(self, path: str, comp_level: Optional[int] = None) -> None:
+        """``node_type\\tname\\t[v1,v2,...]`` lines (io.rs:44-76)."""
+        import gzip
+
+        opener = gzip.open if path.endswith(".gz") or comp_level is not None else open
+        with opener(path, "wt") as f:
+            for i in range(self.len()):
+                nt, nn = self.vocab_.get_name(i)
+                vals = ",".join(repr(float(x)) for x in self.table[i])
+                f.write(f"{nt}\t{nn}\t[{vals}]\n")
+
+    @staticmethod
+    def load(path: str, distance: Optional[Distance] = None, filter_type=None, chunk_size=None,
+             skip_rows=None) -> "NodeEmbeddings":
+        """Reads the format written by save (io.rs:134-198)."""
+        import gzip
+
+        types = None if filter_type is None else ({filter_type} if isinstance(filter_type, str) else set(filter_type))
+        v = Vocab()
+        rows = []
+        opener = gzip.open if path.endswith(".gz") else open
+        with opener(path, "rt") as f:
+            for i, line in enumerate(f):
+                if skip_rows and i < skip_rows:
+                    continue
+                p = line.rstrip("\n").split("\t")
+                if len(p) != 3:
+                    raise ValueError(f"Line {i + 1}: expected node_type<TAB>name<TAB>[embedding]")
+                if types is not None and p[0] not in types:
+                    continue
+                v.get_or_insert(p[0], p[1])
+                rows.append(np.array([float(x) for x in p[2].strip("[]").split(",") if x], np.float32))
+        d = max((len(r) for r in rows), default=0)
+        t = np.zeros((len(rows), d), np.float32)
+        for i, r in enumerate(rows):
+            t[i, : len(r)] = r
+        return NodeEmbeddings(v, t, distance or Distance.Cosine)
+
+
+class FeatureAggregator:
+    """How node embeddings are formed from feature embeddings."""
+
+    def __init__(self, kind: str, alpha: float = 0.0, unigrams: Optional[np.ndarray] = None,
+                 vocab: Optional[Vocab] = None):
+        self.kind, self.alpha, self.unigrams, self.vocab = kind, alpha, unigrams, vocab
+
+    @staticmethod
+    def Averaged() -> "FeatureAggregator":
+        return FeatureAggregator("averaged")
+
+    @staticmethod
+    def Weighted(alpha: float, feature_set) -> "FeatureAggregator":
+        """SIF weights alpha / (alpha + p(feature)) (aggregator.rs:50-120)."""
+        counts = feature_set.count_features().astype(np.float64)
+        p = (counts / max(counts.sum(), 1.0)).astype(np.float32)
+        return FeatureAggregator("weighted", float(alpha), p, feature_set.feature_vocab)
+
+    def __repr__(self) -> str:
+        return f"FeatureAggregator<{self.kind}>"
+
+
+class NodeEmbedder:
+    """Builds node embeddings from a FeatureSet and feature embeddings."""
+
+    def __init__(self, feat_agg: FeatureAggregator):
+        self.feat_agg = feat_agg
+
+    def __repr__(self) -> str:
+        return f"NodeEmbedder<aggregator={self.feat_agg!r}>"
+
+    def _translate(self, feat_set, feature_embeddings: NodeEmbeddings) -> Tuple[np.ndarray, np.ndarray]:
+        fptr, fids = feat_set.to_csr()
+        fv, ev = feat_set.feature_vocab, feature_embeddings.vocab_
+        if fv is ev:
+            return fptr, fids.astype(np.int64)
+        n = len(fv)
+        tr = np.full(n, -1, np.int64)
+        for i in range(n):
+            j = ev.get_node_id(*fv.get_name(i))
+            if j is not None:
+                tr[i] = j
+        return fptr, tr[fids]
+
+    def embed_feature_set(self, feat_set, feature_embeddings: NodeEmbeddings) -> NodeEmbeddings:
+        """Mean (or SIF-weighted mean) of each node's feature rows;
+        nodes without known features stay zero (lib.rs:2092-2124)."""
+        fptr, ids = self._translate(feat_set, feature_embeddings)
+        T = feature_embeddings.table
+        n = len(fptr) - 1
+        node = np.repeat(np.arange(n), np.diff(fptr).astype(np.int64))
+        keep = ids >= 0
+        node, ids = node[keep], ids[keep]
+        if self.feat_agg.kind == "weighted":
+            p = self.feat_agg.unigrams
+            w = (self.feat_agg.alpha / (self.feat_agg.alpha + p[ids])).astype(np.float32)
+        else:
+            w = np.ones(len(ids), np.float32)
+        out = np.zeros((n, T.shape[1]), np.float32)
+        np.add.at(out, node, T[ids] * w[:, None])
+        den = np.bincount(node, weights=w, minlength=n).astype(np.float32)
+        nz = den > 0
+        out[nz] /= den[nz, None]
+        return NodeEmbeddings(feat_set.vocab_, out, Distance.Cosine)
+
+    def embed_adhoc(self, features: Sequence[FQNode], feature_embeddings: NodeEmbeddings,
+                    strict: Optional[bool] = None) -> List[float]:
+        strict = True if strict is None else strict
+        ids = []
+        for nt, nn in features:
+            i = feature_embeddings.vocab_.get_node_id(nt, nn)
+            if i is not None:
+                ids.append(i)
+            elif strict:
+                raise KeyError(f"Feature {nt} {nn} does not exist!")
+        out = np.zeros(feature_embeddings.dims(), np.float32)
+        if ids:
+            out = feature_embeddings.table[ids].mean(0)
+        return out.tolist()
+
+    def bulk_embed_adhoc(self, features_set, feature_embeddings: NodeEmbeddings, strict=None):
+        return [self.embed_adhoc(f, feature_embeddings, strict) for f in features_set]

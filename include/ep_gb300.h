@@ -1,0 +1,230 @@
+/*
+ * ep_gb300.h -- C ABI of the GB300 (sm_103a) Embedding Propagation trainer.
+ *
+ * This is the boundary a host binding (the reference's PyO3 module, a Rust
+ * extern "C" crate, or the ctypes layer in cloverleaf_gb300/) calls in place
+ * of cloverleaf's CPU training path:
+ *
+ *   EmbeddingPropagator.__new__        src/lib.rs:1205-1307  -> ep_config + ep_create
+ *   EmbeddingPropagator.learn_features src/lib.rs:1327-1370  -> ep_upload_graph,
+ *        ep_upload_features, ep_set_table, ep_train, ep_get_table
+ *   EmbeddingPropagation::learn        src/algos/ep/mod.rs:80-287 -> ep_train
+ *
+ * Conventions: every function returns an ep_status (0 = EP_OK, negative =
+ * error) except ep_last_error/ep_destroy/ep_config_default.  No exception or
+ * signal crosses the ABI.  The caller owns every host buffer; the context owns
+ * all device memory.  One context per host thread; each context owns one CUDA
+ * stream.  Node ids are u32 (< 2^32 nodes), CSR row pointers are u64.
+ */
+#ifndef EP_GB300_H
+#define EP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EP_ABI_VERSION 1u
+
+typedef struct ep_ctx ep_ctx;
+
+typedef enum ep_status {
+    EP_OK = 0,
+    EP_ERR_INVALID_ARG = -1,   /* bad pointer, size or config value */
+    EP_ERR_CUDA = -2,          /* a CUDA runtime call failed */
+    EP_ERR_OOM = -3,           /* device allocation failed */
+    EP_ERR_STATE = -4,         /* call out of order (e.g. train before upload) */
+    EP_ERR_DEVICE = -5,        /* a kernel raised its device error flag */
+    EP_ERR_UNSUPPORTED = -6,   /* option not implemented on this path */
+    EP_ERR_NO_DEVICE = -7      /* no usable CUDA device */
+} ep_status;
+
+/* Loss (src/algos/ep/loss.rs:15-38, constructors src/lib.rs:988-1103). */
+enum { EP_LOSS_MARGIN = 0, EP_LOSS_STARSPACE = 1, EP_LOSS_CONTRASTIVE = 2 };
+/* Sample kind for max_nodes / max_features (src/algos/utils.rs:165-184). */
+enum { EP_SAMPLE_ALL = 0, EP_SAMPLE_FIXED = 1, EP_SAMPLE_PROB = 2 };
+/* Loss weighting (src/algos/ep/mod.rs:31-36, src/lib.rs:941-960). */
+enum { EP_LW_NONE = 0, EP_LW_LOG = 1, EP_LW_EXP = 2 };
+/* Implementation form.  PLAIN_FP32: FP32 table, one kernel per stage, the
+ * batch gradient materialised before a separate Adam kernel.  FUSED_BF16:
+ * BF16 table (stochastic rounding) with FP32 accumulation and FP32 Adam
+ * moments, gradient reduction fused with Adam, replayed as a CUDA graph. */
+enum { EP_FORM_PLAIN_FP32 = 0, EP_FORM_FUSED_BF16 = 1 };
+/* Gradient extraction.  REFERENCE: a feature's per-anchor gradient comes from
+ * the first role (h(v), ~h(v), h(u_1..R)) in which it has a finite gradient
+ * (src/algos/ep/mod.rs:361-378).  TRUE: all roles' contributions are summed
+ * (the derivative of the loss). */
+enum { EP_GRAD_REFERENCE = 0, EP_GRAD_TRUE = 1 };
+
+typedef struct ep_config {
+    uint32_t abi_version;        /* must be EP_ABI_VERSION */
+    float alpha;                 /* peak learning rate (lib.rs:1263, default 0.9) */
+    int32_t loss;                /* EP_LOSS_* (default margin) */
+    float gamma;                 /* margin / positive margin (default 1) */
+    float neg_margin;            /* contrastive negative margin */
+    uint32_t negatives;          /* negatives per anchor (default 1) */
+    uint32_t batch_size;         /* default 50 */
+    uint32_t dims;               /* default 100 */
+    uint32_t passes;             /* default 100 */
+    uint64_t seed;               /* default 20222022 (lib.rs:90) */
+    int32_t max_nodes_kind;      /* EP_SAMPLE_*, reconstruction neighbours */
+    float max_nodes;             /* Fixed: count, Prob: p */
+    int32_t max_features_kind;   /* EP_SAMPLE_* */
+    float max_features;
+    int32_t weighted_neighbor_sampling;
+    int32_t weighted_neighbor_averaging;
+    int32_t loss_weighting;      /* EP_LW_* */
+    float loss_weighting_exp;
+    float valid_pct;             /* default 0.1 */
+    uint32_t hard_negatives;     /* default 0 */
+    float noise;                 /* gradient noise, default 0 */
+    int32_t form;                /* EP_FORM_* */
+    int32_t grad_mode;           /* EP_GRAD_* */
+    int32_t device;              /* CUDA device ordinal */
+    int32_t use_graphs;          /* replay each batch as a CUDA graph */
+    int32_t autotune;            /* pick launch shapes by timing candidates */
+} ep_config;
+
+typedef struct ep_pass_stats {
+    uint32_t pass;               /* 1-based */
+    uint32_t batches;
+    float train_loss;            /* mean over batches of sum(loss)/batch_len (mod.rs:256-265) */
+    float valid_loss;            /* NaN when valid_pct == 0 (mod.rs:267-283) */
+    float lr_last;
+    uint32_t pad;
+    uint64_t anchors;            /* anchors processed */
+    uint64_t kept_anchors;       /* finite loss > 0 */
+    uint64_t nan_anchors;
+    uint64_t items;              /* emitted (feature, role) gradient items */
+    uint64_t gathered_rows;      /* G: distinct (role, feature) rows gathered */
+    uint64_t unique_rows;        /* U: rows updated by Adam */
+    uint64_t sampled_neighbors;  /* S */
+    double ms;                   /* device time of the pass's batches */
+    double alg_bytes;            /* G*d*s + U*d*(2s+16) + 4G + 4S + 8*B*(R+2) */
+    uint64_t launches;           /* kernels launched for these batches */
+} ep_pass_stats;
+
+/* Stages timed by ep_profile_batches. */
+enum { EP_STAGE_SAMPLE = 0,      /* batch set-up, sampling, item offsets */
+       EP_STAGE_FORWARD = 1,     /* gather-mean, loss, gradient directions, items */
+       EP_STAGE_SORT = 2,        /* radix sort of items by feature id */
+       EP_STAGE_REDUCE = 3,      /* per-feature reduction (+ fused Adam) and carries */
+       EP_STAGE_ADAM = 4,        /* separate Adam kernel (PLAIN form only) */
+       EP_STAGE_END = 5,         /* loss sums, counters, state advance */
+       EP_N_STAGES = 6 };
+
+/* Explicit samples for the parity hooks (host pointers).  Anchor a has
+ * neighbours nbr[nbr_ptr[a] .. nbr_ptr[a+1]) with base weights nbr_w and
+ * negatives negatives[a*R .. a*R+R), R = config.negatives. */
+typedef struct ep_batch_samples {
+    uint32_t n_anchors;
+    const uint32_t* anchors;
+    const uint32_t* nbr_ptr;     /* n_anchors + 1 */
+    const uint32_t* nbr;
+    const float* nbr_w;
+    const uint32_t* negatives;   /* n_anchors * R */
+} ep_batch_samples;
+
+/* Sparse batch gradient returned by ep_batch_grad (host pointers). */
+typedef struct ep_sparse_grad {
+    uint32_t capacity;           /* rows the caller allocated */
+    uint32_t n_rows;             /* out: touched feature rows */
+    uint32_t* feat_ids;          /* out: capacity entries, ascending */
+    float* rows;                 /* out: capacity * dims */
+    float* loss;                 /* out: n_anchors, after loss weighting */
+    int32_t* status;             /* out: n_anchors: 0 kept, 1 loss <= 0, 2 NaN */
+} ep_sparse_grad;
+
+/* Fills the reference defaults of EmbeddingPropagator.__new__
+ * (src/lib.rs:1262-1274) plus form = PLAIN_FP32, grad_mode = REFERENCE. */
+void ep_config_default(ep_config* cfg);
+
+/* Validates cfg, selects the device, creates the stream.
+ * Replaces EmbeddingPropagator::new (src/lib.rs:1205-1307). */
+int ep_create(const ep_config* cfg, ep_ctx** out);
+
+/* Uploads the graph once: CSR row pointers (n_nodes+1), u32 column ids and
+ * per-row CDF weights as produced by CumCSR::convert (src/graph.rs:399-422).
+ * w_cdf may be NULL (uniform weights).  Rejects non-monotone rows and ids
+ * >= n_nodes.  Replaces the borrow of Graph.graph at src/lib.rs:1345. */
+int ep_upload_graph(ep_ctx* ctx, uint64_t n_nodes, const uint64_t* row_ptr,
+                    const uint32_t* cols, const float* w_cdf);
+
+/* Uploads the node -> feature CSR (FeatureStore, src/feature_store.rs:19-25
+ * flattened): fptr (n_nodes+1), fids < n_feat.  Replaces &features.features
+ * at src/lib.rs:1347. */
+int ep_upload_features(ep_ctx* ctx, uint64_t n_nodes, const uint64_t* fptr,
+                       const uint32_t* fids, uint32_t n_feat);
+
+/* Sets the feature table: init (n_feat*dims FP32, row-major) or NULL for the
+ * reference's seeded init, rows U(-1,1)^d L2-normalised
+ * (src/algos/ep/mod.rs:100-110, 381-392).  Resets the Adam moments and the
+ * step counter (a warm start re-initialises them too, mod.rs:114-116). */
+int ep_set_table(ep_ctx* ctx, const float* init);
+
+/* Runs config.passes passes (src/algos/ep/mod.rs:156-284).  stats may be NULL;
+ * otherwise up to stats_len per-pass records are written. */
+int ep_train(ep_ctx* ctx, ep_pass_stats* stats, uint32_t stats_len);
+
+/* Runs n_batches more batches of the pass sequence (the per-batch step of
+ * mod.rs:174-261), crossing pass boundaries as ep_train would.  Accumulated
+ * counters of the batches run are written to *stats when non-NULL. */
+int ep_train_batches(ep_ctx* ctx, uint32_t n_batches, ep_pass_stats* stats);
+
+/* Measurement hook (no counterpart in the reference): runs n_batches more
+ * batches like ep_train_batches, but launched stage by stage with CUDA events
+ * between the stages, and writes the mean device time per batch of each stage
+ * to stage_ms[EP_N_STAGES].  Counters go to *stats when non-NULL. */
+int ep_profile_batches(ep_ctx* ctx, uint32_t n_batches, double* stage_ms, ep_pass_stats* stats);
+
+/* Parity hook: loss and reduced batch gradient for explicit samples from the
+ * current table, without updating it (mod.rs:183-233 for one batch). */
+int ep_batch_grad(ep_ctx* ctx, const ep_batch_samples* samples, ep_sparse_grad* out);
+
+/* Parity hook: one full optimizer step for explicit samples with learning
+ * rate lr and Adam time pass+1 (optimizer.rs:43-81). */
+int ep_batch_step(ep_ctx* ctx, const ep_batch_samples* samples, float lr, uint32_t pass);
+
+/* Copies the table out as n_feat*dims FP32.  Replaces the EmbeddingStore
+ * returned by learn (src/lib.rs:1362-1368). */
+int ep_get_table(ep_ctx* ctx, float* out);
+
+/* Device-pointer entry points behind the torch.autograd.Function binding.
+ * precision: 0 = FP32 table/compute, 1 = FP64 (gradient checks only).
+ * ep_ag_forward computes per-anchor losses (loss_dev, n_anchors values of the
+ * precision) for explicit samples against table_dev (n_feat*dims);
+ * ep_ag_backward consumes dloss_dev (n_anchors values) and writes the dense
+ * gradient dL/dtable into grad_dev (n_feat*dims, overwritten).  Both run on
+ * `stream` (a cudaStream_t, NULL = the context stream). */
+int ep_ag_forward(ep_ctx* ctx, const ep_batch_samples* samples, int precision,
+                  const void* table_dev, void* loss_dev, void* stream);
+int ep_ag_backward(ep_ctx* ctx, const void* dloss_dev, void* grad_dev, void* stream);
+
+/* Blocks until the context's work is done; reports device error flags. */
+int ep_synchronize(ep_ctx* ctx);
+
+/* Message of the last failing call on ctx (or of the last ep_create failure
+ * when ctx is NULL).  Valid until the next call on the same context. */
+const char* ep_last_error(const ep_ctx* ctx);
+
+void ep_destroy(ep_ctx* ctx);
+
+/* ---- host-side graph construction (src/graph.rs) --------------------- */
+
+/* CSR::construct_from_edges (src/graph.rs:70-142): optional deduplication
+ * (stable sort by (from, to), duplicate weights summed), nodes
+ * 0..max(from,to).  rows_out holds max_node+2 entries, cols_out/w_out
+ * n_edges entries; *n_nodes_out / *n_edges_out receive the sizes. */
+int ep_csr_from_edges(uint64_t n_edges, const uint32_t* from, const uint32_t* to,
+                      const float* w, int dedup, uint64_t* rows_out, uint32_t* cols_out,
+                      float* w_out, uint64_t* n_nodes_out, uint64_t* n_edges_out);
+
+/* CumCSR::convert (src/graph.rs:414-422, 664-691), in place. */
+int ep_cdf_convert(uint64_t n_nodes, const uint64_t* rows, float* w);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

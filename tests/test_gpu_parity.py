@@ -1,0 +1,176 @@
+"""Parity of the CUDA path with the oracle, through the C ABI.
+
+Per-batch checks use explicit samples (the reference's trajectory is
+nondeterministic, so parity is per batch from a frozen table).  Tolerances:
+FP32 loss and gradient within 1e-4 relative (max |diff| / max |oracle|) of
+the FP64 oracle; the BF16 form is compared on the BF16-rounded table, so the
+same 1e-4 bound applies to its FP32 accumulation.
+"""
+import numpy as np
+import pytest
+
+from cloverleaf_gb300 import _native
+from tests._cases import dense_from_sparse, random_problem, rel_err, sample_batch
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def make_ctx(prob, *, loss=1, gamma=0.5, R=4, form=0, grad_mode=0, weighting=0, lw_exp=0.5, neg_margin=0.1,
+             dims=None, table=None):
+    cfg = _native.default_config()
+    cfg.dims = dims or prob["dims"]
+    cfg.loss, cfg.gamma, cfg.neg_margin, cfg.negatives = loss, gamma, neg_margin, R
+    cfg.form, cfg.grad_mode = form, grad_mode
+    cfg.loss_weighting, cfg.loss_weighting_exp = weighting, lw_exp
+    cfg.batch_size = 64
+    cfg.passes = 1
+    cfg.valid_pct = 0.0
+    ctx = _native.Context(cfg)
+    ctx.upload_graph(prob["rows"], prob["cols"], None)
+    ctx.upload_features(prob["fptr"], prob["fids"], prob["n_feat"])
+    ctx.set_table(prob["table"] if table is None else table)
+    return ctx
+
+
+def oracle_batch(oracle, prob, smp, table, *, loss=1, gamma=0.5, grad_mode=0, weighting=0, lw_exp=0.5,
+                 neg_margin=0.1):
+    cfg = oracle.loss_cfg(loss=loss, gamma=gamma, neg_margin=neg_margin, grad_mode=grad_mode,
+                          loss_weighting=weighting, lw_exp=lw_exp)
+    return oracle.batch(prob["fptr"], prob["fids"], prob["n_feat"], table, prob["rows"], smp["anchors"],
+                        smp["nbr_ptr"], smp["nbr"], smp["nbr_w"], smp["neg"], cfg, "f64")
+
+
+def gpu_batch(ctx, prob, smp, dims=None):
+    s = _native.Context.samples(smp["anchors"], smp["nbr_ptr"], smp["nbr"], smp["nbr_w"], smp["neg"])
+    return ctx.batch_grad(s, prob["n_feat"], dims or prob["dims"])
+
+
+def check_parity(oracle, prob, smp, ctx, table, **kw):
+    ol, ost, og, ot = oracle_batch(oracle, prob, smp, table, **kw)
+    gl, gst, ids, rows = gpu_batch(ctx, prob, smp)
+    assert (gst == ost).all(), (gst, ost)
+    kept = ost == 0
+    assert rel_err(gl[kept], ol[kept]) < TOL
+    g, t = dense_from_sparse(ids, rows, prob["n_feat"], prob["dims"])
+    assert (t == ot).all(), np.nonzero(t != ot)
+    assert np.isfinite(rows).all()
+    assert rel_err(g, og) < TOL, rel_err(g, og)
+    return ids, rows
+
+
+@pytest.mark.parametrize("dims", [16, 64, 100, 256])
+@pytest.mark.parametrize("loss", [0, 1, 2])
+def test_batch_grad_plain_fp32(oracle, loss, dims):
+    prob = random_problem(100 + dims, n=300, n_feat=200, dims=dims)
+    smp = sample_batch(5 + loss, prob, B=96, K=5, R=4)
+    gamma = 1.0 if loss == 0 else 0.5
+    ctx = make_ctx(prob, loss=loss, gamma=gamma)
+    check_parity(oracle, prob, smp, ctx, prob["table"], loss=loss, gamma=gamma)
+
+
+@pytest.mark.parametrize("grad_mode", [0, 1])
+@pytest.mark.parametrize("weighting", [0, 1, 2])
+def test_batch_grad_modes_and_weighting(oracle, grad_mode, weighting):
+    prob = random_problem(31, n=150, n_feat=60, dims=32, feats=(1, 8))   # many shared features
+    smp = sample_batch(41, prob, B=128, K=6, R=5, weighted=True)
+    ctx = make_ctx(prob, loss=0, gamma=1.0, R=5, grad_mode=grad_mode, weighting=weighting)
+    check_parity(oracle, prob, smp, ctx, prob["table"], loss=0, gamma=1.0, grad_mode=grad_mode,
+                 weighting=weighting)
+
+
+def test_batch_grad_hot_feature_spans_chunks(oracle):
+    # one feature on every node: its items span many reducer chunks, which
+    # exercises the carry/fix-up path and the look-back for the first role
+    prob = random_problem(5, n=400, n_feat=40, dims=32, feats=(2, 6))
+    fptr, fids = prob["fptr"].copy(), prob["fids"].copy()
+    fids[fptr[:-1].astype(np.int64)] = 0
+    prob.update(fids=fids)
+    smp = sample_batch(6, prob, B=256, K=8, R=6)
+    for grad_mode in (0, 1):
+        ctx = make_ctx(prob, loss=1, gamma=0.5, R=6, grad_mode=grad_mode)
+        check_parity(oracle, prob, smp, ctx, prob["table"], loss=1, gamma=0.5, grad_mode=grad_mode)
+
+
+def test_nan_and_empty_roles(oracle):
+    # t == h for some anchors (anchor and neighbour share their only
+    # feature), empty neighbour lists, a negative equal to the reconstruction
+    prob = random_problem(9, n=50, n_feat=30, dims=8, feats=(1, 1))
+    smp = sample_batch(10, prob, B=40, K=1, R=3)
+    fids = prob["fids"].copy()
+    for a in range(0, 40, 3):
+        j = smp["nbr_ptr"][a]
+        if smp["nbr_ptr"][a + 1] > j:
+            fids[int(prob["fptr"][smp["nbr"][j]])] = fids[int(prob["fptr"][smp["anchors"][a]])]
+    prob.update(fids=fids)
+    # an anchor without neighbours -> NaN loss (status 2)
+    smp["nbr_ptr"] = smp["nbr_ptr"].copy()
+    cut = int(smp["nbr_ptr"][1] - smp["nbr_ptr"][0])
+    smp["nbr"] = smp["nbr"][cut:]
+    smp["nbr_w"] = smp["nbr_w"][cut:]
+    smp["nbr_ptr"] = np.concatenate([[0], smp["nbr_ptr"][1:] - cut]).astype(np.uint32)
+    ctx = make_ctx(prob, loss=0, gamma=1.0, R=3)
+    ol, ost, og, ot = oracle_batch(oracle, prob, smp, prob["table"], loss=0, gamma=1.0)
+    assert ost[0] == 2
+    check_parity(oracle, prob, smp, ctx, prob["table"], loss=0, gamma=1.0)
+
+
+def test_batch_grad_fused_bf16(oracle):
+    prob = random_problem(77, n=300, n_feat=200, dims=128)
+    smp = sample_batch(78, prob, B=128, K=5, R=4)
+    ctx = make_ctx(prob, loss=1, gamma=0.5, form=1)
+    table_bf16 = ctx.get_table(prob["n_feat"], prob["dims"])     # BF16-rounded values
+    assert not np.array_equal(table_bf16, prob["table"])
+    check_parity(oracle, prob, smp, ctx, table_bf16, loss=1, gamma=0.5)
+
+
+def test_batch_grad_deterministic(oracle):
+    prob = random_problem(3, n=400, n_feat=100, dims=64)
+    smp = sample_batch(4, prob, B=256, K=10, R=5)
+    ctx = make_ctx(prob, loss=1, gamma=0.5, R=5)
+    a = gpu_batch(ctx, prob, smp)
+    b = gpu_batch(ctx, prob, smp)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_batch_step_adam_plain(oracle):
+    prob = random_problem(12, n=200, n_feat=120, dims=32)
+    smp = sample_batch(13, prob, B=64, K=5, R=4)
+    ctx = make_ctx(prob, loss=1, gamma=0.5)
+    lr, pass_idx = 0.05, 1
+    s = _native.Context.samples(smp["anchors"], smp["nbr_ptr"], smp["nbr"], smp["nbr_w"], smp["neg"])
+    ctx.batch_step(s, lr, pass_idx)
+    got = ctx.get_table(prob["n_feat"], prob["dims"])
+    _, _, og, ot = oracle_batch(oracle, prob, smp, prob["table"], loss=1, gamma=0.5)
+    z = np.zeros_like(prob["table"])
+    exp, _, _ = oracle.adam(prob["table"], z, z, og.astype(np.float32), ot.astype(np.uint8), lr, pass_idx)
+    # Adam maps a tiny gradient to an update of about +-lr (m/sqrt(v) ~ sign(g)),
+    # so entries whose gradient is at rounding level may differ by up to 2*lr
+    big = np.abs(og) > 1e-3 * np.abs(og).max()
+    diff = np.abs(got - exp)
+    assert diff[big].max() < 1e-5 + 1e-4 * np.abs(exp[big]).max()
+    assert diff.max() <= 2 * lr + 1e-5
+    assert np.array_equal(got[~ot], prob["table"][~ot])     # untouched rows unchanged
+
+
+def test_bad_inputs_fail_cleanly():
+    prob = random_problem(1, n=20, n_feat=10, dims=8)
+    ctx = make_ctx(prob)
+    smp = sample_batch(2, prob, B=4, K=2, R=4)
+    smp["anchors"] = smp["anchors"].copy()
+    smp["anchors"][0] = 10_000
+    with pytest.raises(_native.NativeError) as e:
+        gpu_batch(ctx, prob, smp)
+    assert e.value.code == -1
+    bad = dict(prob)
+    bad["cols"] = prob["cols"].copy()
+    bad["cols"][0] = 999
+    cfg = _native.default_config()
+    cfg.dims = 8
+    c2 = _native.Context(cfg)
+    with pytest.raises(_native.NativeError):
+        c2.upload_graph(bad["rows"], bad["cols"], None)
+    with pytest.raises(_native.NativeError):
+        c2.train(1)         # nothing uploaded

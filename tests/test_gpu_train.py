@@ -1,0 +1,141 @@
+"""End-to-end training on the GPU through the drop-in Python API, compared
+with the oracle's CPU training loop (community recall@10 within 1 point)."""
+import numpy as np
+import pytest
+
+import cloverleaf_gb300 as cl
+from cloverleaf_gb300 import _native, datagen
+from tests._eval import community_recall
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sbm10k():
+    return datagen.workload("sbm10k")
+
+
+def gpu_learn(w, loss, form, seed=20222022, passes=None, valid_pct=0.0, **extra):
+    ep = w["ep"]
+    g = cl.Graph.from_csr(w["rows"], w["cols"], w["weights"])
+    fs = cl.FeatureSet.from_csr(g, w["fptr"], w["fids"], w["n_feat"])
+    lossobj = cl.EPLoss.starspace(ep["gamma"], ep["negatives"]) if loss == "starspace" else \
+        cl.EPLoss.margin(ep["gamma"], ep["negatives"])
+    prop = cl.EmbeddingPropagator(alpha=ep["alpha"], loss=lossobj, batch_size=ep["batch_size"], dims=ep["dims"],
+                                  passes=passes or ep["passes"], seed=seed, max_nodes=ep["max_nodes"],
+                                  valid_pct=valid_pct, indicator=False, form=form, **extra)
+    emb = prop.learn_features(g, fs)
+    return emb, prop.last_stats
+
+
+def oracle_learn(oracle, w, loss):
+    ep = w["ep"]
+    table, st = oracle.train(w["rows"], w["cols"], w["weights"], w["fptr"], w["fids"], w["n_feat"], dims=ep["dims"],
+                             alpha=ep["alpha"], loss=oracle.LOSS_STARSPACE if loss == "starspace" else
+                             oracle.LOSS_MARGIN, gamma=ep["gamma"], negatives=ep["negatives"],
+                             batch_size=ep["batch_size"], passes=ep["passes"],
+                             max_nodes=(oracle.SAMPLE_FIXED, ep["max_nodes"]), threads=0)
+    return table
+
+
+@pytest.mark.parametrize("form", ["plain", "fused"])
+@pytest.mark.parametrize("loss", ["starspace", "margin"])
+def test_recall_matches_cpu_reference(oracle, sbm10k, loss, form):
+    w = sbm10k
+    emb, stats = gpu_learn(w, loss, form)
+    assert emb.table.shape == (w["n_feat"], w["ep"]["dims"])
+    assert np.isfinite(emb.table).all()
+    assert len(stats) == w["ep"]["passes"]
+    assert stats[-1]["train_loss"] < stats[0]["train_loss"]
+    r_gpu = community_recall(w["fptr"], w["fids"], emb.table, w["community"])
+    r_cpu = community_recall(w["fptr"], w["fids"], oracle_learn(oracle, w, loss), w["community"])
+    assert abs(r_gpu - r_cpu) <= 0.01, (r_gpu, r_cpu)
+
+
+def test_training_is_deterministic(sbm10k):
+    a, _ = gpu_learn(sbm10k, "starspace", "fused", passes=2)
+    b, _ = gpu_learn(sbm10k, "starspace", "fused", passes=2)
+    assert np.array_equal(a.table, b.table)
+    c, _ = gpu_learn(sbm10k, "starspace", "plain", passes=2)
+    d, _ = gpu_learn(sbm10k, "starspace", "plain", passes=2)
+    assert np.array_equal(c.table, d.table)
+
+
+def test_pass_stats_and_validation(sbm10k):
+    w = sbm10k
+    emb, stats = gpu_learn(w, "starspace", "fused", passes=2, valid_pct=0.1)
+    n_train = w["rows"].shape[0] - 1 - int(np.float32(10_000) * np.float32(0.1))
+    for s in stats:
+        assert s["anchors"] == n_train
+        assert s["batches"] == -(-n_train // w["ep"]["batch_size"])
+        assert 0 < s["kept_anchors"] <= s["anchors"]
+        assert s["gathered_rows"] <= s["items"]
+        assert 0 < s["unique_rows"] <= w["n_feat"] * s["batches"]
+        assert s["alg_bytes"] > 0 and s["ms"] > 0
+        assert np.isfinite(s["valid_loss"]) and s["valid_loss"] > 0
+
+
+def test_drop_in_api_strings():
+    # the reference's own usage: GraphBuilder + FeatureSet with string ids
+    b = cl.GraphBuilder()
+    rng = np.random.default_rng(0)
+    for i in range(200):
+        for j in rng.integers(0, 200, 3):
+            if i != j:
+                b.add_edge(("user", str(i)), ("user", str(int(j))), 1.0, cl.EdgeType.Undirected)
+    g = b.build_graph()
+    fs = cl.FeatureSet.new_from_graph(g)
+    for i in range(0, 200, 2):   # odd nodes stay featureless
+        fs.set_features(("user", str(i)), [("feat", f"t{i % 7}"), ("feat", f"t{i % 11}")])
+    ep = cl.EmbeddingPropagator(alpha=0.05, loss=cl.EPLoss.starspace(0.5, 3), batch_size=32, dims=16, passes=3,
+                                max_nodes=5, indicator=False)
+    emb = ep.learn_features(g, fs)
+    # fill_missing_nodes gave every odd node its own ("node", id) feature
+    assert fs.get_features(("user", "1"))[0][0] == "node"
+    assert emb.len() == fs.num_features() and emb.dims() == 16
+    assert emb.contains(("feat", "t3"))
+    nn = emb.nearest_neighbor(emb.get_embedding(("feat", "t3")), 3)
+    assert nn[0][0] == ("feat", "t3")
+
+
+def test_warm_start_moves_table_out(sbm10k):
+    w = sbm10k
+    emb, _ = gpu_learn(w, "starspace", "plain", passes=1)
+    init = emb.table.copy()
+    ep = w["ep"]
+    g = cl.Graph.from_csr(w["rows"], w["cols"], w["weights"])
+    fs = cl.FeatureSet.from_csr(g, w["fptr"], w["fids"], w["n_feat"])
+    prop = cl.EmbeddingPropagator(alpha=ep["alpha"], loss=cl.EPLoss.starspace(0.5, 5), batch_size=256, dims=64,
+                                  passes=1, max_nodes=10, valid_pct=0.0, indicator=False)
+    out = prop.learn_features(g, fs, emb)
+    assert emb.dims() == 0                 # moved out, as lib.rs:1337-1341
+    assert out.table.shape == init.shape
+    assert not np.array_equal(out.table, init)
+
+
+def test_unsupported_options_raise():
+    with pytest.raises(NotImplementedError):
+        cl.EmbeddingPropagator(attention=8)
+    with pytest.raises(ValueError):
+        cl.EmbeddingPropagator(max_features=-1.0)
+
+
+def test_large_chung_lu_batches():
+    # 2% of the 10M-node workload: same degree and feature distributions
+    w = datagen.workload("cl10m", scale=0.02)
+    cfg = _native.default_config()
+    ep = w["ep"]
+    cfg.dims, cfg.negatives, cfg.loss, cfg.gamma = ep["dims"], ep["negatives"], _native.LOSS_STARSPACE, ep["gamma"]
+    cfg.batch_size, cfg.alpha, cfg.passes, cfg.valid_pct = 2048, ep["alpha"], 1, 0.0
+    cfg.max_nodes_kind, cfg.max_nodes = _native.SAMPLE_FIXED, float(ep["max_nodes"])
+    cfg.form = _native.FORM_FUSED_BF16
+    ctx = _native.Context(cfg)
+    ctx.upload_graph(w["rows"], w["cols"], None)
+    ctx.upload_features(w["fptr"], w["fids"], w["n_feat"])
+    ctx.set_table(None)
+    s1 = ctx.train_batches(40)
+    s2 = ctx.train_batches(40)
+    assert s1["kept_anchors"] > 0 and s1["nan_anchors"] == 0
+    assert s2["train_loss"] < s1["train_loss"]
+    t = ctx.get_table(w["n_feat"], ep["dims"])
+    assert np.isfinite(t).all()
