@@ -103,6 +103,9 @@ def allsum(x, world):
     return float(t.item())
 
 
+_PINNED = []   # keeps the page-locked tensors behind the numpy views alive
+
+
 def pinned_copy(a: np.ndarray) -> np.ndarray:
     """A copy of `a` in page-locked host memory (so host->device copies run at
     full link speed)."""
@@ -110,9 +113,9 @@ def pinned_copy(a: np.ndarray) -> np.ndarray:
 
     t = torch.empty(a.shape, dtype={np.uint64: torch.int64, np.uint32: torch.int32,
                                     np.float32: torch.float32}[a.dtype.type], pin_memory=True)
+    _PINNED.append(t)
     out = t.numpy().view(a.dtype)
     out[...] = a
-    out._owner = t  # noqa: keep the pinned tensor alive
     return out
 
 
