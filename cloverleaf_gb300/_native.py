@@ -246,7 +246,7 @@ class Context:
         check(lib().ep_train_batches(self._h, n, ctypes.byref(st)), self._h, "ep_train_batches")
         return st.as_dict()
 
-    STAGES = ("sample", "forward", "sort", "reduce", "adam", "end")
+    STAGES = ("sample", "forward", "sort", "reduce", "fixup", "adam", "end")
 
     def profile_batches(self, n):
         ms = (ctypes.c_double * len(self.STAGES))()

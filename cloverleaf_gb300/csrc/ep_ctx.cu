@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -200,6 +201,10 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     c->tt = cfg->form == EP_FORM_FUSED_BF16 ? TT_BF16 : TT_F32;
     c->R = cfg->negatives;
     c->NR = c->R + 2;
+    if (const char* ch = getenv("EP_REDUCE_CHUNK")) {   // reducer items per warp (tuning)
+        const long v = atol(ch);
+        if (v >= 32 && v <= (1l << 20)) c->chunk = (uint32_t)v;
+    }
     *out = c;
     return EP_OK;
 }
@@ -528,6 +533,7 @@ static void sort_and_reduce(ep_ctx* c, BatchState* st, int tt, int out_mode, voi
     if (out_mode == OUT_DENSE) cudaMemsetAsync(c->n_touched.p, 0, 4, s);
     ReduceParams rp = reduce_params(c, st, out_mode, table);
     launch_reduce(tt, (int)c->vpl, rp, c->items_cap, s);
+    launch_fixup(tt, (int)c->vpl, rp, c->items_cap, s);
 }
 
 // Kernels launched per training batch.
@@ -560,6 +566,8 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr) {
     ReduceParams rp = reduce_params(c, st, plain ? OUT_DENSE : OUT_ADAM, c->table.p);
     launch_reduce(c->tt, (int)c->vpl, rp, c->items_cap, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_REDUCE], s);
+    launch_fixup(c->tt, (int)c->vpl, rp, c->items_cap, s);
+    if (ev) cudaEventRecord(ev[EP_STAGE_FIXUP], s);
     if (plain)
         launch_adam_dense(c->tt, (int)c->vpl, st, c->table.p, c->m.as<float>(), c->v.as<float>(), c->gdense.as<float>(),
                           c->touched.as<uint32_t>(), c->n_touched.as<uint32_t>(), c->dpad,

@@ -163,6 +163,7 @@ void launch_radix_sort(BatchState* st, uint32_t* keys, uint32_t* keys_alt, uint3
                        uint32_t* idx_alt, uint32_t* hist, uint64_t cap, int key_bits,
                        uint32_t** sorted_keys, uint32_t** sorted_idx, cudaStream_t s);
 void launch_reduce(int tt, int vpl, const ReduceParams& p, uint64_t items_cap, cudaStream_t s);
+void launch_fixup(int tt, int vpl, const ReduceParams& p, uint64_t items_cap, cudaStream_t s);
 void launch_adam_dense(int tt, int vpl, BatchState* st, void* table, float* m, float* v,
                        const float* g, const uint32_t* touched, const uint32_t* n_touched,
                        uint32_t dpad, uint32_t max_rows, uint64_t seed, cudaStream_t s);

@@ -17,9 +17,10 @@
 // chunk, walking its items in order (so no atomics on gradient rows).  A
 // feature entirely inside a chunk is finished in place: Adam on the row
 // (optimizer.rs:43-81) or a dense gradient row.  A feature spanning chunks
-// leaves partial sums (carries); k_fixup adds them in chunk order and
-// finishes the row, so the summation order is fixed and results are
-// bit-reproducible.
+// leaves partial sums (carries); k_fixup adds them in a fixed order and
+// finishes the row, so results are bit-reproducible.  A feature none of whose
+// items is kept is not in the batch's gradient map and is left untouched
+// (no Adam step), as in mod.rs:223-233.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <type_traits>
@@ -30,7 +31,11 @@
 namespace ep {
 
 constexpr uint32_t NONE = 0xffffffffu;
-enum : uint32_t { CF_HEAD = 1u, CF_THROUGH = 2u, CF_OWNER = 4u };
+// Chunk flags: HEAD = the chunk's first feature started in an earlier chunk
+// (its partial sum is in carry_head); THROUGH = that feature also continues
+// past the chunk; OWNER = the chunk's last feature starts here and continues
+// (partial in carry_tail); *_KEPT = the partial contains at least one kept item.
+enum : uint32_t { CF_HEAD = 1u, CF_THROUGH = 2u, CF_OWNER = 4u, CF_HEAD_KEPT = 8u, CF_TAIL_KEPT = 16u };
 constexpr int RED_THREADS = 256;
 constexpr uint32_t RED_MAX_CTAS = 152 * 8;
 
@@ -160,6 +165,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
         uint32_t pend = NONE;
         A pend_c = 0;
         bool started_here = !head_partial;
+        bool any_kept = false;
         uint32_t flags = 0;
         for (uint32_t ib = i0; ib < i1; ib += 32) {
             const uint32_t i = ib + lane;
@@ -183,16 +189,19 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
                 if (f != cur_f) {
                     flush_pending<A, VPL>(p, pend, pend_c, acc, lane, lane_on);
                     if (started_here) {
-                        finish_row<T, A, VPL>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step);
-                        ++u_cnt;
+                        if (any_kept) {
+                            finish_row<T, A, VPL>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step);
+                            ++u_cnt;
+                        }
                     } else {
                         if (lane_on) store_row<A, VPL, A>((A*)p.carry_head + (uint64_t)c * p.dpad, lane, acc);
-                        flags |= CF_HEAD;
+                        flags |= CF_HEAD | (any_kept ? CF_HEAD_KEPT : 0u);
                     }
 #pragma unroll
                     for (int k = 0; k < VPL; ++k) acc[k] = 0;
                     cur_f = f;
                     started_here = true;
+                    any_kept = false;
                     cur_anchor = s / NR;
                     chosen = NONE;
                 } else if (s / NR != cur_anchor) {
@@ -207,6 +216,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
                     keep = vv && s == chosen;
                 }
                 if (keep) {
+                    any_kept = true;
                     if (s == pend) {
                         pend_c += cc;
                     } else {
@@ -220,16 +230,17 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
         flush_pending<A, VPL>(p, pend, pend_c, acc, lane, lane_on);
         const bool cont = i1 < M && p.skey[i1] == cur_f;
         if (started_here && !cont) {
-            finish_row<T, A, VPL>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step);
-            ++u_cnt;
+            if (any_kept) {
+                finish_row<T, A, VPL>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step);
+                ++u_cnt;
+            }
         } else if (!started_here) {
             if (lane_on) store_row<A, VPL, A>((A*)p.carry_head + (uint64_t)c * p.dpad, lane, acc);
-            flags |= CF_HEAD | (cont ? CF_THROUGH : 0u);
+            flags |= CF_HEAD | (cont ? CF_THROUGH : 0u) | (any_kept ? CF_HEAD_KEPT : 0u);
         } else {
             if (lane_on) store_row<A, VPL, A>((A*)p.carry_tail + (uint64_t)c * p.dpad, lane, acc);
             if (lane == 0) p.carry_f[c] = cur_f;
-            flags |= CF_OWNER;
-            ++u_cnt;
+            flags |= CF_OWNER | (any_kept ? CF_TAIL_KEPT : 0u);
         }
         if (lane == 0) p.carry_flags[c] = flags;
     }
@@ -240,36 +251,78 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
     }
 }
 
+// k_fixup: one CTA per owner chunk (a chunk whose last feature continues into
+// later chunks).  The feature's last item is found by binary search, so the
+// chunks holding its partial sums are known up front; warp w adds partials
+// c+1+w, c+9+w, ... in increasing order, then warp 0 adds the owner's partial
+// and the eight warp sums in warp order: a fixed order, independent of timing.
 template <typename T, typename A, int VPL>
 __global__ void __launch_bounds__(RED_THREADS) k_fixup(ReduceParams p) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    constexpr int NWARP = RED_THREADS / 32;
+    extern __shared__ __align__(16) unsigned char fix_smem[];
+    A* wsum = reinterpret_cast<A*>(fix_smem);          // [NWARP][dpad]
+    __shared__ uint32_t s_last, s_kept;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint32_t M = p.st->n_items;
-    const uint32_t nchunks = (M + p.chunk - 1) / p.chunk;
+    const uint32_t C = p.chunk;
+    const uint32_t nchunks = (M + C - 1) / C;
     const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
     const float lr = p.st->lr, bc1 = p.st->bc1, bc2 = p.st->bc2;
     const uint32_t step = (uint32_t)p.st->step;
-    for (uint32_t c = gw; c < nchunks; c += nw) {
-        if (!(p.carry_flags[c] & CF_OWNER)) continue;
+    unsigned long long u_cnt = 0;
+    for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const uint32_t fl = p.carry_flags[c];
+        if (!(fl & CF_OWNER)) continue;                 // CTA-uniform
         const uint32_t f = p.carry_f[c];
-        A acc[VPL];
-        if (lane_on) RowIO<A, VPL>::load_cg((const A*)p.carry_tail + (uint64_t)c * p.dpad, lane, acc);
-        else {
-#pragma unroll
-            for (int k = 0; k < VPL; ++k) acc[k] = 0;
+        if (threadIdx.x == 0) {
+            // last position holding f: upper bound in skey[(c+1)*C, M)
+            uint32_t lo = (c + 1) * C, hi = M;          // skey[lo] == f is guaranteed
+            while (hi - lo > 1) {
+                const uint32_t mid = lo + (hi - lo) / 2;
+                if (p.skey[mid] == f) lo = mid; else hi = mid;
+            }
+            s_last = lo / C;
+            s_kept = 0;
         }
-        for (uint32_t j = c + 1; j < nchunks; ++j) {
+        __syncthreads();
+        const uint32_t last = s_last;
+        A acc[VPL];
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) acc[k] = 0;
+        uint32_t kept = 0;
+        for (uint32_t j = c + 1 + w; j <= last; j += NWARP) {
+            kept |= p.carry_flags[j] & CF_HEAD_KEPT;
             if (lane_on) {
                 A h[VPL];
                 RowIO<A, VPL>::load_cg((const A*)p.carry_head + (uint64_t)j * p.dpad, lane, h);
 #pragma unroll
                 for (int k = 0; k < VPL; ++k) acc[k] += h[k];
             }
-            if (!(p.carry_flags[j] & CF_THROUGH)) break;
         }
-        finish_row<T, A, VPL>(p, f, acc, lane, lane_on, lr, bc1, bc2, step);
+        if (lane_on) store_row<A, VPL, A>(wsum + (size_t)w * p.dpad, lane, acc);
+        if (lane == 0 && kept) atomicOr(&s_kept, 1u);
+        __syncthreads();
+        if (w == 0) {
+            A tot[VPL];
+            if (lane_on) RowIO<A, VPL>::load_cg((const A*)p.carry_tail + (uint64_t)c * p.dpad, lane, tot);
+            else {
+#pragma unroll
+                for (int k = 0; k < VPL; ++k) tot[k] = 0;
+            }
+            for (int ww = 0; ww < NWARP; ++ww) {
+                if (lane_on) {
+#pragma unroll
+                    for (int k = 0; k < VPL; ++k) tot[k] += wsum[(size_t)ww * p.dpad + lane * VPL + k];
+                }
+            }
+            if ((fl & CF_TAIL_KEPT) || s_kept) {
+                finish_row<T, A, VPL>(p, f, tot, lane, lane_on, lr, bc1, bc2, step);
+                ++u_cnt;
+            }
+        }
+        __syncthreads();
     }
+    if (threadIdx.x == 0 && u_cnt) atomicAdd(&p.st->unique_rows, u_cnt);
 }
 
 // PLAIN form: Adam over the touched list, reading the dense gradient rows.
@@ -296,25 +349,44 @@ __global__ void __launch_bounds__(RED_THREADS) k_adam_dense(BatchState* st, T* t
     }
 }
 
-template <typename T, typename A>
-static void red_dispatch(int vpl, const ReduceParams& p, uint64_t cap, cudaStream_t s) {
+template <typename T, typename A, int VPL>
+static void red_launch(const ReduceParams& p, uint64_t cap, cudaStream_t s, int which) {
     const uint32_t nch = reduce_chunks(cap, p.chunk);
     const uint32_t warps = nch ? nch : 1;
-    uint32_t ctas = (warps + RED_THREADS / 32 - 1) / (RED_THREADS / 32);
-    if (ctas > RED_MAX_CTAS) ctas = RED_MAX_CTAS;
-    switch (vpl) {
-        case 1: k_reduce<T, A, 1><<<ctas, RED_THREADS, 0, s>>>(p); k_fixup<T, A, 1><<<ctas, RED_THREADS, 0, s>>>(p); break;
-        case 2: k_reduce<T, A, 2><<<ctas, RED_THREADS, 0, s>>>(p); k_fixup<T, A, 2><<<ctas, RED_THREADS, 0, s>>>(p); break;
-        case 4: k_reduce<T, A, 4><<<ctas, RED_THREADS, 0, s>>>(p); k_fixup<T, A, 4><<<ctas, RED_THREADS, 0, s>>>(p); break;
-        case 8: k_reduce<T, A, 8><<<ctas, RED_THREADS, 0, s>>>(p); k_fixup<T, A, 8><<<ctas, RED_THREADS, 0, s>>>(p); break;
-        default: k_reduce<T, A, 16><<<ctas, RED_THREADS, 0, s>>>(p); k_fixup<T, A, 16><<<ctas, RED_THREADS, 0, s>>>(p); break;
+    if (which == 0) {
+        uint32_t ctas = (warps + RED_THREADS / 32 - 1) / (RED_THREADS / 32);
+        if (ctas > RED_MAX_CTAS) ctas = RED_MAX_CTAS;
+        k_reduce<T, A, VPL><<<ctas, RED_THREADS, 0, s>>>(p);
+    } else {
+        uint32_t ctas = std::min<uint32_t>(warps, 152 * 4);
+        const size_t smem = (size_t)(RED_THREADS / 32) * p.dpad * sizeof(A);
+        k_fixup<T, A, VPL><<<ctas, RED_THREADS, smem, s>>>(p);
     }
 }
 
+template <typename T, typename A>
+static void red_dispatch(int vpl, const ReduceParams& p, uint64_t cap, cudaStream_t s, int which) {
+    switch (vpl) {
+        case 1: red_launch<T, A, 1>(p, cap, s, which); break;
+        case 2: red_launch<T, A, 2>(p, cap, s, which); break;
+        case 4: red_launch<T, A, 4>(p, cap, s, which); break;
+        case 8: red_launch<T, A, 8>(p, cap, s, which); break;
+        default: red_launch<T, A, 16>(p, cap, s, which); break;
+    }
+}
+
+static void reduce_or_fixup(int tt, int vpl, const ReduceParams& p, uint64_t cap, cudaStream_t s, int which) {
+    if (tt == TT_F32) red_dispatch<float, float>(vpl, p, cap, s, which);
+    else if (tt == TT_BF16) red_dispatch<__nv_bfloat16, float>(vpl, p, cap, s, which);
+    else red_dispatch<double, double>(vpl, p, cap, s, which);
+}
+
 void launch_reduce(int tt, int vpl, const ReduceParams& p, uint64_t cap, cudaStream_t s) {
-    if (tt == TT_F32) red_dispatch<float, float>(vpl, p, cap, s);
-    else if (tt == TT_BF16) red_dispatch<__nv_bfloat16, float>(vpl, p, cap, s);
-    else red_dispatch<double, double>(vpl, p, cap, s);
+    reduce_or_fixup(tt, vpl, p, cap, s, 0);
+}
+
+void launch_fixup(int tt, int vpl, const ReduceParams& p, uint64_t cap, cudaStream_t s) {
+    reduce_or_fixup(tt, vpl, p, cap, s, 1);
 }
 
 template <typename T>

@@ -47,30 +47,37 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_hist(const uint32_t* __r
     }
 }
 
+// Exclusive scan of hist[0, 256 * ntiles) by one CTA: each iteration covers
+// 4096 consecutive entries (4 per thread, coalesced), with a running carry.
 __global__ void __launch_bounds__(1024) k_radix_scan(const BatchState* st, uint32_t* hist) {
     __shared__ uint32_t wsum[32];
+    __shared__ uint32_t carry;
     const uint32_t n = st->n_items;
     const uint32_t ntiles = (n + SORT_TILE - 1) / SORT_TILE;
     const uint32_t len = 256 * ntiles;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    // each thread owns a contiguous run of `per` entries
-    const uint32_t per = (len + 1023) / 1024;
-    const uint32_t b = tid * per, e = min(b + per, len);
-    uint32_t local = 0;
-    for (uint32_t i = b; i < e; ++i) local += hist[i];
-    uint32_t incl = warp_incl_scan(local, lane);
-    if (lane == 31) wsum[w] = incl;
+    if (tid == 0) carry = 0;
     __syncthreads();
-    if (w == 0) {
-        uint32_t s = warp_incl_scan(wsum[lane], lane);
-        wsum[lane] = s;
-    }
-    __syncthreads();
-    uint32_t run = (w ? wsum[w - 1] : 0) + incl - local;
-    for (uint32_t i = b; i < e; ++i) {
-        const uint32_t x = hist[i];
-        hist[i] = run;
-        run += x;
+    for (uint32_t base = 0; base < len; base += 4096) {
+        const uint32_t i = base + 4 * tid;
+        uint32_t x[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) x[k] = i + k < len ? hist[i + k] : 0u;
+        const uint32_t local = x[0] + x[1] + x[2] + x[3];
+        const uint32_t incl = warp_incl_scan(local, lane);
+        if (lane == 31) wsum[w] = incl;
+        __syncthreads();
+        if (w == 0) wsum[lane] = warp_incl_scan(wsum[lane], lane);
+        __syncthreads();
+        uint32_t run = carry + (w ? wsum[w - 1] : 0u) + incl - local;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (i + k < len) hist[i + k] = run;
+            run += x[k];
+        }
+        __syncthreads();
+        if (tid == 0) carry += wsum[31];
+        __syncthreads();
     }
 }
 

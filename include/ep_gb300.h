@@ -111,9 +111,10 @@ enum { EP_STAGE_SAMPLE = 0,      /* batch set-up, sampling, item offsets */
        EP_STAGE_FORWARD = 1,     /* gather-mean, loss, gradient directions, items */
        EP_STAGE_SORT = 2,        /* radix sort of items by feature id */
        EP_STAGE_REDUCE = 3,      /* per-feature reduction (+ fused Adam) and carries */
-       EP_STAGE_ADAM = 4,        /* separate Adam kernel (PLAIN form only) */
-       EP_STAGE_END = 5,         /* loss sums, counters, state advance */
-       EP_N_STAGES = 6 };
+       EP_STAGE_FIXUP = 4,       /* features spanning reducer chunks */
+       EP_STAGE_ADAM = 5,        /* separate Adam kernel (PLAIN form only) */
+       EP_STAGE_END = 6,         /* loss sums, counters, state advance */
+       EP_N_STAGES = 7 };
 
 /* Explicit samples for the parity hooks (host pointers).  Anchor a has
  * neighbours nbr[nbr_ptr[a] .. nbr_ptr[a+1]) with base weights nbr_w and

@@ -32,8 +32,8 @@ enum { ORC_LOSS_MARGIN = 0, ORC_LOSS_STARSPACE = 1, ORC_LOSS_CONTRASTIVE = 2 };
 /* Loss weighting (src/algos/ep/mod.rs:31-36). */
 enum { ORC_LW_NONE = 0, ORC_LW_LOG = 1, ORC_LW_EXP = 2 };
 /* Gradient extraction: reference = first finite occurrence of a feature
- * across roles wins (src/algos/ep/mod.rs:361-378); true = sum of all
- * occurrences (what finite differences measure). */
+ * across roles wins (src/algos/ep/mod.rs:361-378); true = sum of all finite
+ * occurrences (the derivative of the loss wherever it is defined). */
 enum { ORC_GRAD_REFERENCE = 0, ORC_GRAD_TRUE = 1 };
 /* Sample kinds (src/algos/utils.rs:165-217). */
 enum { ORC_SAMPLE_ALL = 0, ORC_SAMPLE_FIXED = 1, ORC_SAMPLE_PROB = 2 };

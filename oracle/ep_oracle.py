@@ -333,11 +333,11 @@ def batch_autograd(fptr, fids, n_feat, table, graph_rows, anchors, nbr_ptr, nbr,
                 if g is None:
                     continue
                 g = g.detach().cpu().numpy()
+                if grad_mode == GRAD_REFERENCE and f in seen:
+                    continue
+                if not np.all(np.isfinite(g)):
+                    continue
                 if grad_mode == GRAD_REFERENCE:
-                    if f in seen:
-                        continue
-                    if not np.all(np.isfinite(g)):
-                        continue
                     seen.add(f)
                 grad[f] += g
                 touched[f] = True

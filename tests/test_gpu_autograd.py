@@ -86,4 +86,6 @@ def test_fp64_matches_oracle_fp64(oracle, sbm1k):
         f(t, *args(s)).sum().backward()
         cfg = oracle.loss_cfg(loss=1, gamma=0.5, grad_mode=0)
         _, _, og, _ = oracle.batch(w["fptr"], w["fids"], w["n_feat"], w["table"], w["rows"], *args(s), cfg, "f64")
-        assert rel_err(t.grad.cpu().numpy(), og) < 1e-10
+        # the reference (and the oracle) accumulate feature counts in f32
+        # (model.rs:268-271), the FP64 kernels in double: agreement ~1e-7
+        assert rel_err(t.grad.cpu().numpy(), og) < 1e-6
