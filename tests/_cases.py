@@ -35,6 +35,17 @@ def sample_batch(seed, prob, B, K, R, weighted=False):
             nbr_w.append(float(rng.uniform(0.5, 2.0)) if weighted else float(deg) / float(r))
         nbr_ptr.append(len(nbr))
     neg = rng.integers(0, prob["n"], (B, R)).astype(np.uint32)
+    if weighted:
+        # A negative equal to an anchor's only neighbour gives t and u the same
+        # features under different count weights: |t - u| is rounding noise and
+        # the gradient direction (t - u)/|t - u| is not reproducible in any
+        # precision.  Redraw such negatives.
+        for a in range(B):
+            if nbr_ptr[a + 1] - nbr_ptr[a] == 1:
+                only = nbr[nbr_ptr[a]]
+                for i in range(R):
+                    while neg[a, i] == only:
+                        neg[a, i] = rng.integers(0, prob["n"])
     return dict(anchors=anchors, nbr_ptr=np.array(nbr_ptr, np.uint32), nbr=np.array(nbr, np.uint32),
                 nbr_w=np.array(nbr_w, np.float32), neg=neg)
 

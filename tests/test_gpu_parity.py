@@ -104,7 +104,9 @@ def test_nan_and_empty_roles(oracle):
         if smp["nbr_ptr"][a + 1] > j:
             fids[int(prob["fptr"][smp["nbr"][j]])] = fids[int(prob["fptr"][smp["anchors"][a]])]
     prob.update(fids=fids)
-    # an anchor without neighbours -> NaN loss (status 2)
+    # an anchor without neighbours: ~h(v) is NaN, every margin term is
+    # filtered, so the loss is the constant 0 and the anchor is skipped
+    # (loss.rs:60-72, mod.rs:209-213): status 1
     smp["nbr_ptr"] = smp["nbr_ptr"].copy()
     cut = int(smp["nbr_ptr"][1] - smp["nbr_ptr"][0])
     smp["nbr"] = smp["nbr"][cut:]
@@ -112,7 +114,7 @@ def test_nan_and_empty_roles(oracle):
     smp["nbr_ptr"] = np.concatenate([[0], smp["nbr_ptr"][1:] - cut]).astype(np.uint32)
     ctx = make_ctx(prob, loss=0, gamma=1.0, R=3)
     ol, ost, og, ot = oracle_batch(oracle, prob, smp, prob["table"], loss=0, gamma=1.0)
-    assert ost[0] == 2
+    assert ost[0] == 1
     check_parity(oracle, prob, smp, ctx, prob["table"], loss=0, gamma=1.0)
 
 
