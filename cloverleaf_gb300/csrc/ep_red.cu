@@ -103,20 +103,79 @@ __device__ __forceinline__ void finish_row(const ReduceParams& p, uint32_t f, co
     adam_row<T, VPL, A>((T*)p.table, p.m, p.v, f, p.dpad, acc, lr, bc1, bc2, p.seed, step, lane, lane_on);
 }
 
-template <typename A, int VPL>
-__device__ __forceinline__ void flush_pending(const ReduceParams& p, uint32_t& pend, A& pend_c, A (&acc)[VPL],
-                                              int lane, bool lane_on) {
-    if (pend == NONE) return;
-    const A sc = ((const A*)p.scale)[pend];
-    if (lane_on) {
-        A d[VPL];
-        RowIO<A, VPL>::load((const A*)p.dir + (uint64_t)pend * p.dpad, lane, d);
-        const A w = pend_c * sc;
+// Work queue of one warp: entry k lives in lane k.  ROW entries add
+// coef * dir[src] to the running feature sum; END entries close a feature
+// segment inside the chunk (finish it, or park it as the chunk's head carry).
+enum : uint32_t { Q_ROW = 0u, Q_END = 1u, Q_HEAD = 2u, Q_KEPT = 4u };
+constexpr int Q_BATCH = 4;   // rows loaded together while draining
+
+// Entries 0..31 live in set 0 (lane k), 32..63 in set 1 (lane k - 32).
+struct Queue {
+    uint32_t id[2], kind[2];
+    float coef[2];
+};
+__device__ __forceinline__ uint32_t q_get_kind(const Queue& q, uint32_t k) {
+    const uint32_t a = __shfl_sync(FULL, q.kind[0], k & 31), b = __shfl_sync(FULL, q.kind[1], k & 31);
+    return k < 32 ? a : b;
+}
+__device__ __forceinline__ uint32_t q_get_id(const Queue& q, uint32_t k) {
+    const uint32_t a = __shfl_sync(FULL, q.id[0], k & 31), b = __shfl_sync(FULL, q.id[1], k & 31);
+    return k < 32 ? a : b;
+}
+__device__ __forceinline__ float q_get_coef(const Queue& q, uint32_t k) {
+    const float a = __shfl_sync(FULL, q.coef[0], k & 31), b = __shfl_sync(FULL, q.coef[1], k & 31);
+    return k < 32 ? a : b;
+}
+
+template <typename T, typename A, int VPL>
+__device__ __forceinline__ void drain_queue(const ReduceParams& p, uint32_t qn, const Queue& q, A (&acc)[VPL],
+                                            uint32_t& flags, uint32_t c, unsigned long long& u_cnt, int lane,
+                                            bool lane_on, float lr, float bc1, float bc2, uint32_t step) {
+    uint32_t k = 0;
+    while (k < qn) {
+        const uint32_t kind = q_get_kind(q, k);
+        if ((kind & 3u) == Q_ROW) {
+            uint32_t n = 1;
+            while (n < Q_BATCH && k + n < qn && (q_get_kind(q, k + n) & 3u) == Q_ROW) ++n;
+            uint32_t src[Q_BATCH];
+            A w[Q_BATCH];
 #pragma unroll
-        for (int k = 0; k < VPL; ++k) acc[k] += w * d[k];
+            for (int i = 0; i < Q_BATCH; ++i) {
+                const uint32_t kk = k + ((uint32_t)i < n ? (uint32_t)i : 0u);
+                src[i] = q_get_id(q, kk);
+                w[i] = (A)q_get_coef(q, kk);
+            }
+            if (lane_on) {
+                A r[Q_BATCH][VPL];
+#pragma unroll
+                for (int i = 0; i < Q_BATCH; ++i)
+                    if ((uint32_t)i < n) RowIO<A, VPL>::load((const A*)p.dir + (uint64_t)src[i] * p.dpad, lane, r[i]);
+#pragma unroll
+                for (int i = 0; i < Q_BATCH; ++i) {
+                    if ((uint32_t)i < n) {
+                        const A sc = w[i] * ((const A*)p.scale)[src[i]];
+#pragma unroll
+                        for (int e = 0; e < VPL; ++e) acc[e] += sc * r[i][e];
+                    }
+                }
+            }
+            k += n;
+        } else {
+            const uint32_t f = q_get_id(q, k);
+            if ((kind & 3u) == Q_END) {
+                if (kind & Q_KEPT) {
+                    finish_row<T, A, VPL>(p, f, acc, lane, lane_on, lr, bc1, bc2, step);
+                    ++u_cnt;
+                }
+            } else {
+                if (lane_on) store_row<A, VPL, A>((A*)p.carry_head + (uint64_t)c * p.dpad, lane, acc);
+                flags |= CF_HEAD | ((kind & Q_KEPT) ? CF_HEAD_KEPT : 0u);
+            }
+#pragma unroll
+            for (int e = 0; e < VPL; ++e) acc[e] = 0;
+            ++k;
+        }
     }
-    pend = NONE;
-    pend_c = 0;
 }
 
 template <typename T, typename A, int VPL>
@@ -167,67 +226,78 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
         bool started_here = !head_partial;
         bool any_kept = false;
         uint32_t flags = 0;
-        for (uint32_t ib = i0; ib < i1; ib += 32) {
-            const uint32_t i = ib + lane;
-            uint32_t f_l = 0, s_l = 0, v_l = 0;
-            float c_l = 0.f;
-            if (i < i1) {
-                f_l = p.skey[i];
-                const uint32_t ix = p.sidx[i];
-                s_l = p.item_src[ix];
-                c_l = p.item_c[ix];
-                v_l = p.valid[s_l];
-                const bool newrun = (i == 0) || (p.skey[i - 1] != f_l) || (p.item_src[p.sidx[i - 1]] != s_l);
-                g_cnt += newrun;
+        // queue (lane-distributed, two entries per lane) and its fill level;
+        // one batch of 32 items pushes at most 64 entries
+        Queue q;
+        q.id[0] = q.id[1] = q.kind[0] = q.kind[1] = 0;
+        q.coef[0] = q.coef[1] = 0.f;
+        uint32_t qn = 0;
+        auto push = [&](uint32_t id, float coef, uint32_t kind) {
+            const int set = qn >= 32;
+            if ((uint32_t)lane == (qn & 31)) {
+                if (set) { q.id[1] = id; q.coef[1] = coef; q.kind[1] = kind; }
+                else { q.id[0] = id; q.coef[0] = coef; q.kind[0] = kind; }
             }
-            const uint32_t m = min(32u, i1 - ib);
-            for (uint32_t j = 0; j < m; ++j) {
-                const uint32_t f = __shfl_sync(FULL, f_l, j);
-                const uint32_t s = __shfl_sync(FULL, s_l, j);
-                const A cc = (A)__shfl_sync(FULL, c_l, j);
-                const uint32_t vv = __shfl_sync(FULL, v_l, j);
-                if (f != cur_f) {
-                    flush_pending<A, VPL>(p, pend, pend_c, acc, lane, lane_on);
-                    if (started_here) {
-                        if (any_kept) {
-                            finish_row<T, A, VPL>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step);
-                            ++u_cnt;
+            ++qn;
+        };
+        for (uint32_t ib = i0;; ib += 32) {
+            if (ib < i1) {
+                const uint32_t i = ib + lane;
+                uint32_t f_l = 0, s_l = 0, v_l = 0;
+                float c_l = 0.f;
+                if (i < i1) {
+                    f_l = p.skey[i];
+                    const uint32_t ix = p.sidx[i];
+                    s_l = p.item_src[ix];
+                    c_l = p.item_c[ix];
+                    v_l = p.valid[s_l];
+                    const bool newrun = (i == 0) || (p.skey[i - 1] != f_l) || (p.item_src[p.sidx[i - 1]] != s_l);
+                    g_cnt += newrun;
+                }
+                const uint32_t m = min(32u, i1 - ib);
+                for (uint32_t j = 0; j < m; ++j) {
+                    const uint32_t f = __shfl_sync(FULL, f_l, j);
+                    const uint32_t s = __shfl_sync(FULL, s_l, j);
+                    const float cc = __shfl_sync(FULL, c_l, j);
+                    const uint32_t vv = __shfl_sync(FULL, v_l, j);
+                    if (f != cur_f) {
+                        if (pend != NONE) { push(pend, (float)pend_c, Q_ROW); pend = NONE; }
+                        push(cur_f, 0.f, (started_here ? Q_END : Q_HEAD) | (any_kept ? Q_KEPT : 0u));
+                        cur_f = f;
+                        started_here = true;
+                        any_kept = false;
+                        cur_anchor = s / NR;
+                        chosen = NONE;
+                    } else if (s / NR != cur_anchor) {
+                        cur_anchor = s / NR;
+                        chosen = NONE;
+                    }
+                    bool keep;
+                    if (p.grad_true) {
+                        keep = vv != 0;
+                    } else {
+                        if (vv && chosen == NONE) chosen = s;
+                        keep = vv && s == chosen;
+                    }
+                    if (keep) {
+                        any_kept = true;
+                        if (s == pend) {
+                            pend_c += (A)cc;
+                        } else {
+                            if (pend != NONE) push(pend, (float)pend_c, Q_ROW);
+                            pend = s;
+                            pend_c = (A)cc;
                         }
-                    } else {
-                        if (lane_on) store_row<A, VPL, A>((A*)p.carry_head + (uint64_t)c * p.dpad, lane, acc);
-                        flags |= CF_HEAD | (any_kept ? CF_HEAD_KEPT : 0u);
-                    }
-#pragma unroll
-                    for (int k = 0; k < VPL; ++k) acc[k] = 0;
-                    cur_f = f;
-                    started_here = true;
-                    any_kept = false;
-                    cur_anchor = s / NR;
-                    chosen = NONE;
-                } else if (s / NR != cur_anchor) {
-                    cur_anchor = s / NR;
-                    chosen = NONE;
-                }
-                bool keep;
-                if (p.grad_true) {
-                    keep = vv != 0;
-                } else {
-                    if (vv && chosen == NONE) chosen = s;
-                    keep = vv && s == chosen;
-                }
-                if (keep) {
-                    any_kept = true;
-                    if (s == pend) {
-                        pend_c += cc;
-                    } else {
-                        flush_pending<A, VPL>(p, pend, pend_c, acc, lane, lane_on);
-                        pend = s;
-                        pend_c = cc;
                     }
                 }
+            } else if (pend != NONE) {
+                push(pend, (float)pend_c, Q_ROW);
+                pend = NONE;
             }
+            drain_queue<T, A, VPL>(p, qn, q, acc, flags, c, u_cnt, lane, lane_on, lr, bc1, bc2, step);
+            qn = 0;
+            if (ib >= i1) break;
         }
-        flush_pending<A, VPL>(p, pend, pend_c, acc, lane, lane_on);
         const bool cont = i1 < M && p.skey[i1] == cur_f;
         if (started_here && !cont) {
             if (any_kept) {
