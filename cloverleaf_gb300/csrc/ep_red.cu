@@ -103,84 +103,50 @@ __device__ __forceinline__ void finish_row(const ReduceParams& p, uint32_t f, co
     adam_row<T, VPL, A>((T*)p.table, p.m, p.v, f, p.dpad, acc, lr, bc1, bc2, p.seed, step, lane, lane_on);
 }
 
-// Work queue of one warp: entry k lives in lane k.  ROW entries add
-// coef * dir[src] to the running feature sum; END entries close a feature
-// segment inside the chunk (finish it, or park it as the chunk's head carry).
-enum : uint32_t { Q_ROW = 0u, Q_END = 1u, Q_HEAD = 2u, Q_KEPT = 4u };
-constexpr int Q_BATCH = 4;   // rows loaded together while draining
-
-// Entries 0..31 live in set 0 (lane k), 32..63 in set 1 (lane k - 32).
-struct Queue {
-    uint32_t id[2], kind[2];
-    float coef[2];
-};
-__device__ __forceinline__ uint32_t q_get_kind(const Queue& q, uint32_t k) {
-    const uint32_t a = __shfl_sync(FULL, q.kind[0], k & 31), b = __shfl_sync(FULL, q.kind[1], k & 31);
-    return k < 32 ? a : b;
-}
-__device__ __forceinline__ uint32_t q_get_id(const Queue& q, uint32_t k) {
-    const uint32_t a = __shfl_sync(FULL, q.id[0], k & 31), b = __shfl_sync(FULL, q.id[1], k & 31);
-    return k < 32 ? a : b;
-}
-__device__ __forceinline__ float q_get_coef(const Queue& q, uint32_t k) {
-    const float a = __shfl_sync(FULL, q.coef[0], k & 31), b = __shfl_sync(FULL, q.coef[1], k & 31);
-    return k < 32 ? a : b;
-}
-
-template <typename T, typename A, int VPL>
-__device__ __forceinline__ void drain_queue(const ReduceParams& p, uint32_t qn, const Queue& q, A (&acc)[VPL],
-                                            uint32_t& flags, uint32_t c, unsigned long long& u_cnt, int lane,
-                                            bool lane_on, float lr, float bc1, float bc2, uint32_t step) {
-    uint32_t k = 0;
-    while (k < qn) {
-        const uint32_t kind = q_get_kind(q, k);
-        if ((kind & 3u) == Q_ROW) {
-            uint32_t n = 1;
-            while (n < Q_BATCH && k + n < qn && (q_get_kind(q, k + n) & 3u) == Q_ROW) ++n;
-            uint32_t src[Q_BATCH];
-            A w[Q_BATCH];
+// Accumulates into acc the rows of the kept items whose lanes are set in
+// `mask` (lane j holds src[j] and the item's coefficient w[j] = c * scale),
+// four rows in flight at a time, in increasing lane order.
+template <typename A, int VPL>
+__device__ __forceinline__ void add_rows(const ReduceParams& p, unsigned mask, uint32_t src_l, A w_l, A (&acc)[VPL],
+                                         int lane, bool lane_on) {
+    while (mask) {
+        uint32_t src[4];
+        A w[4];
+        int n = 0;
 #pragma unroll
-            for (int i = 0; i < Q_BATCH; ++i) {
-                const uint32_t kk = k + ((uint32_t)i < n ? (uint32_t)i : 0u);
-                src[i] = q_get_id(q, kk);
-                w[i] = (A)q_get_coef(q, kk);
-            }
-            if (lane_on) {
-                A r[Q_BATCH][VPL];
+        for (int i = 0; i < 4; ++i) {
+            const int j = mask ? __ffs(mask) - 1 : 0;
+            const bool have = mask != 0;
+            src[i] = __shfl_sync(FULL, src_l, j);
+            w[i] = __shfl_sync(FULL, w_l, j);
+            if (have) { mask &= mask - 1; n = i + 1; }
+        }
+        if (lane_on) {
+            A r[4][VPL];
 #pragma unroll
-                for (int i = 0; i < Q_BATCH; ++i)
-                    if ((uint32_t)i < n) RowIO<A, VPL>::load((const A*)p.dir + (uint64_t)src[i] * p.dpad, lane, r[i]);
+            for (int i = 0; i < 4; ++i)
+                if (i < n) RowIO<A, VPL>::load((const A*)p.dir + (uint64_t)src[i] * p.dpad, lane, r[i]);
 #pragma unroll
-                for (int i = 0; i < Q_BATCH; ++i) {
-                    if ((uint32_t)i < n) {
-                        const A sc = w[i] * ((const A*)p.scale)[src[i]];
+            for (int i = 0; i < 4; ++i)
+                if (i < n) {
 #pragma unroll
-                        for (int e = 0; e < VPL; ++e) acc[e] += sc * r[i][e];
-                    }
+                    for (int e = 0; e < VPL; ++e) acc[e] += w[i] * r[i][e];
                 }
-            }
-            k += n;
-        } else {
-            const uint32_t f = q_get_id(q, k);
-            if ((kind & 3u) == Q_END) {
-                if (kind & Q_KEPT) {
-                    finish_row<T, A, VPL>(p, f, acc, lane, lane_on, lr, bc1, bc2, step);
-                    ++u_cnt;
-                }
-            } else {
-                if (lane_on) store_row<A, VPL, A>((A*)p.carry_head + (uint64_t)c * p.dpad, lane, acc);
-                flags |= CF_HEAD | ((kind & Q_KEPT) ? CF_HEAD_KEPT : 0u);
-            }
-#pragma unroll
-            for (int e = 0; e < VPL; ++e) acc[e] = 0;
-            ++k;
         }
     }
 }
 
+// k_reduce: one warp per chunk of C sorted items, 32 items (one per lane) at a
+// time.  Per batch the first-occurrence rule is evaluated for all 32 items at
+// once with ballots: group starts (new feature or new anchor), valid roles,
+// and for every item the first valid role of its (feature, anchor) group,
+// carried across batches and, at a chunk start, found by walking back.  Then
+// the warp walks the feature segments of the batch, adding the kept items'
+// rows in item order and finishing each feature as its segment closes.
 template <typename T, typename A, int VPL>
 __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
     const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t M = p.st->n_items;
@@ -196,107 +162,119 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
         uint32_t cur_f = p.skey[i0];
         const bool head_partial = i0 > 0 && p.skey[i0 - 1] == cur_f;
         uint32_t cur_anchor = p.item_src[p.sidx[i0]] / NR;
-        uint32_t chosen = NONE;
-        if (!p.grad_true && head_partial) {
-            // The (feature, anchor) group may have started in an earlier
-            // chunk: find its first valid role by walking back.
-            int64_t j = (int64_t)i0 - 1;
-            for (;;) {
-                const int64_t jj = j - lane;
-                bool in = false;
-                uint32_t s = 0;
-                if (jj >= 0 && p.skey[jj] == cur_f) {
-                    s = p.item_src[p.sidx[jj]];
-                    in = (s / NR) == cur_anchor;
+        uint32_t chosen = NONE;           // first valid role of the current group
+        // the item before the batch (lane 0's predecessor)
+        uint32_t prev_src = NONE, prev_f = NONE, prev_anchor = NONE;
+        if (i0 > 0) {
+            prev_src = p.item_src[p.sidx[i0 - 1]];
+            prev_f = p.skey[i0 - 1];
+            prev_anchor = prev_src / NR;
+        }
+        if (head_partial) {
+            if (!p.grad_true) {
+                int64_t j = (int64_t)i0 - 1;
+                for (;;) {
+                    const int64_t jj = j - lane;
+                    bool in = false;
+                    uint32_t s = 0;
+                    if (jj >= 0 && p.skey[jj] == cur_f) {
+                        s = p.item_src[p.sidx[jj]];
+                        in = (s / NR) == cur_anchor;
+                    }
+                    const unsigned inm = __ballot_sync(FULL, in);
+                    const unsigned run = (~inm) ? ((1u << (__ffs(~inm) - 1)) - 1u) : FULL;
+                    const bool vv = in && ((run >> lane) & 1u) && p.valid[s];
+                    const unsigned vm = __ballot_sync(FULL, vv);
+                    if (vm) chosen = __shfl_sync(FULL, s, 31 - __clz(vm));
+                    if (run != FULL) break;
+                    j -= 32;
                 }
-                const unsigned inm = __ballot_sync(FULL, in);
-                const unsigned run = (~inm) ? ((1u << (__ffs(~inm) - 1)) - 1u) : FULL;
-                const bool vv = in && ((run >> lane) & 1u) && p.valid[s];
-                const unsigned vm = __ballot_sync(FULL, vv);
-                if (vm) chosen = __shfl_sync(FULL, s, 31 - __clz(vm));
-                if (run != FULL) break;
-                j -= 32;
             }
         }
         A acc[VPL];
 #pragma unroll
         for (int k = 0; k < VPL; ++k) acc[k] = 0;
-        uint32_t pend = NONE;
-        A pend_c = 0;
         bool started_here = !head_partial;
         bool any_kept = false;
         uint32_t flags = 0;
-        // queue (lane-distributed, two entries per lane) and its fill level;
-        // one batch of 32 items pushes at most 64 entries
-        Queue q;
-        q.id[0] = q.id[1] = q.kind[0] = q.kind[1] = 0;
-        q.coef[0] = q.coef[1] = 0.f;
-        uint32_t qn = 0;
-        auto push = [&](uint32_t id, float coef, uint32_t kind) {
-            const int set = qn >= 32;
-            if ((uint32_t)lane == (qn & 31)) {
-                if (set) { q.id[1] = id; q.coef[1] = coef; q.kind[1] = kind; }
-                else { q.id[0] = id; q.coef[0] = coef; q.kind[0] = kind; }
+        for (uint32_t ib = i0; ib < i1; ib += 32) {
+            const uint32_t i = ib + lane;
+            const bool act = i < i1;
+            uint32_t f = NONE, s = 0;
+            A w = 0;
+            bool v = false;
+            if (act) {
+                f = p.skey[i];
+                s = p.item_src[p.sidx[i]];
+                v = p.valid[s] != 0;
             }
-            ++qn;
-        };
-        for (uint32_t ib = i0;; ib += 32) {
-            if (ib < i1) {
-                const uint32_t i = ib + lane;
-                uint32_t f_l = 0, s_l = 0, v_l = 0;
-                float c_l = 0.f;
-                if (i < i1) {
-                    f_l = p.skey[i];
-                    const uint32_t ix = p.sidx[i];
-                    s_l = p.item_src[ix];
-                    c_l = p.item_c[ix];
-                    v_l = p.valid[s_l];
-                    const bool newrun = (i == 0) || (p.skey[i - 1] != f_l) || (p.item_src[p.sidx[i - 1]] != s_l);
-                    g_cnt += newrun;
-                }
-                const uint32_t m = min(32u, i1 - ib);
-                for (uint32_t j = 0; j < m; ++j) {
-                    const uint32_t f = __shfl_sync(FULL, f_l, j);
-                    const uint32_t s = __shfl_sync(FULL, s_l, j);
-                    const float cc = __shfl_sync(FULL, c_l, j);
-                    const uint32_t vv = __shfl_sync(FULL, v_l, j);
-                    if (f != cur_f) {
-                        if (pend != NONE) { push(pend, (float)pend_c, Q_ROW); pend = NONE; }
-                        push(cur_f, 0.f, (started_here ? Q_END : Q_HEAD) | (any_kept ? Q_KEPT : 0u));
-                        cur_f = f;
-                        started_here = true;
-                        any_kept = false;
-                        cur_anchor = s / NR;
-                        chosen = NONE;
-                    } else if (s / NR != cur_anchor) {
-                        cur_anchor = s / NR;
-                        chosen = NONE;
-                    }
-                    bool keep;
-                    if (p.grad_true) {
-                        keep = vv != 0;
-                    } else {
-                        if (vv && chosen == NONE) chosen = s;
-                        keep = vv && s == chosen;
-                    }
-                    if (keep) {
-                        any_kept = true;
-                        if (s == pend) {
-                            pend_c += (A)cc;
-                        } else {
-                            if (pend != NONE) push(pend, (float)pend_c, Q_ROW);
-                            pend = s;
-                            pend_c = (A)cc;
+            const uint32_t anchor = s / NR;
+            // predecessor of each lane (lane 0: the carried item before the batch)
+            uint32_t pf = __shfl_up_sync(FULL, f, 1), pa = __shfl_up_sync(FULL, anchor, 1);
+            uint32_t ps = __shfl_up_sync(FULL, s, 1);
+            if (lane == 0) { pf = prev_f; pa = prev_anchor; ps = prev_src; }
+            const bool seg_start = act && f != pf;
+            const bool grp_start = act && (seg_start || anchor != pa);
+            if (act) g_cnt += (seg_start || s != ps);
+            const unsigned SS = __ballot_sync(FULL, seg_start);
+            const unsigned GS = __ballot_sync(FULL, grp_start);
+            const unsigned V = __ballot_sync(FULL, act && v);
+            bool keep;
+            if (p.grad_true) {
+                keep = act && v;
+            } else {
+                // lanes of this item's group up to and including itself
+                const unsigned gs_le = GS & (lt_mask | (1u << lane));
+                const int gstart = gs_le ? 31 - __clz(gs_le) : -1;
+                const unsigned grp = (lt_mask | (1u << lane)) & (gstart >= 0 ? ~((1u << gstart) - 1u) : FULL);
+                const unsigned vg = V & grp;
+                const int fv = vg ? __ffs(vg) - 1 : 0;
+                const uint32_t src_fv = __shfl_sync(FULL, s, fv);
+                uint32_t ch = NONE;
+                if (gstart < 0 && chosen != NONE) ch = chosen;      // group began before this batch
+                else if (vg) ch = src_fv;
+                keep = act && v && s == ch;
+                // carry the group state of the batch's last item
+                const int last = 31 - __clz(__ballot_sync(FULL, act));
+                chosen = __shfl_sync(FULL, ch, last);
+            }
+            if (keep) w = (A)p.item_c[p.sidx[i]] * ((const A*)p.scale)[s];
+            const unsigned K = __ballot_sync(FULL, keep);
+            const unsigned ACT = __ballot_sync(FULL, act);
+            const int last = 31 - __clz(ACT);
+            // walk the segments of this batch
+            unsigned starts = SS;
+            int lo = 0;
+            while (lo <= last) {
+                // the segment containing lane lo runs to the next start after lo
+                const unsigned later = starts & ~((2u << lo) - 1u) & ((lo == 31) ? 0u : FULL);
+                const int hi = later ? __ffs(later) - 1 : last + 1;
+                if ((SS >> lo) & 1u) {
+                    // a new segment starts at lo: close the current one first
+                    if (started_here) {
+                        if (any_kept) {
+                            finish_row<T, A, VPL>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step);
+                            ++u_cnt;
                         }
+                    } else {
+                        if (lane_on) store_row<A, VPL, A>((A*)p.carry_head + (uint64_t)c * p.dpad, lane, acc);
+                        flags |= CF_HEAD | (any_kept ? CF_HEAD_KEPT : 0u);
                     }
+#pragma unroll
+                    for (int k = 0; k < VPL; ++k) acc[k] = 0;
+                    started_here = true;
+                    any_kept = false;
+                    cur_f = __shfl_sync(FULL, f, lo);
                 }
-            } else if (pend != NONE) {
-                push(pend, (float)pend_c, Q_ROW);
-                pend = NONE;
+                const unsigned rng = (hi >= 32 ? FULL : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+                const unsigned km = K & rng;
+                any_kept = any_kept || km != 0;
+                add_rows<A, VPL>(p, km, s, w, acc, lane, lane_on);
+                lo = hi;
             }
-            drain_queue<T, A, VPL>(p, qn, q, acc, flags, c, u_cnt, lane, lane_on, lr, bc1, bc2, step);
-            qn = 0;
-            if (ib >= i1) break;
+            prev_f = __shfl_sync(FULL, f, last);
+            prev_anchor = __shfl_sync(FULL, anchor, last);
+            prev_src = __shfl_sync(FULL, s, last);
         }
         const bool cont = i1 < M && p.skey[i1] == cur_f;
         if (started_here && !cont) {
@@ -360,13 +338,23 @@ __global__ void __launch_bounds__(RED_THREADS) k_fixup(ReduceParams p) {
 #pragma unroll
         for (int k = 0; k < VPL; ++k) acc[k] = 0;
         uint32_t kept = 0;
-        for (uint32_t j = c + 1 + w; j <= last; j += NWARP) {
-            kept |= p.carry_flags[j] & CF_HEAD_KEPT;
-            if (lane_on) {
-                A h[VPL];
-                RowIO<A, VPL>::load_cg((const A*)p.carry_head + (uint64_t)j * p.dpad, lane, h);
+        // partials j = c+1+w, c+1+w+NWARP, ...: four loads in flight, summed in order
+        for (uint32_t j = c + 1 + w; j <= last; j += 4 * NWARP) {
+            A h[4][VPL];
 #pragma unroll
-                for (int k = 0; k < VPL; ++k) acc[k] += h[k];
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t jj = j + u * NWARP;
+                if (jj <= last) {
+                    kept |= p.carry_flags[jj] & CF_HEAD_KEPT;
+                    if (lane_on) RowIO<A, VPL>::load_cg((const A*)p.carry_head + (uint64_t)jj * p.dpad, lane, h[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (j + u * NWARP <= last && lane_on) {
+#pragma unroll
+                    for (int k = 0; k < VPL; ++k) acc[k] += h[u][k];
+                }
             }
         }
         if (lane_on) store_row<A, VPL, A>(wsum + (size_t)w * p.dpad, lane, acc);

@@ -8,8 +8,10 @@
 //
 // One pass per 8-bit digit, three kernels per pass:
 //   k_radix_hist     per-tile digit counts -> hist[digit * ntiles + tile]
-//   k_radix_scan     exclusive scan of hist (digit-major = stable tile order)
-//   k_radix_scatter  per-tile stable ranks (warp match + per-warp counters)
+//   k_radix_colscan  one warp per digit: exclusive scan of that digit's counts
+//                    over the tiles (in place) and the digit total
+//   k_radix_scatter  digit bases from the 256 totals (scanned per CTA), then
+//                    per-tile stable ranks (warp match + per-warp counters)
 // The item count lives in device memory (BatchState::n_items), so the same
 // launches replay inside a CUDA graph for any batch.
 #include <cuda_runtime.h>
@@ -26,7 +28,7 @@ constexpr int SORT_MAX_GRID = 152 * 4;
 
 size_t radix_hist_entries(uint64_t cap) {
     const uint64_t tiles = (cap + SORT_TILE - 1) / SORT_TILE;
-    return (size_t)(256 * (tiles ? tiles : 1));
+    return (size_t)(256 * (tiles ? tiles : 1)) + 256;   // + digit totals
 }
 
 __global__ void __launch_bounds__(SORT_THREADS) k_radix_hist(const uint32_t* __restrict__ keys, const BatchState* st,
@@ -47,38 +49,24 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_hist(const uint32_t* __r
     }
 }
 
-// Exclusive scan of hist[0, 256 * ntiles) by one CTA: each iteration covers
-// 4096 consecutive entries (4 per thread, coalesced), with a running carry.
-__global__ void __launch_bounds__(1024) k_radix_scan(const BatchState* st, uint32_t* hist) {
-    __shared__ uint32_t wsum[32];
-    __shared__ uint32_t carry;
+// One warp per digit: exclusive scan of hist[d * ntiles .. + ntiles) and the
+// digit's total in dtot[d].
+__global__ void __launch_bounds__(256) k_radix_colscan(const BatchState* st, uint32_t* hist, uint32_t* dtot) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (d >= 256) return;
     const uint32_t n = st->n_items;
     const uint32_t ntiles = (n + SORT_TILE - 1) / SORT_TILE;
-    const uint32_t len = 256 * ntiles;
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    if (tid == 0) carry = 0;
-    __syncthreads();
-    for (uint32_t base = 0; base < len; base += 4096) {
-        const uint32_t i = base + 4 * tid;
-        uint32_t x[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) x[k] = i + k < len ? hist[i + k] : 0u;
-        const uint32_t local = x[0] + x[1] + x[2] + x[3];
-        const uint32_t incl = warp_incl_scan(local, lane);
-        if (lane == 31) wsum[w] = incl;
-        __syncthreads();
-        if (w == 0) wsum[lane] = warp_incl_scan(wsum[lane], lane);
-        __syncthreads();
-        uint32_t run = carry + (w ? wsum[w - 1] : 0u) + incl - local;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (i + k < len) hist[i + k] = run;
-            run += x[k];
-        }
-        __syncthreads();
-        if (tid == 0) carry += wsum[31];
-        __syncthreads();
+    uint32_t* col = hist + (size_t)d * ntiles;
+    uint32_t carry = 0;
+    for (uint32_t b = 0; b < ntiles; b += 32) {
+        const uint32_t t = b + lane;
+        const uint32_t x = t < ntiles ? col[t] : 0u;
+        const uint32_t incl = warp_incl_scan(x, lane);
+        if (t < ntiles) col[t] = carry + incl - x;
+        carry += __shfl_sync(FULL, incl, 31);
     }
+    if (lane == 0) dtot[d] = carry;
 }
 
 __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(const uint32_t* __restrict__ keys_in,
@@ -86,11 +74,25 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(const uint32_t* 
                                                                 uint32_t* __restrict__ keys_out,
                                                                 uint32_t* __restrict__ vals_out,
                                                                 const BatchState* st, int shift,
-                                                                const uint32_t* __restrict__ hist) {
+                                                                const uint32_t* __restrict__ hist,
+                                                                const uint32_t* __restrict__ dtot) {
     __shared__ uint32_t wcount[SORT_THREADS / 32][256];
+    __shared__ uint32_t dbase[256];
+    __shared__ uint32_t wtot[SORT_THREADS / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint32_t n = st->n_items;
     const uint32_t ntiles = (n + SORT_TILE - 1) / SORT_TILE;
+    if (blockIdx.x >= ntiles) return;
+    {   // exclusive scan of the 256 digit totals -> first position of each digit
+        const uint32_t x = dtot[threadIdx.x];
+        const uint32_t incl = warp_incl_scan(x, lane);
+        if (lane == 31) wtot[w] = incl;
+        __syncthreads();
+        uint32_t off = 0;
+        for (int ww = 0; ww < w; ++ww) off += wtot[ww];
+        dbase[threadIdx.x] = off + incl - x;
+        __syncthreads();
+    }
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         for (int i = threadIdx.x; i < (SORT_THREADS / 32) * 256; i += SORT_THREADS) (&wcount[0][0])[i] = 0;
         __syncthreads();
@@ -128,7 +130,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(const uint32_t* 
             const uint32_t i = base + r * 32 + lane;
             if (i < n) {
                 const uint32_t dig = (key[r] >> shift) & 255u;
-                const uint32_t pos = hist[dig * ntiles + tile] + wcount[w][dig] + rank[r];
+                const uint32_t pos = dbase[dig] + hist[dig * ntiles + tile] + wcount[w][dig] + rank[r];
                 keys_out[pos] = key[r];
                 vals_out[pos] = val[r];
             }
@@ -156,9 +158,10 @@ void launch_radix_sort(BatchState* st, uint32_t* keys, uint32_t* keys_alt, uint3
         uint32_t* kout = K[(p + 1) & 1];
         vin = p == 0 ? nullptr : V[(p - 1) & 1];
         uint32_t* vout = V[p & 1];
+        uint32_t* dtot = hist + radix_hist_entries(cap) - 256;
         k_radix_hist<<<grid, SORT_THREADS, 0, s>>>(kin, st, shift, hist);
-        k_radix_scan<<<1, 1024, 0, s>>>(st, hist);
-        k_radix_scatter<<<grid, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, st, shift, hist);
+        k_radix_colscan<<<32, 256, 0, s>>>(st, hist, dtot);
+        k_radix_scatter<<<grid, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, st, shift, hist, dtot);
         kin = kout;
         vin = vout;
     }
