@@ -98,6 +98,10 @@ def test_nan_and_empty_roles(oracle):
     # feature), empty neighbour lists, a negative equal to the reconstruction
     prob = random_problem(9, n=50, n_feat=30, dims=8, feats=(1, 1))
     smp = sample_batch(10, prob, B=40, K=1, R=3)
+    # unit neighbour weights: every role then counts its single feature 2x, so
+    # equal feature sets give bit-identical means (an exact zero distance,
+    # NaN direction, dropped), not means that differ by rounding
+    smp["nbr_w"] = np.ones_like(smp["nbr_w"])
     fids = prob["fids"].copy()
     for a in range(0, 40, 3):
         j = smp["nbr_ptr"][a]
