@@ -77,7 +77,7 @@ struct ep_ctx {
 
     // per-batch scratch
     DevBuf st, st_eval, st_inj;
-    DevBuf anchors, nbr, nbr_w, nbr_cnt, neg, occ, dir, scale, valid, loss, status;
+    DevBuf anchors, nbr, nbr_w, nbr_cnt, neg, occ, dir, scale, valid, loss, status, deferred;
     DevBuf item_f, item_src, item_c, key_alt, idx, idx_alt, hist;
     DevBuf carry_head, carry_tail, carry_f, carry_flags, gdense, touched, n_touched, packed, xfer, bound;
     uint64_t items_cap = 0;
@@ -360,6 +360,7 @@ static int ensure_bufs(ep_ctx* c, uint32_t B, uint32_t K, uint64_t items, uint32
                   c->nbr_cnt.ensure((size_t)B * 4) && c->neg.ensure((size_t)B * c->R * 4) && c->occ.ensure(((size_t)B + 1) * 4) &&
                   c->dir.ensure((size_t)B * NR * c->dpad * es) && c->scale.ensure((size_t)B * NR * es) &&
                   c->valid.ensure((size_t)B * NR) && c->loss.ensure((size_t)B * es) && c->status.ensure((size_t)B * 4) &&
+                  c->deferred.ensure((size_t)B) &&
                   c->item_f.ensure(items * 4) && c->item_src.ensure(items * 4) && c->item_c.ensure(items * 4) &&
                   c->key_alt.ensure(items * 4) && c->idx.ensure(items * 4) && c->idx_alt.ensure(items * 4) &&
                   c->hist.ensure(radix_hist_entries(items) * 4) && c->carry_head.ensure((size_t)nch * c->dpad * es) &&
@@ -493,6 +494,7 @@ static ForwardParams forward_params(ep_ctx* c, BatchState* st, const void* table
     fp.item_f = c->item_f.as<uint32_t>();
     fp.item_src = c->item_src.as<uint32_t>();
     fp.item_c = c->item_c.as<float>();
+    fp.deferred = c->deferred.as<uint8_t>();
     return fp;
 }
 
@@ -540,7 +542,7 @@ static void sort_and_reduce(ep_ctx* c, BatchState* st, int tt, int out_mode, voi
 static uint32_t kernels_per_batch(const ep_ctx* c) {
     const uint32_t b = bits_for(c->n_feat);
     const uint32_t radix = 3 * (b ? (b + 7) / 8 : 1);
-    return 3 /* begin, sample, scan */ + 1 /* forward */ + radix + 2 /* reduce, fixup */ +
+    return 3 /* begin, sample, scan */ + 2 /* forward: staged, direct */ + radix + 2 /* reduce, fixup */ +
            (c->cfg.form == EP_FORM_PLAIN_FP32 ? 1 : 0) + 1 /* end */;
 }
 

@@ -125,6 +125,25 @@ struct RowIO {
 #pragma unroll
         for (int k = 0; k < VPL; ++k) out[k] = cvt_in<A, T>(u.t[k]);
     }
+    // Raw row slice kept in its storage type while loads are in flight.
+    struct Raw { V v[NV]; };
+    // number of raw slices that fit in about 32 registers
+    static constexpr int INFLIGHT = (BYTES >= 128) ? 1 : (128 / BYTES > 8 ? 8 : 128 / BYTES);
+    static __device__ __forceinline__ Raw load_raw(const T* __restrict__ row, int lane) {
+        Raw r;
+        const V* src = reinterpret_cast<const V*>(row + lane * VPL);
+#pragma unroll
+        for (int i = 0; i < NV; ++i) r.v[i] = __ldg(src + i);
+        return r;
+    }
+    template <typename A>
+    static __device__ __forceinline__ void fma(A (&acc)[VPL], A c, const Raw& r) {
+        union { V v[NV]; T t[VPL]; } u;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) u.v[i] = r.v[i];
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) acc[k] += c * cvt_in<A, T>(u.t[k]);
+    }
     static __device__ __forceinline__ void store_raw(T* row, int lane, const T (&in)[VPL]) {
         union { V v[NV]; T t[VPL]; } u;
 #pragma unroll

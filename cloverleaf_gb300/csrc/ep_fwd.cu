@@ -367,6 +367,145 @@ __device__ A gather_role(const ForwardParams& p, const T* __restrict__ table, co
     return ntot;
 }
 
+// ---------------------------------------------------------------------------
+// Staged gather (the common case): per-warp shared-memory tables of the
+// anchor's role nodes and of all their feature occurrences, so that the row
+// pointers of all roles are loaded in one round, all feature ids in one more,
+// and each role's rows are then read eight at a time from the table.
+// ---------------------------------------------------------------------------
+constexpr uint32_t NODE_CAP = 64;     // 1 + neighbours + negatives
+constexpr uint32_t OCC_CAP = 512;     // feature occurrences of one anchor
+constexpr uint32_t ROLE_CAP = 34;     // R + 2
+constexpr int FWD_WARPS = 8;
+
+struct WarpTables {
+    uint32_t node_fs[NODE_CAP];       // first feature index (fptr) of the node
+    uint32_t node_incl[NODE_CAP];     // inclusive prefix of feature counts
+    float node_c[NODE_CAP];           // count weight of the node's occurrences
+    uint32_t role_ob[ROLE_CAP + 1];   // first occurrence of each role
+    float role_n[ROLE_CAP];           // sum of count weights of each role
+    uint32_t occ_f[OCC_CAP];
+    float occ_c[OCC_CAP];
+};
+
+__device__ __forceinline__ uint32_t node_role(uint32_t q, uint32_t cnt) {
+    return q == 0 ? 0u : (q <= cnt ? 1u : 2u + (q - 1u - cnt));
+}
+
+// Phases A and B.  Returns false (warp-uniform) when the anchor does not fit
+// the tables; nothing has been emitted then.
+template <typename A>
+__device__ bool stage_anchor(const ForwardParams& p, WarpTables& W, uint32_t a, uint32_t v, uint32_t cnt,
+                             uint64_t pos, bool emit, uint32_t sbase, int lane) {
+    const uint32_t R = p.R;
+    const uint32_t n_nodes = 1 + cnt + R;
+    if (n_nodes > NODE_CAP || R + 2 > ROLE_CAP) return false;
+    const uint32_t* nb = p.nbr + (uint64_t)a * p.Kcap;
+    const float* nw = p.nbr_w + (uint64_t)a * p.Kcap;
+    const uint32_t* ng = p.neg + (uint64_t)a * R;
+    uint32_t carry = 0;
+    float n1 = 0.f;                  // role 1 weight total (lane-partial)
+    bool big = false;
+    for (uint32_t q0 = 0; q0 < n_nodes; q0 += 32) {
+        const uint32_t q = q0 + lane;
+        uint32_t fn = 0;
+        if (q < n_nodes) {
+            uint32_t u;
+            float c;
+            if (q == 0) { u = v; c = 1.f; }
+            else if (q <= cnt) { u = nb[q - 1]; c = nw[q - 1]; }
+            else { u = ng[q - 1 - cnt]; c = 1.f; }
+            c += p.feat_scalar;
+            const uint64_t fs = p.fptr[u];
+            fn = (uint32_t)(p.fptr[u + 1] - fs);
+            big = big || (fs + fn) > 0xffffffffull;
+            W.node_fs[q] = (uint32_t)fs;
+            W.node_c[q] = c;
+            const uint32_t r = node_role(q, cnt);
+            const float wsum = c * (float)fn;
+            if (r == 1) n1 += wsum;
+            else W.role_n[r] = wsum;
+        }
+        const uint32_t incl = warp_incl_scan(fn, lane) + carry;
+        if (q < n_nodes) W.node_incl[q] = incl;
+        carry = __shfl_sync(FULL, incl, 31);
+    }
+    if (__any_sync(FULL, big)) return false;
+    const uint32_t total = carry;
+    if (total > OCC_CAP) return false;
+    n1 = warp_sum<float>(n1);
+    __syncwarp();
+    if (lane == 0) {
+        W.role_n[1] = n1;
+        W.role_ob[0] = 0;
+        W.role_ob[1] = W.node_incl[0];
+        W.role_ob[2] = W.node_incl[cnt];
+        for (uint32_t i = 1; i <= R; ++i) W.role_ob[2 + i] = W.node_incl[cnt + i];
+    }
+    // phase B: one feature id per lane, four batches of loads in flight
+    for (uint32_t o0 = 0; o0 < total; o0 += 128) {
+        uint32_t fid[4], q_of[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const uint32_t o = o0 + b * 32 + lane;
+            fid[b] = 0;
+            q_of[b] = 0;
+            if (o < total) {
+                // owner: the first node whose inclusive prefix exceeds o
+                uint32_t lo = 0, hi = n_nodes - 1;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (W.node_incl[mid] > o) hi = mid; else lo = mid + 1;
+                }
+                const uint32_t excl = lo ? W.node_incl[lo - 1] : 0u;
+                q_of[b] = lo;
+                fid[b] = p.fids[(uint64_t)W.node_fs[lo] + (o - excl)];
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const uint32_t o = o0 + b * 32 + lane;
+            if (o < total) {
+                const float c = W.node_c[q_of[b]];
+                W.occ_f[o] = fid[b];
+                W.occ_c[o] = c;
+                if (emit) {
+                    p.item_f[pos + o] = fid[b];
+                    p.item_src[pos + o] = sbase + node_role(q_of[b], cnt);
+                    p.item_c[pos + o] = c;
+                }
+            }
+        }
+    }
+    __syncwarp();
+    return true;
+}
+
+// Phase C: the weighted sum of a role's rows from the occurrence table,
+// eight rows in flight; returns the role's weight total.
+template <typename T, typename A, int VPL>
+__device__ __forceinline__ A role_from_table(const ForwardParams& p, const T* __restrict__ table, const WarpTables& W,
+                                             uint32_t r, A (&acc)[VPL], int lane, bool lane_on) {
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) acc[k] = 0;
+    const uint32_t ob = W.role_ob[r], oe = W.role_ob[r + 1];
+    const uint32_t dpad = p.dpad;
+    using IO = RowIO<T, VPL>;
+    constexpr int U = IO::INFLIGHT;
+    if (lane_on) {
+        for (uint32_t j = ob; j < oe; j += U) {
+            typename IO::Raw rows[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (j + u < oe) rows[u] = IO::load_raw(table + (uint64_t)W.occ_f[j + u] * dpad, lane);
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (j + u < oe) IO::template fma<A>(acc, (A)W.occ_c[j + u], rows[u]);
+        }
+    }
+    return (A)W.role_n[r];
+}
+
 template <typename A, int VPL>
 __device__ __forceinline__ A warp_dot(const A (&x)[VPL], const A (&y)[VPL]) {
     A s = 0;
@@ -383,8 +522,12 @@ __device__ __forceinline__ bool warp_all_finite(const A (&x)[VPL]) {
     return __all_sync(FULL, ok);
 }
 
-template <typename T, typename A, int VPL>
-__global__ void __launch_bounds__(256) k_forward(ForwardParams p) {
+// STAGED = true: the common path through the per-warp tables; anchors that do
+// not fit are flagged in p.deferred and skipped.  STAGED = false: the direct
+// path, run afterwards for the flagged anchors only (every anchor when
+// p.deferred is null).  Both produce identical items, directions and scales.
+template <typename T, typename A, int VPL, bool STAGED>
+__global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 3 : 2) : 1) k_forward(ForwardParams p) {
     const int lane = threadIdx.x & 31;
     const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t n = p.st->n_anchors;
@@ -399,11 +542,27 @@ __global__ void __launch_bounds__(256) k_forward(ForwardParams p) {
     uint64_t pos = emit ? p.occ_off[a] : 0;
     const uint64_t sbase = (uint64_t)a * NR;
 
-    A hv[VPL], tv[VPL], u[VPL];
-    const A n_h = gather_role<T, A, VPL>(p, table, &v, nullptr, 1, (uint32_t)sbase, pos, emit, hv, lane, lane_on);
+    extern __shared__ __align__(16) unsigned char fwd_smem[];
+    WarpTables& W = reinterpret_cast<WarpTables*>(fwd_smem)[threadIdx.x >> 5];
     const uint32_t cnt = p.nbr_cnt[a];
-    const A n_t = gather_role<T, A, VPL>(p, table, p.nbr + (uint64_t)a * p.Kcap, p.nbr_w + (uint64_t)a * p.Kcap,
-                                         cnt, (uint32_t)(sbase + 1), pos, emit, tv, lane, lane_on);
+    if constexpr (STAGED) {
+        const bool staged = stage_anchor<A>(p, W, a, v, cnt, pos, emit, (uint32_t)sbase, lane);
+        if (lane == 0) p.deferred[a] = staged ? 0 : 1;
+        if (!staged) return;
+    } else {
+        if (p.deferred && !p.deferred[a]) return;
+    }
+    // role r of this anchor: from the staged table, or gathered directly (the
+    // direct path emits its items as it goes)
+    auto role_mean = [&](uint32_t r, const uint32_t* nodes, const float* w, uint32_t count, A (&acc)[VPL]) -> A {
+        if constexpr (STAGED) return role_from_table<T, A, VPL>(p, table, W, r, acc, lane, lane_on);
+        else return gather_role<T, A, VPL>(p, table, nodes, w, count, (uint32_t)(sbase + r), pos, emit, acc, lane,
+                                           lane_on);
+    };
+
+    A hv[VPL], tv[VPL], u[VPL];
+    const A n_h = role_mean(0, &v, nullptr, 1, hv);
+    const A n_t = role_mean(1, p.nbr + (uint64_t)a * p.Kcap, p.nbr_w + (uint64_t)a * p.Kcap, cnt, tv);
 #pragma unroll
     for (int k = 0; k < VPL; ++k) { hv[k] /= n_h; tv[k] /= n_t; }
 
@@ -438,8 +597,7 @@ __global__ void __launch_bounds__(256) k_forward(ForwardParams p) {
 
     for (uint32_t i = 0; i < R; ++i) {
         const uint32_t src = (uint32_t)(sbase + 2 + i);
-        const A n_u = gather_role<T, A, VPL>(p, table, p.neg + (uint64_t)a * R + i, nullptr, 1, src, pos, emit, u,
-                                             lane, lane_on);
+        const A n_u = role_mean(2 + i, p.neg + (uint64_t)a * R + i, nullptr, 1, u);
 #pragma unroll
         for (int k = 0; k < VPL; ++k) u[k] /= n_u;
         A d[VPL];
@@ -705,15 +863,27 @@ void launch_scan_occ(BatchState* st, uint32_t* occ, uint32_t cap, uint64_t items
     k_scan_occ<<<1, 1024, 0, s>>>(st, occ, items_cap);
 }
 
+template <typename T, typename A, int VPL>
+static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s) {
+    const uint32_t blocks = (cap + FWD_WARPS - 1) / FWD_WARPS;
+    const size_t smem = sizeof(WarpTables) * FWD_WARPS;
+    static bool attr = false;   // opt in to > 48 KB of dynamic shared memory once
+    if (!attr) {
+        cudaFuncSetAttribute(k_forward<T, A, VPL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    k_forward<T, A, VPL, true><<<blocks, 32 * FWD_WARPS, smem, s>>>(p);
+    k_forward<T, A, VPL, false><<<blocks, 32 * FWD_WARPS, 0, s>>>(p);
+}
+
 template <typename T, typename A>
 static void fwd_dispatch(int vpl, const ForwardParams& p, uint32_t cap, cudaStream_t s) {
-    const uint32_t blocks = (cap + 7) / 8;
     switch (vpl) {
-        case 1: k_forward<T, A, 1><<<blocks, 256, 0, s>>>(p); break;
-        case 2: k_forward<T, A, 2><<<blocks, 256, 0, s>>>(p); break;
-        case 4: k_forward<T, A, 4><<<blocks, 256, 0, s>>>(p); break;
-        case 8: k_forward<T, A, 8><<<blocks, 256, 0, s>>>(p); break;
-        default: k_forward<T, A, 16><<<blocks, 256, 0, s>>>(p); break;
+        case 1: fwd_launch<T, A, 1>(p, cap, s); break;
+        case 2: fwd_launch<T, A, 2>(p, cap, s); break;
+        case 4: fwd_launch<T, A, 4>(p, cap, s); break;
+        case 8: fwd_launch<T, A, 8>(p, cap, s); break;
+        default: fwd_launch<T, A, 16>(p, cap, s); break;
     }
 }
 

@@ -112,6 +112,7 @@ struct ForwardParams {
     int dloss_f64;
     int emit;                 // 0: forward only (validation)
     uint64_t items_cap;
+    uint8_t* deferred;        // [n_anchors]: 1 = anchor left to the direct path
     // outputs
     void* dir;              // A[n_anchors * NR * dpad]
     void* scale;            // A[n_anchors * NR]
