@@ -86,7 +86,7 @@ struct ep_ctx {
     bool prepared = false;
     cudaGraphExec_t gexec = nullptr;
     uint32_t* sorted_keys = nullptr;
-    uint32_t* sorted_idx = nullptr;
+    uint2* sorted_vals = nullptr;
     BatchState* h_st = nullptr;   // pinned mirror
 
     // host-side view of the pass sequence (mirrors the device BatchState)
@@ -362,7 +362,7 @@ static int ensure_bufs(ep_ctx* c, uint32_t B, uint32_t K, uint64_t items, uint32
                   c->valid.ensure((size_t)B * NR) && c->loss.ensure((size_t)B * es) && c->status.ensure((size_t)B * 4) &&
                   c->deferred.ensure((size_t)B) &&
                   c->item_f.ensure(items * 4) && c->item_src.ensure(items * 4) && c->item_c.ensure(items * 4) &&
-                  c->key_alt.ensure(items * 4) && c->idx.ensure(items * 4) && c->idx_alt.ensure(items * 4) &&
+                  c->key_alt.ensure(items * 4) && c->idx.ensure(items * 8) && c->idx_alt.ensure(items * 8) &&
                   c->hist.ensure(radix_hist_entries(items) * 4) && c->carry_head.ensure((size_t)nch * c->dpad * es) &&
                   c->carry_tail.ensure((size_t)nch * c->dpad * es) && c->carry_f.ensure((size_t)nch * 4) &&
                   c->carry_flags.ensure((size_t)nch * 4) && c->n_touched.ensure(4);
@@ -507,9 +507,7 @@ static ReduceParams reduce_params(ep_ctx* c, BatchState* st, int out_mode, void*
     rp.grad_true = c->cfg.grad_mode == EP_GRAD_TRUE;
     rp.out_mode = out_mode;
     rp.skey = c->sorted_keys;
-    rp.sidx = c->sorted_idx;
-    rp.item_src = c->item_src.as<uint32_t>();
-    rp.item_c = c->item_c.as<float>();
+    rp.sval = c->sorted_vals;
     rp.dir = c->dir.p;
     rp.scale = c->scale.p;
     rp.valid = c->valid.as<uint8_t>();
@@ -529,9 +527,9 @@ static ReduceParams reduce_params(ep_ctx* c, BatchState* st, int out_mode, void*
 
 // Sort the emitted items and reduce them; tt selects the kernel family.
 static void sort_and_reduce(ep_ctx* c, BatchState* st, int tt, int out_mode, void* table, cudaStream_t s) {
-    launch_radix_sort(st, c->item_f.as<uint32_t>(), c->key_alt.as<uint32_t>(), c->idx.as<uint32_t>(),
-                      c->idx_alt.as<uint32_t>(), c->hist.as<uint32_t>(), c->items_cap, (int)bits_for(c->n_feat),
-                      &c->sorted_keys, &c->sorted_idx, s);
+    launch_radix_sort(st, c->item_f.as<uint32_t>(), c->key_alt.as<uint32_t>(), c->item_src.as<uint32_t>(),
+                      c->item_c.as<float>(), c->idx.as<uint2>(), c->idx_alt.as<uint2>(), c->hist.as<uint32_t>(),
+                      c->items_cap, (int)bits_for(c->n_feat), &c->sorted_keys, &c->sorted_vals, s);
     if (out_mode == OUT_DENSE) cudaMemsetAsync(c->n_touched.p, 0, 4, s);
     ReduceParams rp = reduce_params(c, st, out_mode, table);
     launch_reduce(tt, (int)c->vpl, rp, c->items_cap, s);
@@ -559,9 +557,9 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr) {
     ForwardParams fp = forward_params(c, st, c->table.p, true, false);
     launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_FORWARD], s);
-    launch_radix_sort(st, c->item_f.as<uint32_t>(), c->key_alt.as<uint32_t>(), c->idx.as<uint32_t>(),
-                      c->idx_alt.as<uint32_t>(), c->hist.as<uint32_t>(), c->items_cap, (int)bits_for(c->n_feat),
-                      &c->sorted_keys, &c->sorted_idx, s);
+    launch_radix_sort(st, c->item_f.as<uint32_t>(), c->key_alt.as<uint32_t>(), c->item_src.as<uint32_t>(),
+                      c->item_c.as<float>(), c->idx.as<uint2>(), c->idx_alt.as<uint2>(), c->hist.as<uint32_t>(),
+                      c->items_cap, (int)bits_for(c->n_feat), &c->sorted_keys, &c->sorted_vals, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_SORT], s);
     const bool plain = c->cfg.form == EP_FORM_PLAIN_FP32;
     if (plain) cudaMemsetAsync(c->n_touched.p, 0, 4, s);

@@ -130,9 +130,7 @@ struct ReduceParams {
     int grad_true;          // EP_GRAD_TRUE
     int out_mode;           // OutMode
     const uint32_t* skey;   // sorted feature ids
-    const uint32_t* sidx;   // item index of each sorted position
-    const uint32_t* item_src;
-    const float* item_c;
+    const uint2* sval;      // (role-src, count-weight bits) of each sorted item
     const void* dir;        // A
     const void* scale;      // A
     const uint8_t* valid;
@@ -160,9 +158,9 @@ void launch_sample(const SampleParams& p, cudaStream_t s);
 void launch_scan_occ(BatchState* st, uint32_t* occ, uint32_t cap, uint64_t items_cap,
                      cudaStream_t s);
 void launch_forward(int tt, int vpl, const ForwardParams& p, uint32_t cap, cudaStream_t s);
-void launch_radix_sort(BatchState* st, uint32_t* keys, uint32_t* keys_alt, uint32_t* idx,
-                       uint32_t* idx_alt, uint32_t* hist, uint64_t cap, int key_bits,
-                       uint32_t** sorted_keys, uint32_t** sorted_idx, cudaStream_t s);
+void launch_radix_sort(BatchState* st, uint32_t* keys, uint32_t* keys_alt, const uint32_t* item_src,
+                       const float* item_c, uint2* vals, uint2* vals_alt, uint32_t* hist, uint64_t cap,
+                       int key_bits, uint32_t** sorted_keys, uint2** sorted_vals, cudaStream_t s);
 void launch_reduce(int tt, int vpl, const ReduceParams& p, uint64_t items_cap, cudaStream_t s);
 void launch_fixup(int tt, int vpl, const ReduceParams& p, uint64_t items_cap, cudaStream_t s);
 void launch_adam_dense(int tt, int vpl, BatchState* st, void* table, float* m, float* v,

@@ -37,6 +37,7 @@ constexpr uint32_t NONE = 0xffffffffu;
 // (partial in carry_tail); *_KEPT = the partial contains at least one kept item.
 enum : uint32_t { CF_HEAD = 1u, CF_THROUGH = 2u, CF_OWNER = 4u, CF_HEAD_KEPT = 8u, CF_TAIL_KEPT = 16u };
 constexpr int RED_THREADS = 256;
+constexpr int FIX_THREADS = 128;
 constexpr uint32_t RED_MAX_CTAS = 152 * 8;
 
 uint32_t reduce_chunks(uint64_t cap, uint32_t chunk) { return (uint32_t)((cap + chunk - 1) / chunk); }
@@ -103,6 +104,35 @@ __device__ __forceinline__ void finish_row(const ReduceParams& p, uint32_t f, co
     adam_row<T, VPL, A>((T*)p.table, p.m, p.v, f, p.dpad, acc, lr, bc1, bc2, p.seed, step, lane, lane_on);
 }
 
+// Bulk L2 prefetch (cp.async.bulk.prefetch) of one feature's Adam state:
+// moment rows m, v and the table row.  Rows must be 16-byte multiples.
+template <typename T>
+__device__ __forceinline__ void prefetch_row_state(const ReduceParams& p, uint32_t f) {
+    const uint32_t mb = p.dpad * 4u, tb = p.dpad * (uint32_t)sizeof(T);
+    if ((mb & 15u) || (tb & 15u)) return;
+    const char* m = reinterpret_cast<const char*>(p.m) + (uint64_t)f * mb;
+    const char* v = reinterpret_cast<const char*>(p.v) + (uint64_t)f * mb;
+    const char* t = reinterpret_cast<const char*>(p.table) + (uint64_t)f * tb;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(m), "r"(mb) : "memory");
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(v), "r"(mb) : "memory");
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(t), "r"(tb) : "memory");
+}
+
+// For the 32 items starting at position b (clipped to end), the lanes whose
+// item starts a feature segment prefetch that feature's Adam state.
+template <typename T>
+__device__ __forceinline__ void prefetch_segment_state(const ReduceParams& p, uint32_t b, uint32_t end, int lane) {
+    if constexpr (sizeof(T) == 8) {
+        return;   // FP64 tables exist only for gradient checks (no Adam)
+    } else {
+        const uint32_t i = b + lane;
+        if (i < end && i > 0) {
+            const uint32_t f = p.skey[i];
+            if (f != p.skey[i - 1]) prefetch_row_state<T>(p, f);
+        }
+    }
+}
+
 // Accumulates into acc the rows of the kept items whose lanes are set in
 // `mask` (lane j holds src[j] and the item's coefficient w[j] = c * scale),
 // four rows in flight at a time, in increasing lane order.
@@ -161,12 +191,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
         const uint32_t i0 = c * C, i1 = min(i0 + C, M);
         uint32_t cur_f = p.skey[i0];
         const bool head_partial = i0 > 0 && p.skey[i0 - 1] == cur_f;
-        uint32_t cur_anchor = p.item_src[p.sidx[i0]] / NR;
+        uint32_t cur_anchor = p.sval[i0].x / NR;
         uint32_t chosen = NONE;           // first valid role of the current group
         // the item before the batch (lane 0's predecessor)
         uint32_t prev_src = NONE, prev_f = NONE, prev_anchor = NONE;
         if (i0 > 0) {
-            prev_src = p.item_src[p.sidx[i0 - 1]];
+            prev_src = p.sval[i0 - 1].x;
             prev_f = p.skey[i0 - 1];
             prev_anchor = prev_src / NR;
         }
@@ -178,7 +208,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
                     bool in = false;
                     uint32_t s = 0;
                     if (jj >= 0 && p.skey[jj] == cur_f) {
-                        s = p.item_src[p.sidx[jj]];
+                        s = p.sval[jj].x;
                         in = (s / NR) == cur_anchor;
                     }
                     const unsigned inm = __ballot_sync(FULL, in);
@@ -197,17 +227,24 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
         bool started_here = !head_partial;
         bool any_kept = false;
         uint32_t flags = 0;
+        if (p.out_mode == OUT_ADAM) prefetch_segment_state<T>(p, i0, i1, lane);
         for (uint32_t ib = i0; ib < i1; ib += 32) {
             const uint32_t i = ib + lane;
             const bool act = i < i1;
             uint32_t f = NONE, s = 0;
+            float cf = 0.f;
             A w = 0;
             bool v = false;
             if (act) {
                 f = p.skey[i];
-                s = p.item_src[p.sidx[i]];
+                const uint2 sv = p.sval[i];
+                s = sv.x;
+                cf = __uint_as_float(sv.y);
                 v = p.valid[s] != 0;
             }
+            // look ahead: warm L2 with the Adam state of features starting in the
+            // next batch, so their updates do not wait for DRAM
+            if (p.out_mode == OUT_ADAM) prefetch_segment_state<T>(p, ib + 32, i1, lane);
             const uint32_t anchor = s / NR;
             // predecessor of each lane (lane 0: the carried item before the batch)
             uint32_t pf = __shfl_up_sync(FULL, f, 1), pa = __shfl_up_sync(FULL, anchor, 1);
@@ -238,7 +275,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
                 const int last = 31 - __clz(__ballot_sync(FULL, act));
                 chosen = __shfl_sync(FULL, ch, last);
             }
-            if (keep) w = (A)p.item_c[p.sidx[i]] * ((const A*)p.scale)[s];
+            if (keep) w = (A)cf * ((const A*)p.scale)[s];
             const unsigned K = __ballot_sync(FULL, keep);
             const unsigned ACT = __ballot_sync(FULL, act);
             const int last = 31 - __clz(ACT);
@@ -305,8 +342,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
 // c+1+w, c+9+w, ... in increasing order, then warp 0 adds the owner's partial
 // and the eight warp sums in warp order: a fixed order, independent of timing.
 template <typename T, typename A, int VPL>
-__global__ void __launch_bounds__(RED_THREADS) k_fixup(ReduceParams p) {
-    constexpr int NWARP = RED_THREADS / 32;
+__global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
+    constexpr int NWARP = FIX_THREADS / 32;
     extern __shared__ __align__(16) unsigned char fix_smem[];
     A* wsum = reinterpret_cast<A*>(fix_smem);          // [NWARP][dpad]
     __shared__ uint32_t s_last, s_kept;
@@ -322,15 +359,28 @@ __global__ void __launch_bounds__(RED_THREADS) k_fixup(ReduceParams p) {
         const uint32_t fl = p.carry_flags[c];
         if (!(fl & CF_OWNER)) continue;                 // CTA-uniform
         const uint32_t f = p.carry_f[c];
-        if (threadIdx.x == 0) {
-            // last position holding f: upper bound in skey[(c+1)*C, M)
-            uint32_t lo = (c + 1) * C, hi = M;          // skey[lo] == f is guaranteed
-            while (hi - lo > 1) {
-                const uint32_t mid = lo + (hi - lo) / 2;
-                if (p.skey[mid] == f) lo = mid; else hi = mid;
+        if (w == 0) {
+            if (p.out_mode == OUT_ADAM && lane == 0) {
+                if constexpr (sizeof(T) != 8) prefetch_row_state<T>(p, f);
             }
-            s_last = lo / C;
-            s_kept = 0;
+            // chunk holding the feature's last item: usually c + 1; otherwise a
+            // 32-ary search over [(c+1)*C, M), where skey == f is a prefix
+            uint32_t last = c + 1;
+            if (p.carry_flags[c + 1] & CF_THROUGH) {
+                uint32_t lo = (c + 2) * C - 1, hi = M;   // skey[lo] == f, skey[hi] != f (or hi == M)
+                while (hi - lo > 1) {
+                    const uint32_t span = hi - lo;
+                    const uint32_t stepw = span > 32 ? span / 32 : 1;
+                    const uint32_t probe = lo + (uint32_t)(lane + 1) * stepw;
+                    const bool in = probe < hi && p.skey[probe] == f;
+                    const uint32_t k = __popc(__ballot_sync(FULL, in));
+                    const uint32_t nlo = lo + k * stepw;
+                    hi = min(hi, nlo + stepw);
+                    lo = nlo;
+                }
+                last = lo / C;
+            }
+            if (lane == 0) { s_last = last; s_kept = 0; }
         }
         __syncthreads();
         const uint32_t last = s_last;
@@ -416,9 +466,9 @@ static void red_launch(const ReduceParams& p, uint64_t cap, cudaStream_t s, int 
         if (ctas > RED_MAX_CTAS) ctas = RED_MAX_CTAS;
         k_reduce<T, A, VPL><<<ctas, RED_THREADS, 0, s>>>(p);
     } else {
-        uint32_t ctas = std::min<uint32_t>(warps, 152 * 4);
-        const size_t smem = (size_t)(RED_THREADS / 32) * p.dpad * sizeof(A);
-        k_fixup<T, A, VPL><<<ctas, RED_THREADS, smem, s>>>(p);
+        uint32_t ctas = std::min<uint32_t>(warps, 152 * 16);
+        const size_t smem = (size_t)(FIX_THREADS / 32) * p.dpad * sizeof(A);
+        k_fixup<T, A, VPL><<<ctas, FIX_THREADS, smem, s>>>(p);
     }
 }
 

@@ -1,5 +1,8 @@
 // ep_sort.cu -- stable LSD radix sort of gradient items by feature id.
 //
+// The value carried with each key is the item's (role-src, count-weight bits)
+// pair, so the reduction reads both with one coalesced load.
+//
 // Replaces the per-batch std::HashMap merge of src/algos/ep/mod.rs:223-233
 // and the racy Hogwild row writes (src/hogwild.rs:15-60): after a stable sort
 // by feature id the items of one feature are contiguous and keep their
@@ -70,9 +73,11 @@ __global__ void __launch_bounds__(256) k_radix_colscan(const BatchState* st, uin
 }
 
 __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(const uint32_t* __restrict__ keys_in,
-                                                                const uint32_t* __restrict__ vals_in,
+                                                                const uint2* __restrict__ vals_in,
+                                                                const uint32_t* __restrict__ item_src,
+                                                                const float* __restrict__ item_c,
                                                                 uint32_t* __restrict__ keys_out,
-                                                                uint32_t* __restrict__ vals_out,
+                                                                uint2* __restrict__ vals_out,
                                                                 const BatchState* st, int shift,
                                                                 const uint32_t* __restrict__ hist,
                                                                 const uint32_t* __restrict__ dtot) {
@@ -97,13 +102,15 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(const uint32_t* 
         for (int i = threadIdx.x; i < (SORT_THREADS / 32) * 256; i += SORT_THREADS) (&wcount[0][0])[i] = 0;
         __syncthreads();
         const uint32_t base = tile * SORT_TILE + w * (32 * SORT_ROUNDS);
-        uint32_t key[SORT_ROUNDS], val[SORT_ROUNDS], rank[SORT_ROUNDS];
+        uint32_t key[SORT_ROUNDS], rank[SORT_ROUNDS];
+        uint2 val[SORT_ROUNDS];
 #pragma unroll
         for (int r = 0; r < SORT_ROUNDS; ++r) {
             const uint32_t i = base + r * 32 + lane;
             const bool ok = i < n;
             key[r] = ok ? keys_in[i] : 0u;
-            val[r] = ok ? (vals_in ? vals_in[i] : i) : 0u;
+            val[r] = ok ? (vals_in ? vals_in[i] : make_uint2(item_src[i], __float_as_uint(item_c[i])))
+                        : make_uint2(0u, 0u);
             const uint32_t dig = ok ? ((key[r] >> shift) & 255u) : 256u;
             const unsigned peers = __match_any_sync(FULL, dig);
             const uint32_t before = ok ? wcount[w][dig] : 0u;
@@ -139,34 +146,35 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(const uint32_t* 
     }
 }
 
-// Sorts keys[0, n_items) with values = original positions.  Ping-pongs
-// between (keys, keys_alt) and (idx, idx_alt); returns where the result is.
-void launch_radix_sort(BatchState* st, uint32_t* keys, uint32_t* keys_alt, uint32_t* idx, uint32_t* idx_alt,
-                       uint32_t* hist, uint64_t cap, int key_bits, uint32_t** sorted_keys, uint32_t** sorted_idx,
-                       cudaStream_t s) {
+// Sorts keys[0, n_items) carrying (item_src, item_c) values.  Ping-pongs
+// between (keys, keys_alt) and (vals, vals_alt); returns where the result is.
+void launch_radix_sort(BatchState* st, uint32_t* keys, uint32_t* keys_alt, const uint32_t* item_src,
+                       const float* item_c, uint2* vals, uint2* vals_alt, uint32_t* hist, uint64_t cap,
+                       int key_bits, uint32_t** sorted_keys, uint2** sorted_vals, cudaStream_t s) {
     const uint64_t tiles = (cap + SORT_TILE - 1) / SORT_TILE;
     const unsigned grid = (unsigned)(tiles < SORT_MAX_GRID ? (tiles ? tiles : 1) : SORT_MAX_GRID);
     const int passes = key_bits <= 0 ? 1 : (key_bits + 7) / 8;
-    // pass p reads K[p % 2] and writes K[(p + 1) % 2]; values start as the
-    // identity (vals_in == nullptr) and then alternate between idx / idx_alt.
+    // pass p reads K[p % 2] and writes K[(p + 1) % 2]; values start from the
+    // item arrays (vals_in == nullptr) and then alternate between vals / vals_alt.
     uint32_t* K[2] = {keys, keys_alt};
-    uint32_t* V[2] = {idx, idx_alt};
-    uint32_t *kin = nullptr, *vin = nullptr;
+    uint2* V[2] = {vals, vals_alt};
+    uint32_t* kin = nullptr;
+    uint2* vin = nullptr;
+    uint32_t* dtot = hist + radix_hist_entries(cap) - 256;
     for (int p = 0; p < passes; ++p) {
         const int shift = 8 * p;
         kin = K[p & 1];
         uint32_t* kout = K[(p + 1) & 1];
         vin = p == 0 ? nullptr : V[(p - 1) & 1];
-        uint32_t* vout = V[p & 1];
-        uint32_t* dtot = hist + radix_hist_entries(cap) - 256;
+        uint2* vout = V[p & 1];
         k_radix_hist<<<grid, SORT_THREADS, 0, s>>>(kin, st, shift, hist);
         k_radix_colscan<<<32, 256, 0, s>>>(st, hist, dtot);
-        k_radix_scatter<<<grid, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, st, shift, hist, dtot);
+        k_radix_scatter<<<grid, SORT_THREADS, 0, s>>>(kin, vin, item_src, item_c, kout, vout, st, shift, hist, dtot);
         kin = kout;
         vin = vout;
     }
     *sorted_keys = kin;
-    *sorted_idx = vin;
+    *sorted_vals = vin;
 }
 
 }  // namespace ep
