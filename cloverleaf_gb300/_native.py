@@ -137,6 +137,7 @@ SIGNATURES = {
     "ep_batch_grad": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), ctypes.POINTER(EpSparseGrad)]),
     "ep_batch_step": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), _F32, _U32]),
     "ep_get_table": (ctypes.c_int, [_P, _P]),
+    "ep_get_table_static": (ctypes.c_int, [_P, _U64, _U64, _P]),
     "ep_ag_forward": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), ctypes.c_int, _P, _P, _P]),
     "ep_ag_backward": (ctypes.c_int, [_P, _P, _P, _P]),
     "ep_synchronize": (ctypes.c_int, [_P]),

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -925,5 +926,79 @@ extern "C" int ep_ag_backward(ep_ctx* c, const void* dloss_dev, void* grad_dev, 
                      (uint32_t)std::min<uint64_t>(c->n_feat, c->items_cap), s);
     CK(cudaGetLastError(), "gradient scatter");
     CK(cudaStreamSynchronize(s), "autograd backward");
+    return EP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Table download without device allocation (no counterpart in the reference).
+//
+// ep_get_table stages the whole table as dense FP32 in a context buffer that
+// it allocates on first use: n_feat * dims * 4 bytes, 10 GB for 10M features
+// at 256 dims.  Some callers cannot allocate device memory at that point: a
+// process whose HBM is already held by the table and by a caching allocator
+// or memory pool, or a serving loop that reads rows while other work runs and
+// must not call cudaMalloc/cudaFree (which can synchronise the device).
+// ep_get_table_static reads a window of rows through a fixed scratch that is
+// part of the library's static device image, so the call allocates nothing.
+//
+// The scratch belongs to the device, not to a context: calls on one device
+// that overlap in time (from two host threads, or two contexts on different
+// streams) write the same scratch and corrupt each other's rows, so callers
+// serialise them.  Nothing in the scratch has to start at zero: each call
+// writes every element it copies out before the copy.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kStaticScratchBytes = (size_t)8 << 20;   // 8 MiB
+static_assert(kStaticScratchBytes == (size_t)EP_STATIC_SCRATCH_BYTES, "header and scratch size disagree");
+constexpr int kStaticMaxDevices = 64;
+
+__device__ __align__(256) float g_static_scratch[kStaticScratchBytes / sizeof(float)];
+
+std::mutex g_static_mu;
+float* g_static_ptr[kStaticMaxDevices] = {};   // device address of g_static_scratch, per device
+
+// Looks up the scratch's device address once per device; the device must be
+// current.  Only the address returned here is handed to kernels and copies.
+cudaError_t static_scratch(int device, float** out) {
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_ptr[device]) {
+        float* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_static_scratch);
+        if (e != cudaSuccess) return e;
+        g_static_ptr[device] = p;
+    }
+    *out = g_static_ptr[device];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int ep_get_table_static(ep_ctx* c, uint64_t first_row, uint64_t n_rows, float* out) {
+    if (!c) return EP_ERR_INVALID_ARG;
+    if (!out && n_rows) return c->fail(EP_ERR_INVALID_ARG, "out is NULL");
+    if (!c->table_ok) return c->fail(EP_ERR_STATE, "no table");
+    if (first_row > c->n_feat || n_rows > c->n_feat - first_row)
+        return c->fail(EP_ERR_INVALID_ARG, "rows [%llu, %llu) outside the table's %u rows",
+                       (unsigned long long)first_row, (unsigned long long)(first_row + n_rows), c->n_feat);
+    const uint64_t row_bytes = (uint64_t)c->dims * sizeof(float);
+    const uint64_t max_rows = kStaticScratchBytes / row_bytes;
+    if (n_rows > max_rows)
+        return c->fail(EP_ERR_INVALID_ARG,
+                       "%llu rows exceed the %zu-byte static scratch: at most %llu rows of %u dims per call",
+                       (unsigned long long)n_rows, kStaticScratchBytes, (unsigned long long)max_rows, c->dims);
+    if (c->device < 0 || c->device >= kStaticMaxDevices)
+        return c->fail(EP_ERR_UNSUPPORTED, "device %d beyond the %d devices the static scratch serves", c->device,
+                       kStaticMaxDevices);
+    CK(cudaSetDevice(c->device), "select device");
+    float* scratch = nullptr;
+    CK(static_scratch(c->device, &scratch), "cudaGetSymbolAddress of the static scratch");
+    if (!n_rows) return EP_OK;
+    const size_t es = c->tt == TT_BF16 ? 2 : (c->tt == TT_F32 ? 4 : 8);
+    const char* rows = c->table.as<const char>() + first_row * c->dpad * es;
+    launch_convert_table(c->tt, const_cast<char*>(rows), scratch, n_rows, c->dims, c->dpad, 0, c->stream);
+    CK(cudaGetLastError(), "static table download");
+    CK(cudaMemcpyAsync(out, scratch, n_rows * row_bytes, cudaMemcpyDeviceToHost, c->stream), "static table download");
+    CK(cudaStreamSynchronize(c->stream), "static table download");
     return EP_OK;
 }

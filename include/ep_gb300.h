@@ -192,6 +192,25 @@ int ep_batch_step(ep_ctx* ctx, const ep_batch_samples* samples, float lr, uint32
  * returned by learn (src/lib.rs:1362-1368). */
 int ep_get_table(ep_ctx* ctx, float* out);
 
+/* Row download without device allocation (no counterpart in the reference).
+ * Writes rows [first_row, first_row + n_rows) of the table to out (host
+ * memory, n_rows * dims FP32), the same values ep_get_table gives for them.
+ * ep_get_table stages the whole table in a device buffer it allocates on
+ * first use (n_feat * dims * 4 bytes); this call instead goes through a fixed
+ * scratch of EP_STATIC_SCRATCH_BYTES in the library's static device image and
+ * allocates no device memory.  It is meant for callers that cannot allocate
+ * at that point: HBM already held by the table and a memory pool, or a
+ * serving loop that must not call cudaMalloc/cudaFree while other work runs.
+ * Limit: at most EP_STATIC_SCRATCH_BYTES / (4 * dims) rows per call (4096 rows
+ * at 512 dims); a larger window fails with EP_ERR_INVALID_ARG and no work is
+ * done.  The first call on each device looks up the scratch's device address;
+ * make that first call before any stream capture begins.  The scratch is
+ * shared by every context on a device, so calls on one device must not
+ * overlap in time (they would overwrite each other's rows).  Nothing in the
+ * scratch needs to start at zero. */
+#define EP_STATIC_SCRATCH_BYTES (8u << 20)
+int ep_get_table_static(ep_ctx* ctx, uint64_t first_row, uint64_t n_rows, float* out);
+
 /* Device-pointer entry points behind the torch.autograd.Function binding.
  * precision: 0 = FP32 table/compute, 1 = FP64 (gradient checks only).
  * ep_ag_forward computes per-anchor losses (loss_dev, n_anchors values of the
