@@ -80,10 +80,11 @@ struct ep_ctx {
     DevBuf st, st_eval, st_inj;
     DevBuf anchors, nbr, nbr_w, nbr_cnt, neg, occ, dir, scale, valid, loss, status, deferred;
     DevBuf item_f, item_src, item_c, key_alt, idx, idx_alt, hist;
-    DevBuf carry_head, carry_tail, carry_f, carry_flags, gdense, touched, n_touched, packed, xfer, bound;
+    DevBuf carry_head, carry_tail, carry_f, carry_flags, long_list, gdense, touched, n_touched, packed, xfer, bound;
     uint64_t items_cap = 0;
     uint32_t buf_B = 0, buf_K = 0, buf_es = 0;
     uint32_t chunk = 128;
+    bool fused_split = true;    // FUSED form: reduce to gradient rows, then a separate Adam kernel
     bool prepared = false;
     cudaGraphExec_t gexec = nullptr;
     uint32_t* sorted_keys = nullptr;
@@ -191,7 +192,7 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     c->cfg = *cfg;
     c->device = cfg->device;
     if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMallocHost((void**)&c->h_st, sizeof(BatchState)) != cudaSuccess) {
+        cudaMallocHost((void**)&c->h_st, sizeof(BatchState)) != cudaSuccess || reduce_kernels_setup() != cudaSuccess) {
         g_create_err = std::string("CUDA setup failed: ") + cudaGetErrorString(cudaGetLastError());
         delete c;
         return EP_ERR_CUDA;
@@ -202,6 +203,7 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     c->tt = cfg->form == EP_FORM_FUSED_BF16 ? TT_BF16 : TT_F32;
     c->R = cfg->negatives;
     c->NR = c->R + 2;
+    if (const char* fs = getenv("EP_FUSED_SPLIT")) c->fused_split = atoi(fs) != 0;   // (tuning)
     if (const char* ch = getenv("EP_REDUCE_CHUNK")) {   // reducer items per warp (tuning)
         const long v = atol(ch);
         if (v >= 32 && v <= (1l << 20)) c->chunk = (uint32_t)v;
@@ -366,7 +368,8 @@ static int ensure_bufs(ep_ctx* c, uint32_t B, uint32_t K, uint64_t items, uint32
                   c->key_alt.ensure(items * 4) && c->idx.ensure(items * 8) && c->idx_alt.ensure(items * 8) &&
                   c->hist.ensure(radix_hist_entries(items) * 4) && c->carry_head.ensure((size_t)nch * c->dpad * es) &&
                   c->carry_tail.ensure((size_t)nch * c->dpad * es) && c->carry_f.ensure((size_t)nch * 4) &&
-                  c->carry_flags.ensure((size_t)nch * 4) && c->n_touched.ensure(4);
+                  c->carry_flags.ensure((size_t)nch * 4) && c->long_list.ensure((size_t)nch * 4) &&
+                  c->n_touched.ensure(4);
         if (!ok) return c->fail(EP_ERR_OOM, "batch scratch allocation failed (B=%u K=%u items=%llu)", B, K, (unsigned long long)items);
         c->buf_B = B;
         c->buf_K = K;
@@ -422,7 +425,7 @@ static int prepare_train(ep_ctx* c) {
     uint64_t items = 0;
     for (uint32_t i = 0; i < top; ++i) items += hb[i];
     if (items > 0xfffffff0ull) return c->fail(EP_ERR_UNSUPPORTED, "a batch can emit more than 2^32 gradient items");
-    int rc = ensure_bufs(c, B, K, items, 4, c->cfg.form == EP_FORM_PLAIN_FP32);
+    int rc = ensure_bufs(c, B, K, items, 4, c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_split);
     if (rc) return rc;
     c->Bcap = B;
     c->Kcap = c->buf_K;
@@ -523,6 +526,7 @@ static ReduceParams reduce_params(ep_ctx* c, BatchState* st, int out_mode, void*
     rp.carry_tail = c->carry_tail.p;
     rp.carry_f = c->carry_f.as<uint32_t>();
     rp.carry_flags = c->carry_flags.as<uint32_t>();
+    rp.long_list = c->long_list.as<uint32_t>();
     return rp;
 }
 
@@ -541,8 +545,8 @@ static void sort_and_reduce(ep_ctx* c, BatchState* st, int tt, int out_mode, voi
 static uint32_t kernels_per_batch(const ep_ctx* c) {
     const uint32_t b = bits_for(c->n_feat);
     const uint32_t radix = 3 * (b ? (b + 7) / 8 : 1);
-    return 3 /* begin, sample, scan */ + 2 /* forward: staged, direct */ + radix + 2 /* reduce, fixup */ +
-           (c->cfg.form == EP_FORM_PLAIN_FP32 ? 1 : 0) + 1 /* end */;
+    return 3 /* begin, sample, scan */ + 2 /* forward: staged, direct */ + radix + 3 /* reduce, fixup x2 */ +
+           (c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_split ? 1 : 0) + 1 /* end */;
 }
 
 // Issues one training batch on the context stream; ev (optional) receives an
@@ -562,7 +566,7 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr) {
                       c->item_c.as<float>(), c->idx.as<uint2>(), c->idx_alt.as<uint2>(), c->hist.as<uint32_t>(),
                       c->items_cap, (int)bits_for(c->n_feat), &c->sorted_keys, &c->sorted_vals, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_SORT], s);
-    const bool plain = c->cfg.form == EP_FORM_PLAIN_FP32;
+    const bool plain = c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_split;
     if (plain) cudaMemsetAsync(c->n_touched.p, 0, 4, s);
     ReduceParams rp = reduce_params(c, st, plain ? OUT_DENSE : OUT_ADAM, c->table.p);
     launch_reduce(c->tt, (int)c->vpl, rp, c->items_cap, s);

@@ -49,7 +49,7 @@ struct BatchState {
     // pass accumulators (reset by the host at a pass start)
     double pass_err_sum;
     uint32_t pass_batches;
-    uint32_t pad0;
+    uint32_t n_long;        // long-span fixups queued by k_fixup for k_fixup_long
     unsigned long long anchors, kept, nan_anchors, items, gathered, unique_rows, sampled;
     double valid_sum;
 };
@@ -148,6 +148,7 @@ struct ReduceParams {
     void* carry_tail;
     uint32_t* carry_f;
     uint32_t* carry_flags;
+    uint32_t* long_list;    // owner chunks of long spans [n_chunks]
 };
 
 // ---- launchers (defined in the kernel translation units) -----------------
@@ -183,5 +184,6 @@ void launch_pack_rows(size_t es, const void* dense, const uint32_t* rows, const 
                       cudaStream_t s);
 size_t radix_hist_entries(uint64_t cap);
 uint32_t reduce_chunks(uint64_t cap, uint32_t chunk);
+cudaError_t reduce_kernels_setup();
 
 }  // namespace ep

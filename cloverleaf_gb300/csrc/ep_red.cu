@@ -43,7 +43,47 @@ constexpr uint32_t RED_MAX_CTAS = 152 * 8;
 uint32_t reduce_chunks(uint64_t cap, uint32_t chunk) { return (uint32_t)((cap + chunk - 1) / chunk); }
 
 // Adam on one row (optimizer.rs:43-81): t = pass + 1, beta1 0.9, beta2 0.999,
-// eps 1e-8; rows containing NaN are skipped (optimizer.rs:56).
+// eps 1e-8; rows containing NaN are skipped (optimizer.rs:56).  adam_apply
+// takes the row's loaded moments and weights (mm, vv, ee) and stores the
+// updated row.
+template <typename T, int VPL>
+__device__ __forceinline__ void adam_apply(T* __restrict__ table, float* __restrict__ m, float* __restrict__ v,
+                                           uint32_t f, uint32_t dpad, const float (&g)[VPL], float (&mm)[VPL],
+                                           float (&vv)[VPL], float (&ee)[VPL], float lr, float bc1, float bc2,
+                                           uint64_t seed, uint32_t step, int lane) {
+    const uint64_t o = (uint64_t)f * dpad;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) {
+        const float gk = g[k];
+        mm[k] = b1 * mm[k] + (1.f - b1) * gk;
+        vv[k] = b2 * vv[k] + (1.f - b2) * (gk * gk);
+        const float mh = mm[k] / bc1;
+        const float vh = vv[k] / bc2;
+        ee[k] -= lr * (mh / (sqrtf(vh) + eps));
+    }
+    RowIO<float, VPL>::store_raw(m + o, lane, mm);
+    RowIO<float, VPL>::store_raw(v + o, lane, vv);
+    if constexpr (std::is_same<T, float>::value) {
+        RowIO<float, VPL>::store_raw(table + o, lane, ee);
+    } else {
+        // BF16 table: stochastic rounding, 16 random bits per element from
+        // one Philox block per 8 elements.
+        __nv_bfloat16 out[VPL];
+#pragma unroll
+        for (int k0 = 0; k0 < VPL; k0 += 8) {
+            const u32x4 r = philox(u32x4{f, step, (ST_ROUND << 24) | (uint32_t)lane, (uint32_t)k0}, seed);
+            const uint32_t w[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+            for (int k = k0; k < k0 + 8 && k < VPL; ++k) {
+                const uint32_t bits = (k & 1) ? (w[(k - k0) >> 1] >> 16) : (w[(k - k0) >> 1] & 0xffffu);
+                out[k] = bf16_stochastic(ee[k], bits);
+            }
+        }
+        RowIO<__nv_bfloat16, VPL>::store_raw(table + o, lane, out);
+    }
+}
+
 template <typename T, int VPL, typename A>
 __device__ __forceinline__ void adam_row(T* __restrict__ table, float* __restrict__ m, float* __restrict__ v,
                                          uint32_t f, uint32_t dpad, const A (&g)[VPL], float lr, float bc1, float bc2,
@@ -56,52 +96,46 @@ __device__ __forceinline__ void adam_row(T* __restrict__ table, float* __restric
         return;  // FP64 tables exist only for gradient checks
     } else {
         const uint64_t o = (uint64_t)f * dpad;
-        float mm[VPL], vv[VPL], ee[VPL];
+        float gg[VPL], mm[VPL], vv[VPL], ee[VPL];
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) gg[k] = (float)g[k];
         RowIO<float, VPL>::load_cg(m + o, lane, mm);
         RowIO<float, VPL>::load_cg(v + o, lane, vv);
         RowIO<T, VPL>::load_cg(table + o, lane, ee);
-        const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-#pragma unroll
-        for (int k = 0; k < VPL; ++k) {
-            const float gk = (float)g[k];
-            mm[k] = b1 * mm[k] + (1.f - b1) * gk;
-            vv[k] = b2 * vv[k] + (1.f - b2) * (gk * gk);
-            const float mh = mm[k] / bc1;
-            const float vh = vv[k] / bc2;
-            ee[k] -= lr * (mh / (sqrtf(vh) + eps));
-        }
-        RowIO<float, VPL>::store_raw(m + o, lane, mm);
-        RowIO<float, VPL>::store_raw(v + o, lane, vv);
-        if constexpr (std::is_same<T, float>::value) {
-            RowIO<float, VPL>::store_raw(table + o, lane, ee);
-        } else {
-            // BF16 table: stochastic rounding, 16 random bits per element from
-            // one Philox block per 8 elements.
-            __nv_bfloat16 out[VPL];
-#pragma unroll
-            for (int k0 = 0; k0 < VPL; k0 += 8) {
-                const u32x4 r = philox(u32x4{f, step, (ST_ROUND << 24) | (uint32_t)lane, (uint32_t)k0}, seed);
-                const uint32_t w[4] = {r.x, r.y, r.z, r.w};
-#pragma unroll
-                for (int k = k0; k < k0 + 8 && k < VPL; ++k) {
-                    const uint32_t bits = (k & 1) ? (w[(k - k0) >> 1] >> 16) : (w[(k - k0) >> 1] & 0xffffu);
-                    out[k] = bf16_stochastic(ee[k], bits);
-                }
-            }
-            RowIO<__nv_bfloat16, VPL>::store_raw(table + o, lane, out);
-        }
+        adam_apply<T, VPL>(table, m, v, f, dpad, gg, mm, vv, ee, lr, bc1, bc2, seed, step, lane);
     }
 }
 
-template <typename T, typename A, int VPL>
+// Per-warp list of features finished in OUT_DENSE mode, flushed to the
+// touched list with one atomic per FIN_CAP entries (or at the end).
+constexpr uint32_t FIN_CAP = 64;
+
+__device__ __forceinline__ void fin_flush(const ReduceParams& p, uint32_t* fin, uint32_t& n_fin, int lane) {
+    if (!n_fin) return;
+    __syncwarp();
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(p.n_touched, n_fin);
+    base = __shfl_sync(FULL, base, 0);
+    for (uint32_t j = lane; j < n_fin; j += 32) p.touched[base + j] = fin[j];
+    __syncwarp();
+    n_fin = 0;
+}
+
+template <typename T, typename A, int VPL, int MODE>
 __device__ __forceinline__ void finish_row(const ReduceParams& p, uint32_t f, const A (&acc)[VPL], int lane,
-                                           bool lane_on, float lr, float bc1, float bc2, uint32_t step) {
-    if (p.out_mode == OUT_DENSE) {
+                                           bool lane_on, float lr, float bc1, float bc2, uint32_t step,
+                                           uint32_t* fin, uint32_t& n_fin) {
+    if constexpr (MODE == OUT_DENSE) {
         if (lane_on) store_row<A, VPL, A>((A*)p.gdense + (uint64_t)f * p.dpad, lane, acc);
-        if (lane == 0) p.touched[atomicAdd(p.n_touched, 1u)] = f;
-        return;
+        if (fin) {
+            if (lane == 0) fin[n_fin] = f;
+            if (++n_fin == FIN_CAP) fin_flush(p, fin, n_fin, lane);
+        } else if (lane == 0) {
+            p.touched[atomicAdd(p.n_touched, 1u)] = f;
+        }
+    } else {
+        adam_row<T, VPL, A>((T*)p.table, p.m, p.v, f, p.dpad, acc, lr, bc1, bc2, p.seed, step, lane, lane_on);
     }
-    adam_row<T, VPL, A>((T*)p.table, p.m, p.v, f, p.dpad, acc, lr, bc1, bc2, p.seed, step, lane, lane_on);
 }
 
 // Bulk L2 prefetch (cp.async.bulk.prefetch) of one feature's Adam state:
@@ -173,9 +207,13 @@ __device__ __forceinline__ void add_rows(const ReduceParams& p, unsigned mask, u
 // carried across batches and, at a chunk start, found by walking back.  Then
 // the warp walks the feature segments of the batch, adding the kept items'
 // rows in item order and finishing each feature as its segment closes.
-template <typename T, typename A, int VPL>
-__global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
+template <typename T, typename A, int VPL, int MODE>
+__global__ void __launch_bounds__(RED_THREADS, VPL >= 16 ? 1 : (MODE == OUT_DENSE ? 3 : 2)) k_reduce(ReduceParams p) {
+    __shared__ uint32_t fin_all[RED_THREADS / 32][FIN_CAP];
     const int lane = threadIdx.x & 31;
+    uint32_t* fin = fin_all[threadIdx.x >> 5];
+    uint32_t n_fin = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) p.st->n_long = 0;   // read by k_fixup / k_fixup_long
     const unsigned lt_mask = (1u << lane) - 1u;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -227,7 +265,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
         bool started_here = !head_partial;
         bool any_kept = false;
         uint32_t flags = 0;
-        if (p.out_mode == OUT_ADAM) prefetch_segment_state<T>(p, i0, i1, lane);
+        if constexpr (MODE == OUT_ADAM) prefetch_segment_state<T>(p, i0, i1, lane);
         for (uint32_t ib = i0; ib < i1; ib += 32) {
             const uint32_t i = ib + lane;
             const bool act = i < i1;
@@ -244,7 +282,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
             }
             // look ahead: warm L2 with the Adam state of features starting in the
             // next batch, so their updates do not wait for DRAM
-            if (p.out_mode == OUT_ADAM) prefetch_segment_state<T>(p, ib + 32, i1, lane);
+            if constexpr (MODE == OUT_ADAM) prefetch_segment_state<T>(p, ib + 32, i1, lane);
             const uint32_t anchor = s / NR;
             // predecessor of each lane (lane 0: the carried item before the batch)
             uint32_t pf = __shfl_up_sync(FULL, f, 1), pa = __shfl_up_sync(FULL, anchor, 1);
@@ -290,7 +328,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
                     // a new segment starts at lo: close the current one first
                     if (started_here) {
                         if (any_kept) {
-                            finish_row<T, A, VPL>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step);
+                            finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step, fin, n_fin);
                             ++u_cnt;
                         }
                     } else {
@@ -316,7 +354,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
         const bool cont = i1 < M && p.skey[i1] == cur_f;
         if (started_here && !cont) {
             if (any_kept) {
-                finish_row<T, A, VPL>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step);
+                finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step, fin, n_fin);
                 ++u_cnt;
             }
         } else if (!started_here) {
@@ -329,6 +367,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
         }
         if (lane == 0) p.carry_flags[c] = flags;
     }
+    if constexpr (MODE == OUT_DENSE) fin_flush(p, fin, n_fin, lane);
     g_cnt = warp_sum<unsigned long long>(g_cnt);
     if (lane == 0) {
         if (g_cnt) atomicAdd(&p.st->gathered, g_cnt);
@@ -336,18 +375,39 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce(ReduceParams p) {
     }
 }
 
-// k_fixup: one CTA per owner chunk (a chunk whose last feature continues into
-// later chunks).  The feature's last item is found by binary search, so the
-// chunks holding its partial sums are known up front; warp w adds partials
-// c+1+w, c+9+w, ... in increasing order, then warp 0 adds the owner's partial
-// and the eight warp sums in warp order: a fixed order, independent of timing.
-template <typename T, typename A, int VPL>
+// Chunk holding the last item of feature f, whose segment starts in chunk c
+// and continues into c + 1: usually c + 1; otherwise a 32-ary warp search
+// over [(c+2)*C - 1, M), where skey == f is a prefix.
+__device__ __forceinline__ uint32_t owner_last(const ReduceParams& p, uint32_t c, uint32_t f, uint32_t M, uint32_t C,
+                                               int lane) {
+    if (!(p.carry_flags[c + 1] & CF_THROUGH)) return c + 1;
+    uint32_t lo = (c + 2) * C - 1, hi = M;   // skey[lo] == f; skey[hi] != f or hi == M
+    while (hi - lo > 1) {
+        const uint32_t span = hi - lo;
+        const uint32_t stepw = span > 32 ? span / 32 : 1;
+        const uint32_t probe = lo + (uint32_t)(lane + 1) * stepw;
+        const bool in = probe < hi && p.skey[probe] == f;
+        const uint32_t k = __popc(__ballot_sync(FULL, in));
+        const uint32_t nlo = lo + k * stepw;
+        hi = min(hi, nlo + stepw);
+        lo = nlo;
+    }
+    return lo / C;
+}
+
+// k_fixup: one warp per owner chunk (a chunk whose last feature continues into
+// later chunks).  Spans of up to FIX_SHORT partials are summed by the warp in
+// chunk order (owner's tail, then the heads of c+1 .. last) and finished;
+// longer spans are queued for k_fixup_long.
+constexpr uint32_t FIX_SHORT = 16;
+// k_fixup_long block size: as many warps as the row width leaves registers for
+__host__ __device__ constexpr int fixl_threads(int vpl) { return vpl >= 16 ? 256 : (vpl >= 8 ? 512 : 1024); }
+
+template <typename T, typename A, int VPL, int MODE>
 __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
-    constexpr int NWARP = FIX_THREADS / 32;
-    extern __shared__ __align__(16) unsigned char fix_smem[];
-    A* wsum = reinterpret_cast<A*>(fix_smem);          // [NWARP][dpad]
-    __shared__ uint32_t s_last, s_kept;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t M = p.st->n_items;
     const uint32_t C = p.chunk;
     const uint32_t nchunks = (M + C - 1) / C;
@@ -355,31 +415,75 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
     const float lr = p.st->lr, bc1 = p.st->bc1, bc2 = p.st->bc2;
     const uint32_t step = (uint32_t)p.st->step;
     unsigned long long u_cnt = 0;
-    for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    for (uint32_t c = gw; c < nchunks; c += nw) {
         const uint32_t fl = p.carry_flags[c];
-        if (!(fl & CF_OWNER)) continue;                 // CTA-uniform
+        if (!(fl & CF_OWNER)) continue;                 // warp-uniform
+        const uint32_t f = p.carry_f[c];
+        if constexpr (MODE == OUT_ADAM && sizeof(T) != 8) {
+            if (lane == 0) prefetch_row_state<T>(p, f);
+        }
+        const uint32_t last = owner_last(p, c, f, M, C, lane);
+        if (last - c > FIX_SHORT) {
+            if (lane == 0) p.long_list[atomicAdd(&p.st->n_long, 1u)] = c;
+            continue;
+        }
+        A acc[VPL];
+        if (lane_on) RowIO<A, VPL>::load_cg((const A*)p.carry_tail + (uint64_t)c * p.dpad, lane, acc);
+        else {
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) acc[k] = 0;
+        }
+        uint32_t kept = fl & CF_TAIL_KEPT;
+        for (uint32_t j = c + 1; j <= last; j += 4) {
+            A h[4][VPL];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (j + u <= last) {
+                    kept |= p.carry_flags[j + u] & CF_HEAD_KEPT;
+                    if (lane_on) RowIO<A, VPL>::load_cg((const A*)p.carry_head + (uint64_t)(j + u) * p.dpad, lane, h[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (j + u <= last && lane_on) {
+#pragma unroll
+                    for (int k = 0; k < VPL; ++k) acc[k] += h[u][k];
+                }
+            }
+        }
+        if (kept) {
+            uint32_t none = 0;
+            finish_row<T, A, VPL, MODE>(p, f, acc, lane, lane_on, lr, bc1, bc2, step, nullptr, none);
+            ++u_cnt;
+        }
+    }
+    if (lane == 0 && u_cnt) atomicAdd(&p.st->unique_rows, u_cnt);
+}
+
+// k_fixup_long: one CTA of NWARP warps per queued long span.  Warp w adds
+// the heads of chunks c+1+w, c+1+w+NWARP, ... in increasing order; warp 0 then
+// adds the owner's tail and the NWARP warp sums in warp order: a fixed order,
+// independent of timing and of the queue order.
+template <typename T, typename A, int VPL, int MODE>
+__global__ void __launch_bounds__(fixl_threads(VPL)) k_fixup_long(ReduceParams p) {
+    constexpr int NWARP = fixl_threads(VPL) / 32;
+    extern __shared__ __align__(16) unsigned char fixl_smem[];
+    A* wsum = reinterpret_cast<A*>(fixl_smem);          // [NWARP][dpad]
+    __shared__ uint32_t s_last, s_kept;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t M = p.st->n_items;
+    const uint32_t C = p.chunk;
+    const uint32_t n_long = p.st->n_long;
+    const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
+    const float lr = p.st->lr, bc1 = p.st->bc1, bc2 = p.st->bc2;
+    const uint32_t step = (uint32_t)p.st->step;
+    unsigned long long u_cnt = 0;
+    for (uint32_t q = blockIdx.x; q < n_long; q += gridDim.x) {
+        const uint32_t c = p.long_list[q];
+        const uint32_t fl = p.carry_flags[c];
         const uint32_t f = p.carry_f[c];
         if (w == 0) {
-            if (p.out_mode == OUT_ADAM && lane == 0) {
-                if constexpr (sizeof(T) != 8) prefetch_row_state<T>(p, f);
-            }
-            // chunk holding the feature's last item: usually c + 1; otherwise a
-            // 32-ary search over [(c+1)*C, M), where skey == f is a prefix
-            uint32_t last = c + 1;
-            if (p.carry_flags[c + 1] & CF_THROUGH) {
-                uint32_t lo = (c + 2) * C - 1, hi = M;   // skey[lo] == f, skey[hi] != f (or hi == M)
-                while (hi - lo > 1) {
-                    const uint32_t span = hi - lo;
-                    const uint32_t stepw = span > 32 ? span / 32 : 1;
-                    const uint32_t probe = lo + (uint32_t)(lane + 1) * stepw;
-                    const bool in = probe < hi && p.skey[probe] == f;
-                    const uint32_t k = __popc(__ballot_sync(FULL, in));
-                    const uint32_t nlo = lo + k * stepw;
-                    hi = min(hi, nlo + stepw);
-                    lo = nlo;
-                }
-                last = lo / C;
-            }
+            const uint32_t last = owner_last(p, c, f, M, C, lane);
             if (lane == 0) { s_last = last; s_kept = 0; }
         }
         __syncthreads();
@@ -388,7 +492,6 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
 #pragma unroll
         for (int k = 0; k < VPL; ++k) acc[k] = 0;
         uint32_t kept = 0;
-        // partials j = c+1+w, c+1+w+NWARP, ...: four loads in flight, summed in order
         for (uint32_t j = c + 1 + w; j <= last; j += 4 * NWARP) {
             A h[4][VPL];
 #pragma unroll
@@ -424,7 +527,8 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
                 }
             }
             if ((fl & CF_TAIL_KEPT) || s_kept) {
-                finish_row<T, A, VPL>(p, f, tot, lane, lane_on, lr, bc1, bc2, step);
+                uint32_t none = 0;
+                finish_row<T, A, VPL, MODE>(p, f, tot, lane, lane_on, lr, bc1, bc2, step, nullptr, none);
                 ++u_cnt;
             }
         }
@@ -433,7 +537,9 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
     if (threadIdx.x == 0 && u_cnt) atomicAdd(&p.st->unique_rows, u_cnt);
 }
 
-// PLAIN form: Adam over the touched list, reading the dense gradient rows.
+// Adam over the touched list, reading the dense gradient rows (PLAIN form,
+// and the FUSED form's split reduction).  Two rows per warp iteration, with
+// all eight row loads (g, m, v, table for each) issued before any is used.
 template <typename T, int VPL>
 __global__ void __launch_bounds__(RED_THREADS) k_adam_dense(BatchState* st, T* table, float* m, float* v,
                                                             const float* g, const uint32_t* touched,
@@ -445,15 +551,36 @@ __global__ void __launch_bounds__(RED_THREADS) k_adam_dense(BatchState* st, T* t
     const bool lane_on = (uint32_t)(lane * VPL) < dpad;
     const float lr = st->lr, bc1 = st->bc1, bc2 = st->bc2;
     const uint32_t step = (uint32_t)st->step;
-    for (uint32_t r = gw; r < n; r += nw) {
-        const uint32_t f = touched[r];
-        float gg[VPL];
-        if (lane_on) RowIO<float, VPL>::load_cg(g + (uint64_t)f * dpad, lane, gg);
-        else {
+    for (uint32_t r0 = 2 * gw; r0 < n; r0 += 2 * nw) {
+        uint32_t f[2];
+        bool on[2];
+        float gg[2][VPL], mm[2][VPL], vv[2][VPL], ee[2][VPL];
 #pragma unroll
-            for (int k = 0; k < VPL; ++k) gg[k] = 0.f;
+        for (int u = 0; u < 2; ++u) {
+            on[u] = r0 + u < n;
+            f[u] = on[u] ? touched[r0 + u] : 0u;
         }
-        adam_row<T, VPL, float>(table, m, v, f, dpad, gg, lr, bc1, bc2, seed, step, lane, lane_on);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (on[u] && lane_on) {
+                const uint64_t o = (uint64_t)f[u] * dpad;
+                RowIO<float, VPL>::load_cg(g + o, lane, gg[u]);
+                RowIO<float, VPL>::load_cg(m + o, lane, mm[u]);
+                RowIO<float, VPL>::load_cg(v + o, lane, vv[u]);
+                RowIO<T, VPL>::load_cg(table + o, lane, ee[u]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < VPL; ++k) gg[u][k] = mm[u][k] = vv[u][k] = ee[u][k] = 0.f;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            bool bad = false;
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) bad = bad || (gg[u][k] != gg[u][k]);
+            if (on[u] && !__any_sync(FULL, bad) && lane_on)
+                adam_apply<T, VPL>(table, m, v, f[u], dpad, gg[u], mm[u], vv[u], ee[u], lr, bc1, bc2, seed, step, lane);
+        }
     }
 }
 
@@ -464,12 +591,49 @@ static void red_launch(const ReduceParams& p, uint64_t cap, cudaStream_t s, int 
     if (which == 0) {
         uint32_t ctas = (warps + RED_THREADS / 32 - 1) / (RED_THREADS / 32);
         if (ctas > RED_MAX_CTAS) ctas = RED_MAX_CTAS;
-        k_reduce<T, A, VPL><<<ctas, RED_THREADS, 0, s>>>(p);
+        if (p.out_mode == OUT_DENSE) k_reduce<T, A, VPL, OUT_DENSE><<<ctas, RED_THREADS, 0, s>>>(p);
+        else k_reduce<T, A, VPL, OUT_ADAM><<<ctas, RED_THREADS, 0, s>>>(p);
     } else {
-        uint32_t ctas = std::min<uint32_t>(warps, 152 * 16);
-        const size_t smem = (size_t)(FIX_THREADS / 32) * p.dpad * sizeof(A);
-        k_fixup<T, A, VPL><<<ctas, FIX_THREADS, smem, s>>>(p);
+        uint32_t ctas = std::min<uint32_t>((warps + FIX_THREADS / 32 - 1) / (FIX_THREADS / 32), 152 * 16);
+        constexpr int LT = fixl_threads(VPL);
+        const size_t lsmem = (size_t)(LT / 32) * p.dpad * sizeof(A);
+        if (p.out_mode == OUT_DENSE) {
+            k_fixup<T, A, VPL, OUT_DENSE><<<ctas, FIX_THREADS, 0, s>>>(p);
+            k_fixup_long<T, A, VPL, OUT_DENSE><<<152, LT, lsmem, s>>>(p);
+        } else {
+            k_fixup<T, A, VPL, OUT_ADAM><<<ctas, FIX_THREADS, 0, s>>>(p);
+            k_fixup_long<T, A, VPL, OUT_ADAM><<<152, LT, lsmem, s>>>(p);
+        }
     }
+}
+
+template <typename T, typename A, int VPL>
+static cudaError_t fixl_setup() {
+    const int bytes = (fixl_threads(VPL) / 32) * VPL * 32 * (int)sizeof(A);
+    cudaError_t e = cudaFuncSetAttribute(k_fixup_long<T, A, VPL, OUT_DENSE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_fixup_long<T, A, VPL, OUT_ADAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return e;
+}
+
+template <typename T, typename A>
+static cudaError_t fixl_setup_all() {
+    cudaError_t e = cudaSuccess;
+    const cudaError_t r[5] = {fixl_setup<T, A, 1>(), fixl_setup<T, A, 2>(), fixl_setup<T, A, 4>(),
+                              fixl_setup<T, A, 8>(), fixl_setup<T, A, 16>()};
+    for (cudaError_t x : r)
+        if (x != cudaSuccess) e = x;
+    return e;
+}
+
+// Opts the long-span fixup kernels in to their dynamic shared memory (one row
+// per warp, up to 64 KB); called at context creation, outside any capture.
+cudaError_t reduce_kernels_setup() {
+    cudaError_t e = fixl_setup_all<float, float>();
+    const cudaError_t b = fixl_setup_all<__nv_bfloat16, float>();
+    const cudaError_t d = fixl_setup_all<double, double>();
+    return e != cudaSuccess ? e : (b != cudaSuccess ? b : d);
 }
 
 template <typename T, typename A>
