@@ -545,7 +545,8 @@ static void sort_and_reduce(ep_ctx* c, BatchState* st, int tt, int out_mode, voi
 static uint32_t kernels_per_batch(const ep_ctx* c) {
     const uint32_t b = bits_for(c->n_feat);
     const uint32_t radix = 3 * (b ? (b + 7) / 8 : 1);
-    return 3 /* begin, sample, scan */ + 2 /* forward: staged, direct */ + radix + 3 /* reduce, fixup x2 */ +
+    return 3 /* begin, sample, scan */ + 3 /* forward: staged, direct gather; loss */ + radix +
+           3 /* reduce, fixup x2 */ +
            (c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_split ? 1 : 0) + 1 /* end */;
 }
 

@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace ep {
 
 constexpr unsigned FULL = 0xffffffffu;
@@ -97,6 +99,25 @@ template <typename A, typename T> __device__ __forceinline__ A cvt_in(T x) { ret
 template <> __device__ __forceinline__ double cvt_in<double, double>(double x) { return x; }
 template <> __device__ __forceinline__ float cvt_in<float, double>(double x) { return (float)x; }
 
+// acc[k] += c * x[k] over a lane's slice.  FP32 pairs go through the packed
+// FMA of sm_100+ (__ffma2_rn: two independent fused multiply-adds, each
+// rounded once, so results equal the scalar loop's bit for bit).
+template <typename A, int VPL>
+__device__ __forceinline__ void axpy_slice(A (&acc)[VPL], A c, const A (&x)[VPL]) {
+    if constexpr (std::is_same<A, float>::value && VPL >= 2 && (VPL % 2) == 0) {
+        const float2 cc = make_float2(c, c);
+#pragma unroll
+        for (int k = 0; k < VPL; k += 2) {
+            const float2 r = __ffma2_rn(cc, make_float2(x[k], x[k + 1]), make_float2(acc[k], acc[k + 1]));
+            acc[k] = r.x;
+            acc[k + 1] = r.y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) acc[k] += c * x[k];
+    }
+}
+
 template <typename T, int VPL>
 struct RowIO {
     static constexpr int BYTES = VPL * (int)sizeof(T);
@@ -141,8 +162,10 @@ struct RowIO {
         union { V v[NV]; T t[VPL]; } u;
 #pragma unroll
         for (int i = 0; i < NV; ++i) u.v[i] = r.v[i];
+        A x[VPL];
 #pragma unroll
-        for (int k = 0; k < VPL; ++k) acc[k] += c * cvt_in<A, T>(u.t[k]);
+        for (int k = 0; k < VPL; ++k) x[k] = cvt_in<A, T>(u.t[k]);
+        axpy_slice<A, VPL>(acc, c, x);
     }
     static __device__ __forceinline__ void store_raw(T* row, int lane, const T (&in)[VPL]) {
         union { V v[NV]; T t[VPL]; } u;

@@ -282,8 +282,7 @@ __global__ void __launch_bounds__(1024) k_scan_occ(BatchState* st, uint32_t* occ
 // ---------------------------------------------------------------------------
 template <typename T, typename A, int VPL>
 __device__ __forceinline__ void fma_row(A (&acc)[VPL], A c, const A (&r)[VPL]) {
-#pragma unroll
-    for (int k = 0; k < VPL; ++k) acc[k] += c * r[k];
+    axpy_slice<A, VPL>(acc, c, r);
 }
 
 // Gathers one role: the (weighted) mean numerator over every feature
@@ -481,29 +480,56 @@ __device__ bool stage_anchor(const ForwardParams& p, WarpTables& W, uint32_t a, 
     return true;
 }
 
-// Phase C: the weighted sum of a role's rows from the occurrence table,
-// eight rows in flight; returns the role's weight total.
+// Phase C: every role's rows in occurrence order (role-major), U rows in
+// flight across role boundaries.  As each role closes, its mean
+// sum(c * row) / sum(c) is written to the role's direction row and its weight
+// total sum(c) to scale; the loss kernel reads both back.
 template <typename T, typename A, int VPL>
-__device__ __forceinline__ A role_from_table(const ForwardParams& p, const T* __restrict__ table, const WarpTables& W,
-                                             uint32_t r, A (&acc)[VPL], int lane, bool lane_on) {
-#pragma unroll
-    for (int k = 0; k < VPL; ++k) acc[k] = 0;
-    const uint32_t ob = W.role_ob[r], oe = W.role_ob[r + 1];
-    const uint32_t dpad = p.dpad;
+__device__ __forceinline__ void roles_from_table(const ForwardParams& p, const T* __restrict__ table,
+                                                 const WarpTables& W, uint32_t NR, uint64_t sbase, int lane,
+                                                 bool lane_on) {
     using IO = RowIO<T, VPL>;
     constexpr int U = IO::INFLIGHT;
-    if (lane_on) {
-        for (uint32_t j = ob; j < oe; j += U) {
-            typename IO::Raw rows[U];
+    const uint32_t dpad = p.dpad;
+    A* dir = (A*)p.dir;
+    A* scale = (A*)p.scale;
+    const uint32_t total = W.role_ob[NR];
+    A acc[VPL];
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) acc[k] = 0;
+    uint32_t r = 0, rend = W.role_ob[1];
+    auto close_role = [&]() {
+        const A n = (A)W.role_n[r];
+        if (lane_on) {
+            const A rn = (A)1 / n;
+            A m[VPL];
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) m[k] = acc[k] * rn;
+            store_row<A, VPL, A>(dir + (sbase + r) * dpad, lane, m);
+        }
+        if (lane == 0) scale[sbase + r] = n;
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) acc[k] = 0;
+        ++r;
+        if (r < NR) rend = W.role_ob[r + 1];
+    };
+    for (uint32_t j = 0; j < total; j += U) {
+        typename IO::Raw rows[U];
+        if (lane_on) {
 #pragma unroll
             for (int u = 0; u < U; ++u)
-                if (j + u < oe) rows[u] = IO::load_raw(table + (uint64_t)W.occ_f[j + u] * dpad, lane);
+                if (j + u < total) rows[u] = IO::load_raw(table + (uint64_t)W.occ_f[j + u] * dpad, lane);
+        }
 #pragma unroll
-            for (int u = 0; u < U; ++u)
-                if (j + u < oe) IO::template fma<A>(acc, (A)W.occ_c[j + u], rows[u]);
+        for (int u = 0; u < U; ++u) {
+            const uint32_t jj = j + u;
+            if (jj < total) {
+                while (jj >= rend) close_role();
+                if (lane_on) IO::template fma<A>(acc, (A)W.occ_c[jj], rows[u]);
+            }
         }
     }
-    return (A)W.role_n[r];
+    while (r < NR) close_role();
 }
 
 template <typename A, int VPL>
@@ -514,6 +540,23 @@ __device__ __forceinline__ A warp_dot(const A (&x)[VPL], const A (&y)[VPL]) {
     return warp_sum<A>(s);
 }
 
+// Two dot products x1.y1 and x2.y2 reduced together (the two shuffle chains
+// interleave).
+template <typename A, int VPL>
+__device__ __forceinline__ void warp_dot2(const A (&x1)[VPL], const A (&y1)[VPL], const A (&x2)[VPL],
+                                          const A (&y2)[VPL], A& d1, A& d2) {
+    A s = 0, t = 0;
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) { s += x1[k] * y1[k]; t += x2[k] * y2[k]; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(FULL, s, o);
+        t += __shfl_xor_sync(FULL, t, o);
+    }
+    d1 = s;
+    d2 = t;
+}
+
 template <typename A, int VPL>
 __device__ __forceinline__ bool warp_all_finite(const A (&x)[VPL]) {
     bool ok = true;
@@ -522,12 +565,15 @@ __device__ __forceinline__ bool warp_all_finite(const A (&x)[VPL]) {
     return __all_sync(FULL, ok);
 }
 
-// STAGED = true: the common path through the per-warp tables; anchors that do
-// not fit are flagged in p.deferred and skipped.  STAGED = false: the direct
-// path, run afterwards for the flagged anchors only (every anchor when
-// p.deferred is null).  Both produce identical items, directions and scales.
+// k_fwd_gather: one warp per anchor; the mean of every role of the anchor
+// (h(v), ~h(v), h(u_1..R)) into its direction row, the role's weight total
+// into scale, and the anchor's gradient items.  STAGED = true: the common path
+// through the per-warp tables; anchors that do not fit are flagged in
+// p.deferred and skipped.  STAGED = false: the direct path, run afterwards for
+// the flagged anchors only (every anchor when p.deferred is null).  Both
+// produce identical items, means and totals.
 template <typename T, typename A, int VPL, bool STAGED>
-__global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 3 : 2) : 1) k_forward(ForwardParams p) {
+__global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 4 : 3) : 1) k_fwd_gather(ForwardParams p) {
     const int lane = threadIdx.x & 31;
     const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t n = p.st->n_anchors;
@@ -535,36 +581,70 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 3 : 2) : 1) k_forwar
     const uint32_t R = p.R, NR = R + 2, dpad = p.dpad;
     const bool lane_on = (uint32_t)(lane * VPL) < dpad;
     const T* __restrict__ table = (const T*)p.table;
-    A* dir = (A*)p.dir;
-    A* scale = (A*)p.scale;
     const uint32_t v = p.anchors[a];
     const bool emit = p.emit && p.st->n_items > 0;
     uint64_t pos = emit ? p.occ_off[a] : 0;
     const uint64_t sbase = (uint64_t)a * NR;
-
-    extern __shared__ __align__(16) unsigned char fwd_smem[];
-    WarpTables& W = reinterpret_cast<WarpTables*>(fwd_smem)[threadIdx.x >> 5];
     const uint32_t cnt = p.nbr_cnt[a];
     if constexpr (STAGED) {
+        extern __shared__ __align__(16) unsigned char fwd_smem[];
+        WarpTables& W = reinterpret_cast<WarpTables*>(fwd_smem)[threadIdx.x >> 5];
         const bool staged = stage_anchor<A>(p, W, a, v, cnt, pos, emit, (uint32_t)sbase, lane);
         if (lane == 0) p.deferred[a] = staged ? 0 : 1;
         if (!staged) return;
+        roles_from_table<T, A, VPL>(p, table, W, NR, sbase, lane, lane_on);
     } else {
         if (p.deferred && !p.deferred[a]) return;
+        A* dir = (A*)p.dir;
+        A* scale = (A*)p.scale;
+        for (uint32_t r = 0; r < NR; ++r) {
+            const uint32_t* nodes = r == 0 ? &v : (r == 1 ? p.nbr + (uint64_t)a * p.Kcap : p.neg + (uint64_t)a * R + (r - 2));
+            const float* w = r == 1 ? p.nbr_w + (uint64_t)a * p.Kcap : nullptr;
+            const uint32_t count = r == 1 ? cnt : 1u;
+            A acc[VPL];
+            const A nr = gather_role<T, A, VPL>(p, table, nodes, w, count, (uint32_t)(sbase + r), pos, emit, acc,
+                                                lane, lane_on);
+            if (lane_on) {
+                const A rn = (A)1 / nr;
+#pragma unroll
+                for (int k = 0; k < VPL; ++k) acc[k] *= rn;
+                store_row<A, VPL, A>(dir + (sbase + r) * dpad, lane, acc);
+            }
+            if (lane == 0) scale[sbase + r] = nr;
+        }
     }
-    // role r of this anchor: from the staged table, or gathered directly (the
-    // direct path emits its items as it goes)
-    auto role_mean = [&](uint32_t r, const uint32_t* nodes, const float* w, uint32_t count, A (&acc)[VPL]) -> A {
-        if constexpr (STAGED) return role_from_table<T, A, VPL>(p, table, W, r, acc, lane, lane_on);
-        else return gather_role<T, A, VPL>(p, table, nodes, w, count, (uint32_t)(sbase + r), pos, emit, acc, lane,
-                                           lane_on);
+}
+
+// k_fwd_loss: one warp per anchor; reads the role means and totals written by
+// k_fwd_gather, evaluates the loss (loss.rs:56-129) and overwrites each role's
+// mean with its gradient direction and its total with its gradient scale.
+template <typename A, int VPL>
+__global__ void __launch_bounds__(128) k_fwd_loss(ForwardParams p) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t n = p.st->n_anchors;
+    if (a >= n) return;
+    const uint32_t R = p.R, NR = R + 2, dpad = p.dpad;
+    const bool lane_on = (uint32_t)(lane * VPL) < dpad;
+    A* dir = (A*)p.dir;
+    A* scale = (A*)p.scale;
+    const uint32_t v = p.anchors[a];
+    const uint64_t sbase = (uint64_t)a * NR;
+    auto load_mean = [&](uint64_t src, A (&x)[VPL]) {
+        if (lane_on) RowIO<A, VPL>::load_cg(dir + src * dpad, lane, x);
+        else {
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) x[k] = 0;
+        }
     };
 
-    A hv[VPL], tv[VPL], u[VPL];
-    const A n_h = role_mean(0, &v, nullptr, 1, hv);
-    const A n_t = role_mean(1, p.nbr + (uint64_t)a * p.Kcap, p.nbr_w + (uint64_t)a * p.Kcap, cnt, tv);
-#pragma unroll
-    for (int k = 0; k < VPL; ++k) { hv[k] /= n_h; tv[k] /= n_t; }
+    A hv[VPL], tv[VPL], u[VPL], un[VPL];
+    load_mean(sbase, hv);
+    load_mean(sbase + 1, tv);
+    if (R) load_mean(sbase + 2, un);
+    // role weight totals: lane i holds role i's (roles beyond 32 read directly)
+    const A n_lane = (uint32_t)lane < NR ? scale[sbase + lane] : (A)0;
+    const A n_h = __shfl_sync(FULL, n_lane, 0), n_t = __shfl_sync(FULL, n_lane, 1);
 
     // loss weighting divisor (mod.rs:190-200)
     A wdiv = 1;
@@ -588,18 +668,22 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 3 : 2) : 1) k_forwar
         na = sqrt(warp_dot<A, VPL>(xa, xa));
         d1 = (A)p.gamma + na;
     } else {
-        nt = sqrt(warp_dot<A, VPL>(tv, tv));
-        nh = sqrt(warp_dot<A, VPL>(hv, hv));
+        A tt_, hh_;
+        warp_dot2<A, VPL>(tv, tv, hv, hv, tt_, hh_);
+        nt = sqrt(tt_);
+        nh = sqrt(hh_);
+        const A rnt = (A)1 / nt, rnh = (A)1 / nh;
 #pragma unroll
-        for (int k = 0; k < VPL; ++k) { xa[k] = tv[k] / nt; xh[k] = hv[k] / nh; }
+        for (int k = 0; k < VPL; ++k) { xa[k] = tv[k] * rnt; xh[k] = hv[k] * rnh; }
         rd = warp_dot<A, VPL>(xa, xh);
     }
 
     for (uint32_t i = 0; i < R; ++i) {
-        const uint32_t src = (uint32_t)(sbase + 2 + i);
-        const A n_u = role_mean(2 + i, p.neg + (uint64_t)a * R + i, nullptr, 1, u);
+        const uint64_t src = sbase + 2 + i;
 #pragma unroll
-        for (int k = 0; k < VPL; ++k) u[k] /= n_u;
+        for (int k = 0; k < VPL; ++k) u[k] = un[k];
+        if (i + 1 < R) load_mean(src + 1, un);      // next negative's mean in flight
+        const A n_u = 2 + i < 32 ? __shfl_sync(FULL, n_lane, 2 + i) : scale[src];
         A d[VPL];
         bool kept;
         if (p.loss == LOSS_MARGIN) {
@@ -611,25 +695,31 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 3 : 2) : 1) k_forwar
             if (kept) {
                 ++P;
                 lsum += li;
+                const A rnb = (A)1 / nb;
 #pragma unroll
-                for (int k = 0; k < VPL; ++k) { d[k] = d[k] / nb; gsum[k] += d[k]; }
+                for (int k = 0; k < VPL; ++k) { d[k] = d[k] * rnb; gsum[k] += d[k]; }
             }
         } else {
-            const A nu = sqrt(warp_dot<A, VPL>(u, u));
+            // |u|^2 and h.u in one reduction: cos(h, u) = (h.u / |u|) / |h|
+            A uu, hu;
+            warp_dot2<A, VPL>(u, u, xh, u, uu, hu);
+            const A nu = sqrt(uu);
+            const A rnu = (A)1 / nu;
 #pragma unroll
-            for (int k = 0; k < VPL; ++k) u[k] /= nu;
-            const A cs = warp_dot<A, VPL>(xh, u);
+            for (int k = 0; k < VPL; ++k) u[k] *= rnu;
+            const A cs = hu * rnu;
             const A li = p.loss == LOSS_STARSPACE ? (A)p.gamma - (rd - cs) : cs - (A)p.neg_margin;
             kept = li > 0;
             if (kept) {
                 ++P;
                 lsum += li;
 #pragma unroll
-                for (int k = 0; k < VPL; ++k) { gsum[k] += u[k]; d[k] = (xh[k] - u[k] * cs) / nu; }
+                for (int k = 0; k < VPL; ++k) { gsum[k] += u[k]; d[k] = (xh[k] - u[k] * cs) * rnu; }
             }
         }
         bool fin = kept ? warp_all_finite<A, VPL>(d) : false;
-        if (kept && lane_on) store_row<A, VPL, A>(dir + (uint64_t)src * dpad, lane, d);
+        if (kept && lane_on) store_row<A, VPL, A>(dir + src * dpad, lane, d);
+        __syncwarp();
         if (lane == 0) {
             p.valid[src] = (uint8_t)(kept && fin);
             scale[src] = kept ? (A)1 / n_u : (A)0;   // finalised below
@@ -655,9 +745,10 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 3 : 2) : 1) k_forwar
     bool reach_t = true;
     if (p.loss == LOSS_MARGIN) {
         const A invP = P ? (A)1 / (A)P : (A)0;
+        const A rna = (A)1 / na;
 #pragma unroll
         for (int k = 0; k < VPL; ++k) {
-            const A ak = xa[k] / na;   // NaN when t == h, dropped by the extraction rule
+            const A ak = xa[k] * rna;   // NaN when t == h, dropped by the extraction rule
             dh[k] = -ak;
             dt[k] = ak - gsum[k] * invP;
         }
@@ -670,12 +761,13 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 3 : 2) : 1) k_forwar
             gtn[k] = -xh[k] * cnt_t * inv;
             ghn[k] = (gsum[k] - xa[k] * cnt_t) * inv;
         }
-        const A st_ = warp_dot<A, VPL>(xa, gtn);
-        const A sh_ = warp_dot<A, VPL>(xh, ghn);
+        A st_, sh_;
+        warp_dot2<A, VPL>(xa, gtn, xh, ghn, st_, sh_);
+        const A rnt = (A)1 / nt, rnh = (A)1 / nh;
 #pragma unroll
         for (int k = 0; k < VPL; ++k) {
-            dt[k] = (gtn[k] - xa[k] * st_) / nt;
-            dh[k] = (ghn[k] - xh[k] * sh_) / nh;
+            dt[k] = (gtn[k] - xa[k] * st_) * rnt;
+            dh[k] = (ghn[k] - xh[k] * sh_) * rnh;
         }
     }
     const bool fin_h = warp_all_finite<A, VPL>(dh);
@@ -869,11 +961,12 @@ static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s) {
     const size_t smem = sizeof(WarpTables) * FWD_WARPS;
     static bool attr = false;   // opt in to > 48 KB of dynamic shared memory once
     if (!attr) {
-        cudaFuncSetAttribute(k_forward<T, A, VPL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_fwd_gather<T, A, VPL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
     }
-    k_forward<T, A, VPL, true><<<blocks, 32 * FWD_WARPS, smem, s>>>(p);
-    k_forward<T, A, VPL, false><<<blocks, 32 * FWD_WARPS, 0, s>>>(p);
+    k_fwd_gather<T, A, VPL, true><<<blocks, 32 * FWD_WARPS, smem, s>>>(p);
+    k_fwd_gather<T, A, VPL, false><<<blocks, 32 * FWD_WARPS, 0, s>>>(p);
+    k_fwd_loss<A, VPL><<<(cap + 3) / 4, 128, 0, s>>>(p);
 }
 
 template <typename T, typename A>

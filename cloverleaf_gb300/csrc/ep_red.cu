@@ -53,13 +53,14 @@ __device__ __forceinline__ void adam_apply(T* __restrict__ table, float* __restr
                                            uint64_t seed, uint32_t step, int lane) {
     const uint64_t o = (uint64_t)f * dpad;
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float rb1 = 1.f / bc1, rb2 = 1.f / bc2;
 #pragma unroll
     for (int k = 0; k < VPL; ++k) {
         const float gk = g[k];
         mm[k] = b1 * mm[k] + (1.f - b1) * gk;
         vv[k] = b2 * vv[k] + (1.f - b2) * (gk * gk);
-        const float mh = mm[k] / bc1;
-        const float vh = vv[k] / bc2;
+        const float mh = mm[k] * rb1;
+        const float vh = vv[k] * rb2;
         ee[k] -= lr * (mh / (sqrtf(vh) + eps));
     }
     RowIO<float, VPL>::store_raw(m + o, lane, mm);
@@ -192,10 +193,7 @@ __device__ __forceinline__ void add_rows(const ReduceParams& p, unsigned mask, u
                 if (i < n) RowIO<A, VPL>::load((const A*)p.dir + (uint64_t)src[i] * p.dpad, lane, r[i]);
 #pragma unroll
             for (int i = 0; i < 4; ++i)
-                if (i < n) {
-#pragma unroll
-                    for (int e = 0; e < VPL; ++e) acc[e] += w[i] * r[i][e];
-                }
+                if (i < n) axpy_slice<A, VPL>(acc, w[i], r[i]);
         }
     }
 }
