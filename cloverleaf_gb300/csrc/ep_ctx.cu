@@ -78,13 +78,16 @@ struct ep_ctx {
 
     // per-batch scratch
     DevBuf st, st_eval, st_inj;
-    DevBuf anchors, nbr, nbr_w, nbr_cnt, neg, occ, dir, scale, valid, loss, status, deferred;
+    DevBuf anchors, nbr, nbr_w, nbr_cnt, neg, occ, dir, dir16, scale, valid, loss, status, deferred;
     DevBuf item_f, item_src, item_c, key_alt, idx, idx_alt, hist;
     DevBuf carry_head, carry_tail, carry_f, carry_flags, long_list, gdense, touched, n_touched, packed, xfer, bound;
     uint64_t items_cap = 0;
     uint32_t buf_B = 0, buf_K = 0, buf_es = 0;
     uint32_t chunk = 128;
-    bool fused_split = true;    // FUSED form: reduce to gradient rows, then a separate Adam kernel
+    // FUSED form's Adam placement: 0 = by the reducing warp as each feature
+    // closes; 1 = gradient rows, then a separate Adam kernel; 2 = queued in
+    // the reducing warp's shared memory and updated four rows at a time
+    int fused_mode = 2;
     bool prepared = false;
     cudaGraphExec_t gexec = nullptr;
     uint32_t* sorted_keys = nullptr;
@@ -203,7 +206,10 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     c->tt = cfg->form == EP_FORM_FUSED_BF16 ? TT_BF16 : TT_F32;
     c->R = cfg->negatives;
     c->NR = c->R + 2;
-    if (const char* fs = getenv("EP_FUSED_SPLIT")) c->fused_split = atoi(fs) != 0;   // (tuning)
+    if (const char* fm = getenv("EP_FUSED_MODE")) {   // (tuning)
+        const int v = atoi(fm);
+        if (v >= 0 && v <= 2) c->fused_mode = v;
+    }
     if (const char* ch = getenv("EP_REDUCE_CHUNK")) {   // reducer items per warp (tuning)
         const long v = atol(ch);
         if (v >= 32 && v <= (1l << 20)) c->chunk = (uint32_t)v;
@@ -361,7 +367,9 @@ static int ensure_bufs(ep_ctx* c, uint32_t B, uint32_t K, uint64_t items, uint32
         const uint32_t nch = reduce_chunks(items, c->chunk);
         bool ok = c->anchors.ensure((size_t)B * 4) && c->nbr.ensure((size_t)B * K * 4) && c->nbr_w.ensure((size_t)B * K * 4) &&
                   c->nbr_cnt.ensure((size_t)B * 4) && c->neg.ensure((size_t)B * c->R * 4) && c->occ.ensure(((size_t)B + 1) * 4) &&
-                  c->dir.ensure((size_t)B * NR * c->dpad * es) && c->scale.ensure((size_t)B * NR * es) &&
+                  c->dir.ensure((size_t)B * NR * c->dpad * es) &&
+                  (c->tt != TT_BF16 || c->dir16.ensure((size_t)B * NR * c->dpad * 2)) &&
+                  c->scale.ensure((size_t)B * NR * es) &&
                   c->valid.ensure((size_t)B * NR) && c->loss.ensure((size_t)B * es) && c->status.ensure((size_t)B * 4) &&
                   c->deferred.ensure((size_t)B) &&
                   c->item_f.ensure(items * 4) && c->item_src.ensure(items * 4) && c->item_c.ensure(items * 4) &&
@@ -425,7 +433,7 @@ static int prepare_train(ep_ctx* c) {
     uint64_t items = 0;
     for (uint32_t i = 0; i < top; ++i) items += hb[i];
     if (items > 0xfffffff0ull) return c->fail(EP_ERR_UNSUPPORTED, "a batch can emit more than 2^32 gradient items");
-    int rc = ensure_bufs(c, B, K, items, 4, c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_split);
+    int rc = ensure_bufs(c, B, K, items, 4, c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_mode == 1);
     if (rc) return rc;
     c->Bcap = B;
     c->Kcap = c->buf_K;
@@ -491,6 +499,7 @@ static ForwardParams forward_params(ep_ctx* c, BatchState* st, const void* table
     fp.emit = emit;
     fp.items_cap = c->items_cap;
     fp.dir = c->dir.p;
+    fp.dir16 = c->dir16.p;
     fp.scale = c->scale.p;
     fp.valid = c->valid.as<uint8_t>();
     fp.loss_out = c->loss.p;
@@ -513,6 +522,7 @@ static ReduceParams reduce_params(ep_ctx* c, BatchState* st, int out_mode, void*
     rp.skey = c->sorted_keys;
     rp.sval = c->sorted_vals;
     rp.dir = c->dir.p;
+    rp.dir16 = c->dir16.p;
     rp.scale = c->scale.p;
     rp.valid = c->valid.as<uint8_t>();
     rp.table = table;
@@ -547,7 +557,7 @@ static uint32_t kernels_per_batch(const ep_ctx* c) {
     const uint32_t radix = 3 * (b ? (b + 7) / 8 : 1);
     return 3 /* begin, sample, scan */ + 3 /* forward: staged, direct gather; loss */ + radix +
            3 /* reduce, fixup x2 */ +
-           (c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_split ? 1 : 0) + 1 /* end */;
+           (c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_mode == 1 ? 1 : 0) + 1 /* end */;
 }
 
 // Issues one training batch on the context stream; ev (optional) receives an
@@ -567,9 +577,9 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr) {
                       c->item_c.as<float>(), c->idx.as<uint2>(), c->idx_alt.as<uint2>(), c->hist.as<uint32_t>(),
                       c->items_cap, (int)bits_for(c->n_feat), &c->sorted_keys, &c->sorted_vals, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_SORT], s);
-    const bool plain = c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_split;
+    const bool plain = c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_mode == 1;
     if (plain) cudaMemsetAsync(c->n_touched.p, 0, 4, s);
-    ReduceParams rp = reduce_params(c, st, plain ? OUT_DENSE : OUT_ADAM, c->table.p);
+    ReduceParams rp = reduce_params(c, st, plain ? OUT_DENSE : (c->fused_mode == 2 ? OUT_QUEUE : OUT_ADAM), c->table.p);
     launch_reduce(c->tt, (int)c->vpl, rp, c->items_cap, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_REDUCE], s);
     launch_fixup(c->tt, (int)c->vpl, rp, c->items_cap, s);

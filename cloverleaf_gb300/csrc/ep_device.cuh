@@ -146,6 +146,16 @@ struct RowIO {
 #pragma unroll
         for (int k = 0; k < VPL; ++k) out[k] = cvt_in<A, T>(u.t[k]);
     }
+    // Plain load through a generic pointer (shared or global memory).
+    template <typename A>
+    static __device__ __forceinline__ void load_generic(const T* row, int lane, A (&out)[VPL]) {
+        union { V v[NV]; T t[VPL]; } u;
+        const V* src = reinterpret_cast<const V*>(row + lane * VPL);
+#pragma unroll
+        for (int i = 0; i < NV; ++i) u.v[i] = src[i];
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) out[k] = cvt_in<A, T>(u.t[k]);
+    }
     // Raw row slice kept in its storage type while loads are in flight.
     struct Raw { V v[NV]; };
     // number of raw slices that fit in about 32 registers
@@ -181,6 +191,11 @@ template <typename T> struct FromA;
 template <> struct FromA<float> {
     template <typename A> static __device__ __forceinline__ float cvt(A x) { return (float)x; }
 };
+template <> struct FromA<__nv_bfloat16> {
+    template <typename A> static __device__ __forceinline__ __nv_bfloat16 cvt(A x) {
+        return __float2bfloat16_rn((float)x);
+    }
+};
 template <> struct FromA<double> {
     template <typename A> static __device__ __forceinline__ double cvt(A x) { return (double)x; }
 };
@@ -193,6 +208,11 @@ __device__ __forceinline__ void store_row(T* row, int lane, const A (&in)[VPL]) 
     for (int k = 0; k < VPL; ++k) t[k] = FromA<T>::cvt(in[k]);
     RowIO<T, VPL>::store_raw(row, lane, t);
 }
+
+// Storage type of the per-role gradient directions: BF16 next to a BF16
+// table (accumulated in FP32 by the reducer), else the accumulation type.
+template <typename T, typename A> struct DirOf { using type = A; };
+template <> struct DirOf<__nv_bfloat16, float> { using type = __nv_bfloat16; };
 
 // FP32 -> BF16 with stochastic rounding: adds uniform 16-bit noise below the
 // BF16 mantissa before truncation, so E[bf16(x)] = x and small Adam updates

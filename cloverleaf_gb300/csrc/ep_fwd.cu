@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <type_traits>
+
 #include "ep_device.cuh"
 #include "ep_internal.h"
 
@@ -618,8 +620,9 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 4 : 3) : 1) k_fwd_ga
 // k_fwd_loss: one warp per anchor; reads the role means and totals written by
 // k_fwd_gather, evaluates the loss (loss.rs:56-129) and overwrites each role's
 // mean with its gradient direction and its total with its gradient scale.
-template <typename A, int VPL>
+template <typename T, typename A, int VPL>
 __global__ void __launch_bounds__(128) k_fwd_loss(ForwardParams p) {
+    using D = typename DirOf<T, A>::type;
     const int lane = threadIdx.x & 31;
     const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t n = p.st->n_anchors;
@@ -627,6 +630,7 @@ __global__ void __launch_bounds__(128) k_fwd_loss(ForwardParams p) {
     const uint32_t R = p.R, NR = R + 2, dpad = p.dpad;
     const bool lane_on = (uint32_t)(lane * VPL) < dpad;
     A* dir = (A*)p.dir;
+    D* dout = std::is_same<D, A>::value ? (D*)p.dir : (D*)p.dir16;
     A* scale = (A*)p.scale;
     const uint32_t v = p.anchors[a];
     const uint64_t sbase = (uint64_t)a * NR;
@@ -718,7 +722,7 @@ __global__ void __launch_bounds__(128) k_fwd_loss(ForwardParams p) {
             }
         }
         bool fin = kept ? warp_all_finite<A, VPL>(d) : false;
-        if (kept && lane_on) store_row<A, VPL, A>(dir + src * dpad, lane, d);
+        if (kept && lane_on) store_row<D, VPL, A>(dout + src * dpad, lane, d);
         __syncwarp();
         if (lane == 0) {
             p.valid[src] = (uint8_t)(kept && fin);
@@ -773,8 +777,8 @@ __global__ void __launch_bounds__(128) k_fwd_loss(ForwardParams p) {
     const bool fin_h = warp_all_finite<A, VPL>(dh);
     const bool fin_t = warp_all_finite<A, VPL>(dt);
     if (lane_on) {
-        store_row<A, VPL, A>(dir + sbase * dpad, lane, dh);
-        store_row<A, VPL, A>(dir + (sbase + 1) * dpad, lane, dt);
+        store_row<D, VPL, A>(dout + sbase * dpad, lane, dh);
+        store_row<D, VPL, A>(dout + (sbase + 1) * dpad, lane, dt);
     }
     if (lane == 0) {
         p.valid[sbase] = (uint8_t)(ok && fin_h);
@@ -966,7 +970,7 @@ static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s) {
     }
     k_fwd_gather<T, A, VPL, true><<<blocks, 32 * FWD_WARPS, smem, s>>>(p);
     k_fwd_gather<T, A, VPL, false><<<blocks, 32 * FWD_WARPS, 0, s>>>(p);
-    k_fwd_loss<A, VPL><<<(cap + 3) / 4, 128, 0, s>>>(p);
+    k_fwd_loss<T, A, VPL><<<(cap + 3) / 4, 128, 0, s>>>(p);
 }
 
 template <typename T, typename A>

@@ -30,7 +30,11 @@ enum : uint32_t {
     ERR_NBR_OVERFLOW = 1u << 2,     // sampled neighbours exceeded capacity
 };
 
-enum OutMode : int { OUT_ADAM = 0, OUT_DENSE = 1 };
+// OUT_ADAM: each finished feature row is updated in place by the warp that
+// finished it.  OUT_DENSE: rows go to a dense gradient buffer plus a touched
+// list (a separate Adam kernel, or the caller, consumes them).  OUT_QUEUE:
+// rows are queued in the warp's shared memory and updated four at a time.
+enum OutMode : int { OUT_ADAM = 0, OUT_DENSE = 1, OUT_QUEUE = 2 };
 enum TableType : int { TT_F32 = 0, TT_BF16 = 1, TT_F64 = 2 };
 
 struct BatchState {
@@ -114,7 +118,8 @@ struct ForwardParams {
     uint64_t items_cap;
     uint8_t* deferred;        // [n_anchors]: 1 = anchor left to the direct path
     // outputs
-    void* dir;              // A[n_anchors * NR * dpad]
+    void* dir;              // A[n_anchors * NR * dpad]: role means, then (D == A) directions
+    void* dir16;            // BF16 tables: directions as BF16 (D = bf16)
     void* scale;            // A[n_anchors * NR]
     uint8_t* valid;         // [n_anchors * NR]
     void* loss_out;         // A[n_anchors]
@@ -131,7 +136,8 @@ struct ReduceParams {
     int out_mode;           // OutMode
     const uint32_t* skey;   // sorted feature ids
     const uint2* sval;      // (role-src, count-weight bits) of each sorted item
-    const void* dir;        // A
+    const void* dir;        // directions when D == A
+    const void* dir16;      // directions when D == bf16 (BF16 tables)
     const void* scale;      // A
     const uint8_t* valid;
     // OUT_ADAM

@@ -122,11 +122,144 @@ __device__ __forceinline__ void fin_flush(const ReduceParams& p, uint32_t* fin, 
     n_fin = 0;
 }
 
+// OUT_QUEUE: a per-warp ring of QN slots in shared memory.  Queuing a
+// finished feature row stores its gradient in the slot and starts
+// asynchronous copies (cp.async) of the lane's slices of the feature's m, v
+// and table rows into the slot; the copies of QN - 1 later rows are still in
+// flight when the oldest slot is updated, so the update reads everything from
+// shared memory and rarely waits.  Each lane copies and later reads only its
+// own slices, so the per-thread cp.async groups order everything it needs.
+constexpr uint32_t QN = 3;
+constexpr int QUEUE_THREADS = 128;
+
+template <typename T>
+__host__ __device__ constexpr size_t queue_slot_bytes(uint32_t dpad) {
+    return ((size_t)dpad * (3 * sizeof(float) + sizeof(T)) + 15) & ~(size_t)15;
+}
+
+struct WarpQueue {
+    unsigned char* base;   // QN slots: g, m, v (float[dpad] each), table row (T[dpad])
+    uint32_t* f;           // feature of each slot
+    size_t sb;             // slot bytes
+    uint32_t head, n;
+};
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Asynchronous copy of one lane slice of B bytes (B a multiple of 16, or 8 or 4).
+template <int B>
+__device__ __forceinline__ void cp_slice(void* dst, const void* src) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    if constexpr (B % 16 == 0) {
+#pragma unroll
+        for (int i = 0; i < B / 16; ++i)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + 16 * i),
+                         "l"(reinterpret_cast<const char*>(src) + 16 * i)
+                         : "memory");
+    } else {
+        static_assert(B == 8 || B == 4, "cp.async copies 4, 8 or 16 bytes");
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(src), "n"(B) : "memory");
+    }
+}
+
+// Slices of at least 4 bytes for every row go through cp.async; narrower
+// rows (dims <= 64 with a BF16 table) are read synchronously at the update.
+template <typename T, int VPL>
+struct QueueAsync {
+    static constexpr bool value = VPL * sizeof(T) >= 4 && VPL * sizeof(float) >= 4 && sizeof(T) != 8;
+};
+
+template <typename T, int VPL>
+__device__ __forceinline__ void queue_slot_ptrs(const WarpQueue& q, uint32_t slot, uint32_t dpad, float*& g, float*& m,
+                                                float*& v, T*& t) {
+    g = reinterpret_cast<float*>(q.base + slot * q.sb);
+    m = g + dpad;
+    v = m + dpad;
+    t = reinterpret_cast<T*>(v + dpad);
+}
+
+// Adam on the oldest slot (optimizer.rs:43-81).  The caller has waited for
+// that slot's copies.
+template <typename T, int VPL>
+__device__ __forceinline__ void queue_pop(const ReduceParams& p, WarpQueue& q, int lane, bool lane_on, float lr,
+                                          float bc1, float bc2, uint32_t step) {
+    if constexpr (sizeof(T) != 8) {
+        const uint32_t dpad = p.dpad;
+        float *gs, *ms, *vs;
+        T* ts;
+        queue_slot_ptrs<T, VPL>(q, q.head, dpad, gs, ms, vs, ts);
+        const uint32_t f = q.f[q.head];
+        if (lane_on) {
+            float gg[VPL], mm[VPL], vv[VPL], ee[VPL];
+            RowIO<float, VPL>::load_generic(gs, lane, gg);
+            if constexpr (QueueAsync<T, VPL>::value) {
+                RowIO<float, VPL>::load_generic(ms, lane, mm);
+                RowIO<float, VPL>::load_generic(vs, lane, vv);
+                RowIO<T, VPL>::load_generic(ts, lane, ee);
+            } else {
+                const uint64_t o = (uint64_t)f * dpad;
+                RowIO<float, VPL>::load_cg(p.m + o, lane, mm);
+                RowIO<float, VPL>::load_cg(p.v + o, lane, vv);
+                RowIO<T, VPL>::load_cg((const T*)p.table + o, lane, ee);
+            }
+            adam_apply<T, VPL>((T*)p.table, p.m, p.v, f, dpad, gg, mm, vv, ee, lr, bc1, bc2, p.seed, step, lane);
+        }
+    }
+    q.head = q.head + 1 == QN ? 0u : q.head + 1;
+    --q.n;
+}
+
+// Queues a finished (NaN-free) row; updates the oldest slot first when full.
+template <typename T, typename A, int VPL>
+__device__ __forceinline__ void queue_push(const ReduceParams& p, WarpQueue& q, uint32_t f, const A (&acc)[VPL], int lane,
+                                           bool lane_on, float lr, float bc1, float bc2, uint32_t step) {
+    if (q.n == QN) {
+        cp_async_wait<QN - 1>();
+        __syncwarp();
+        queue_pop<T, VPL>(p, q, lane, lane_on, lr, bc1, bc2, step);
+    }
+    uint32_t slot = q.head + q.n;
+    if (slot >= QN) slot -= QN;
+    float *gs, *ms, *vs;
+    T* ts;
+    const uint32_t dpad = p.dpad;
+    queue_slot_ptrs<T, VPL>(q, slot, dpad, gs, ms, vs, ts);
+    if (lane_on) {
+        store_row<float, VPL, A>(gs, lane, acc);
+        if constexpr (QueueAsync<T, VPL>::value) {
+            const uint64_t o = (uint64_t)f * dpad + (uint64_t)lane * VPL;
+            cp_slice<VPL * 4>(ms + lane * VPL, p.m + o);
+            cp_slice<VPL * 4>(vs + lane * VPL, p.v + o);
+            cp_slice<VPL * (int)sizeof(T)>(ts + lane * VPL, (const T*)p.table + o);
+        }
+    }
+    cp_async_commit();
+    if (lane == 0) q.f[slot] = f;
+    ++q.n;
+}
+
+// Updates every queued slot (end of the warp's work).
+template <typename T, int VPL>
+__device__ __forceinline__ void queue_flush(const ReduceParams& p, WarpQueue& q, int lane, bool lane_on, float lr,
+                                            float bc1, float bc2, uint32_t step) {
+    cp_async_wait<0>();
+    __syncwarp();
+    while (q.n) queue_pop<T, VPL>(p, q, lane, lane_on, lr, bc1, bc2, step);
+}
+
 template <typename T, typename A, int VPL, int MODE>
 __device__ __forceinline__ void finish_row(const ReduceParams& p, uint32_t f, const A (&acc)[VPL], int lane,
                                            bool lane_on, float lr, float bc1, float bc2, uint32_t step,
-                                           uint32_t* fin, uint32_t& n_fin) {
-    if constexpr (MODE == OUT_DENSE) {
+                                           uint32_t* fin, uint32_t& n_fin, WarpQueue* q = nullptr) {
+    if constexpr (MODE == OUT_QUEUE) {
+        // rows containing NaN get no Adam step (optimizer.rs:56): not queued
+        bool bad = false;
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) bad = bad || (acc[k] != acc[k]);
+        if (!__any_sync(FULL, bad)) queue_push<T, A, VPL>(p, *q, f, acc, lane, lane_on, lr, bc1, bc2, step);
+    } else if constexpr (MODE == OUT_DENSE) {
         if (lane_on) store_row<A, VPL, A>((A*)p.gdense + (uint64_t)f * p.dpad, lane, acc);
         if (fin) {
             if (lane == 0) fin[n_fin] = f;
@@ -168,49 +301,36 @@ __device__ __forceinline__ void prefetch_segment_state(const ReduceParams& p, ui
     }
 }
 
-// Accumulates into acc the rows of the kept items whose lanes are set in
-// `mask` (lane j holds src[j] and the item's coefficient w[j] = c * scale),
-// four rows in flight at a time, in increasing lane order.
-template <typename A, int VPL>
-__device__ __forceinline__ void add_rows(const ReduceParams& p, unsigned mask, uint32_t src_l, A w_l, A (&acc)[VPL],
-                                         int lane, bool lane_on) {
-    while (mask) {
-        uint32_t src[4];
-        A w[4];
-        int n = 0;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int j = mask ? __ffs(mask) - 1 : 0;
-            const bool have = mask != 0;
-            src[i] = __shfl_sync(FULL, src_l, j);
-            w[i] = __shfl_sync(FULL, w_l, j);
-            if (have) { mask &= mask - 1; n = i + 1; }
-        }
-        if (lane_on) {
-            A r[4][VPL];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-                if (i < n) RowIO<A, VPL>::load((const A*)p.dir + (uint64_t)src[i] * p.dpad, lane, r[i]);
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-                if (i < n) axpy_slice<A, VPL>(acc, w[i], r[i]);
-        }
-    }
-}
-
 // k_reduce: one warp per chunk of C sorted items, 32 items (one per lane) at a
 // time.  Per batch the first-occurrence rule is evaluated for all 32 items at
 // once with ballots: group starts (new feature or new anchor), valid roles,
 // and for every item the first valid role of its (feature, anchor) group,
-// carried across batches and, at a chunk start, found by walking back.  Then
-// the warp walks the feature segments of the batch, adding the kept items'
-// rows in item order and finishing each feature as its segment closes.
+// carried across batches and, at a chunk start, found by walking back.  The
+// kept items' direction rows are then streamed in item order, several in
+// flight across feature boundaries; a feature is finished when the stream
+// passes the start of the next one.  Item metadata is software-pipelined:
+// while batch b is reduced, the role flags and scales of batch b+1 and the
+// keys of batch b+2 are in flight.
 template <typename T, typename A, int VPL, int MODE>
-__global__ void __launch_bounds__(RED_THREADS, VPL >= 16 ? 1 : (MODE == OUT_DENSE ? 3 : 2)) k_reduce(ReduceParams p) {
-    __shared__ uint32_t fin_all[RED_THREADS / 32][FIN_CAP];
+__global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREADS,
+                                  VPL >= 16 ? 1 : (MODE == OUT_DENSE ? 3 : (MODE == OUT_QUEUE ? 4 : 2)))
+    k_reduce(ReduceParams p) {
+    using D = typename DirOf<T, A>::type;
+    using IO = RowIO<D, VPL>;
+    // rows in flight: about 24-32 registers of raw data in the rows-only mode,
+    // fewer where a finished row is updated in place while others are in flight
+    constexpr int NF = MODE == OUT_DENSE ? (sizeof(D) == 2 ? 4 : 3) : 2;
+    __shared__ uint32_t fin_all[MODE == OUT_DENSE ? RED_THREADS / 32 : 1][FIN_CAP];
+    extern __shared__ __align__(16) unsigned char red_queue[];   // OUT_QUEUE: [warps][QN] slots, then ids
     const int lane = threadIdx.x & 31;
-    uint32_t* fin = fin_all[threadIdx.x >> 5];
+    uint32_t* fin = fin_all[MODE == OUT_DENSE ? (threadIdx.x >> 5) : 0];
     uint32_t n_fin = 0;
+    WarpQueue q;
+    q.sb = queue_slot_bytes<T>(p.dpad);
+    q.base = red_queue + (size_t)(threadIdx.x >> 5) * QN * q.sb;
+    q.f = reinterpret_cast<uint32_t*>(red_queue + (size_t)(blockDim.x >> 5) * QN * q.sb) + (threadIdx.x >> 5) * QN;
+    q.head = 0;
+    q.n = 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) p.st->n_long = 0;   // read by k_fixup / k_fixup_long
     const unsigned lt_mask = (1u << lane) - 1u;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -222,6 +342,8 @@ __global__ void __launch_bounds__(RED_THREADS, VPL >= 16 ? 1 : (MODE == OUT_DENS
     const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
     const float lr = p.st->lr, bc1 = p.st->bc1, bc2 = p.st->bc2;
     const uint32_t step = (uint32_t)p.st->step;
+    const D* dir = std::is_same<D, A>::value ? (const D*)p.dir : (const D*)p.dir16;
+    const A* scale = (const A*)p.scale;
     unsigned long long g_cnt = 0, u_cnt = 0;
     for (uint32_t c = gw; c < nchunks; c += nw) {
         const uint32_t i0 = c * C, i1 = min(i0 + C, M);
@@ -264,22 +386,56 @@ __global__ void __launch_bounds__(RED_THREADS, VPL >= 16 ? 1 : (MODE == OUT_DENS
         bool any_kept = false;
         uint32_t flags = 0;
         if constexpr (MODE == OUT_ADAM) prefetch_segment_state<T>(p, i0, i1, lane);
+
+        // metadata pipeline: (f0, s0, c0, v0, sc0) for the current batch,
+        // (f1, s1, c1) for the next one; v1/sc1 are loaded one batch ahead
+        uint32_t f0 = NONE, s0 = 0, f1 = NONE, s1 = 0;
+        float c0 = 0.f, c1 = 0.f;
+        bool v0 = false;
+        A sc0 = 0;
+        {
+            const uint32_t i = i0 + lane;
+            if (i < i1) {
+                f0 = p.skey[i];
+                const uint2 sv = p.sval[i];
+                s0 = sv.x;
+                c0 = __uint_as_float(sv.y);
+            }
+            const uint32_t j = i0 + 32 + lane;
+            if (j < i1) {
+                f1 = p.skey[j];
+                const uint2 sv = p.sval[j];
+                s1 = sv.x;
+                c1 = __uint_as_float(sv.y);
+            }
+            if (i < i1) {
+                v0 = p.valid[s0] != 0;
+                sc0 = scale[s0];
+            }
+        }
         for (uint32_t ib = i0; ib < i1; ib += 32) {
             const uint32_t i = ib + lane;
             const bool act = i < i1;
-            uint32_t f = NONE, s = 0;
-            float cf = 0.f;
-            A w = 0;
-            bool v = false;
-            if (act) {
-                f = p.skey[i];
-                const uint2 sv = p.sval[i];
-                s = sv.x;
-                cf = __uint_as_float(sv.y);
-                v = p.valid[s] != 0;
+            const uint32_t f = f0, s = s0;
+            const float cf = c0;
+            const bool v = v0;
+            const A sc = sc0;
+            // next batch's role flags and scales; the batch after's keys
+            bool v1 = false;
+            A sc1 = 0;
+            uint32_t f2 = NONE, s2 = 0;
+            float c2 = 0.f;
+            if (ib + 32 + lane < i1) {
+                v1 = p.valid[s1] != 0;
+                sc1 = scale[s1];
             }
-            // look ahead: warm L2 with the Adam state of features starting in the
-            // next batch, so their updates do not wait for DRAM
+            if (ib + 64 + lane < i1) {
+                const uint32_t j = ib + 64 + lane;
+                f2 = p.skey[j];
+                const uint2 sv = p.sval[j];
+                s2 = sv.x;
+                c2 = __uint_as_float(sv.y);
+            }
             if constexpr (MODE == OUT_ADAM) prefetch_segment_state<T>(p, ib + 32, i1, lane);
             const uint32_t anchor = s / NR;
             // predecessor of each lane (lane 0: the carried item before the batch)
@@ -308,51 +464,77 @@ __global__ void __launch_bounds__(RED_THREADS, VPL >= 16 ? 1 : (MODE == OUT_DENS
                 else if (vg) ch = src_fv;
                 keep = act && v && s == ch;
                 // carry the group state of the batch's last item
-                const int last = 31 - __clz(__ballot_sync(FULL, act));
-                chosen = __shfl_sync(FULL, ch, last);
+                const int lastl = 31 - __clz(__ballot_sync(FULL, act));
+                chosen = __shfl_sync(FULL, ch, lastl);
             }
-            if (keep) w = (A)cf * ((const A*)p.scale)[s];
-            const unsigned K = __ballot_sync(FULL, keep);
-            const unsigned ACT = __ballot_sync(FULL, act);
-            const int last = 31 - __clz(ACT);
-            // walk the segments of this batch
+            const A w = keep ? (A)cf * sc : (A)0;
+            unsigned pend = __ballot_sync(FULL, keep);
             unsigned starts = SS;
-            int lo = 0;
-            while (lo <= last) {
-                // the segment containing lane lo runs to the next start after lo
-                const unsigned later = starts & ~((2u << lo) - 1u) & ((lo == 31) ? 0u : FULL);
-                const int hi = later ? __ffs(later) - 1 : last + 1;
-                if ((SS >> lo) & 1u) {
-                    // a new segment starts at lo: close the current one first
-                    if (started_here) {
-                        if (any_kept) {
-                            finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step, fin, n_fin);
-                            ++u_cnt;
-                        }
-                    } else {
-                        if (lane_on) store_row<A, VPL, A>((A*)p.carry_head + (uint64_t)c * p.dpad, lane, acc);
-                        flags |= CF_HEAD | (any_kept ? CF_HEAD_KEPT : 0u);
+            const int last = 31 - __clz(__ballot_sync(FULL, act));
+
+            // closes the open feature (finished here, or a head partial for
+            // the fix-up) and opens the one starting at lane lo
+            auto close_open = [&](int lo) {
+                if (started_here) {
+                    if (any_kept) {
+                        finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step, fin, n_fin, &q);
+                        ++u_cnt;
                     }
-#pragma unroll
-                    for (int k = 0; k < VPL; ++k) acc[k] = 0;
-                    started_here = true;
-                    any_kept = false;
-                    cur_f = __shfl_sync(FULL, f, lo);
+                } else {
+                    if (lane_on) store_row<A, VPL, A>((A*)p.carry_head + (uint64_t)c * p.dpad, lane, acc);
+                    flags |= CF_HEAD | (any_kept ? CF_HEAD_KEPT : 0u);
                 }
-                const unsigned rng = (hi >= 32 ? FULL : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
-                const unsigned km = K & rng;
-                any_kept = any_kept || km != 0;
-                add_rows<A, VPL>(p, km, s, w, acc, lane, lane_on);
-                lo = hi;
+#pragma unroll
+                for (int k = 0; k < VPL; ++k) acc[k] = 0;
+                started_here = true;
+                any_kept = false;
+                cur_f = __shfl_sync(FULL, f, lo);
+            };
+            while (pend) {
+                uint32_t src[NF];
+                A wv[NF];
+                int ln[NF];
+                int n = 0;
+#pragma unroll
+                for (int u = 0; u < NF; ++u) {
+                    const int j = pend ? __ffs(pend) - 1 : 0;
+                    ln[u] = pend ? j : 32;
+                    src[u] = __shfl_sync(FULL, s, j);
+                    wv[u] = __shfl_sync(FULL, w, j);
+                    if (pend) { pend &= pend - 1; n = u + 1; }
+                }
+                typename IO::Raw r[NF];
+                if (lane_on) {
+#pragma unroll
+                    for (int u = 0; u < NF; ++u)
+                        if (u < n) r[u] = IO::load_raw(dir + (uint64_t)src[u] * p.dpad, lane);
+                }
+#pragma unroll
+                for (int u = 0; u < NF; ++u) {
+                    if (u < n) {
+                        while (starts && __ffs(starts) - 1 <= ln[u]) {
+                            close_open(__ffs(starts) - 1);
+                            starts &= starts - 1;
+                        }
+                        if (lane_on) IO::template fma<A>(acc, wv[u], r[u]);
+                        any_kept = true;
+                    }
+                }
+            }
+            while (starts) {
+                close_open(__ffs(starts) - 1);
+                starts &= starts - 1;
             }
             prev_f = __shfl_sync(FULL, f, last);
             prev_anchor = __shfl_sync(FULL, anchor, last);
             prev_src = __shfl_sync(FULL, s, last);
+            f0 = f1; s0 = s1; c0 = c1; v0 = v1; sc0 = sc1;
+            f1 = f2; s1 = s2; c1 = c2;
         }
         const bool cont = i1 < M && p.skey[i1] == cur_f;
         if (started_here && !cont) {
             if (any_kept) {
-                finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step, fin, n_fin);
+                finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step, fin, n_fin, &q);
                 ++u_cnt;
             }
         } else if (!started_here) {
@@ -366,6 +548,7 @@ __global__ void __launch_bounds__(RED_THREADS, VPL >= 16 ? 1 : (MODE == OUT_DENS
         if (lane == 0) p.carry_flags[c] = flags;
     }
     if constexpr (MODE == OUT_DENSE) fin_flush(p, fin, n_fin, lane);
+    if constexpr (MODE == OUT_QUEUE) queue_flush<T, VPL>(p, q, lane, lane_on, lr, bc1, bc2, step);
     g_cnt = warp_sum<unsigned long long>(g_cnt);
     if (lane == 0) {
         if (g_cnt) atomicAdd(&p.st->gathered, g_cnt);
@@ -582,6 +765,11 @@ __global__ void __launch_bounds__(RED_THREADS) k_adam_dense(BatchState* st, T* t
     }
 }
 
+template <typename T>
+static size_t queue_smem(uint32_t dpad) {
+    return (size_t)(QUEUE_THREADS / 32) * QN * (queue_slot_bytes<T>(dpad) + sizeof(uint32_t));
+}
+
 template <typename T, typename A, int VPL>
 static void red_launch(const ReduceParams& p, uint64_t cap, cudaStream_t s, int which) {
     const uint32_t nch = reduce_chunks(cap, p.chunk);
@@ -590,6 +778,11 @@ static void red_launch(const ReduceParams& p, uint64_t cap, cudaStream_t s, int 
         uint32_t ctas = (warps + RED_THREADS / 32 - 1) / (RED_THREADS / 32);
         if (ctas > RED_MAX_CTAS) ctas = RED_MAX_CTAS;
         if (p.out_mode == OUT_DENSE) k_reduce<T, A, VPL, OUT_DENSE><<<ctas, RED_THREADS, 0, s>>>(p);
+        else if (p.out_mode == OUT_QUEUE) {
+            uint32_t qctas = (warps + QUEUE_THREADS / 32 - 1) / (QUEUE_THREADS / 32);
+            if (qctas > 2 * RED_MAX_CTAS) qctas = 2 * RED_MAX_CTAS;
+            k_reduce<T, A, VPL, OUT_QUEUE><<<qctas, QUEUE_THREADS, queue_smem<T>(p.dpad), s>>>(p);
+        }
         else k_reduce<T, A, VPL, OUT_ADAM><<<ctas, RED_THREADS, 0, s>>>(p);
     } else {
         uint32_t ctas = std::min<uint32_t>((warps + FIX_THREADS / 32 - 1) / (FIX_THREADS / 32), 152 * 16);
@@ -612,6 +805,9 @@ static cudaError_t fixl_setup() {
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_fixup_long<T, A, VPL, OUT_ADAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_reduce<T, A, VPL, OUT_QUEUE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)queue_smem<T>(VPL * 32));
     return e;
 }
 

@@ -3,8 +3,10 @@
 Per-batch checks use explicit samples (the reference's trajectory is
 nondeterministic, so parity is per batch from a frozen table).  Tolerances:
 FP32 loss and gradient within 1e-4 relative (max |diff| / max |oracle|) of
-the FP64 oracle; the BF16 form is compared on the BF16-rounded table, so the
-same 1e-4 bound applies to its FP32 accumulation.
+the FP64 oracle.  The BF16 form is compared on the BF16-rounded table: its
+loss (FP32 arithmetic) within the same 1e-4; its gradient within 1e-2,
+because that form stores each role's gradient direction in BF16 (relative
+rounding 2^-9 per element) before the FP32 per-feature sums.
 """
 import numpy as np
 import pytest
@@ -15,6 +17,7 @@ from tests._cases import dense_from_sparse, random_problem, rel_err, sample_batc
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-4
+TOL_GRAD_BF16 = 1e-2
 
 
 def make_ctx(prob, *, loss=1, gamma=0.5, R=4, form=0, grad_mode=0, weighting=0, lw_exp=0.5, neg_margin=0.1,
@@ -47,7 +50,7 @@ def gpu_batch(ctx, prob, smp, dims=None):
     return ctx.batch_grad(s, prob["n_feat"], dims or prob["dims"])
 
 
-def check_parity(oracle, prob, smp, ctx, table, **kw):
+def check_parity(oracle, prob, smp, ctx, table, grad_tol=TOL, **kw):
     ol, ost, og, ot = oracle_batch(oracle, prob, smp, table, **kw)
     gl, gst, ids, rows = gpu_batch(ctx, prob, smp)
     assert (gst == ost).all(), (gst, ost)
@@ -56,7 +59,7 @@ def check_parity(oracle, prob, smp, ctx, table, **kw):
     g, t = dense_from_sparse(ids, rows, prob["n_feat"], prob["dims"])
     assert (t == ot).all(), np.nonzero(t != ot)
     assert np.isfinite(rows).all()
-    assert rel_err(g, og) < TOL, rel_err(g, og)
+    assert rel_err(g, og) < grad_tol, rel_err(g, og)
     return ids, rows
 
 
@@ -128,7 +131,7 @@ def test_batch_grad_fused_bf16(oracle):
     ctx = make_ctx(prob, loss=1, gamma=0.5, form=1)
     table_bf16 = ctx.get_table(prob["n_feat"], prob["dims"])     # BF16-rounded values
     assert not np.array_equal(table_bf16, prob["table"])
-    check_parity(oracle, prob, smp, ctx, table_bf16, loss=1, gamma=0.5)
+    check_parity(oracle, prob, smp, ctx, table_bf16, grad_tol=TOL_GRAD_BF16, loss=1, gamma=0.5)
 
 
 def test_batch_grad_deterministic(oracle):
