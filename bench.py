@@ -173,6 +173,15 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
+def fused_mode():
+    """Adam placement of the fused form (the library default is 2: Adam in the
+    reducer through a per-warp queue; 1: a separate Adam kernel)."""
+    try:
+        return int(os.environ.get("EP_FUSED_MODE", "2"))
+    except ValueError:
+        return 2
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -301,22 +310,35 @@ def main():
     B = pst["batches"] or 1
     d, s_el = ep["dims"], 2.0
     G, U, S, A = pst["gathered_rows"] / B, pst["unique_rows"] / B, pst["sampled_neighbors"] / B, pst["anchors"] / B
+    items = pst["items"] / B
+    # Algorithmic HBM bytes per launch of each stage's kernels (per batch):
+    #   forward  gathered table rows G*d*s, their feature ids 4G, sampled
+    #            neighbour ids 4S, per-role scale/valid 8*B*(R+2)
+    #   reduce   sorted item keys and values 12*items, plus (Adam in the
+    #            reducer) U*d*(2s+16): m, v read+written (FP32), table row
+    #            read+written; (Adam split off) the U*d*4 gradient rows
+    #   adam     (split form only) gradient rows + Adam state U*d*(2s+20)
+    split = fused_mode() == 1
     stage_bytes = {"forward": G * d * s_el + 4 * G + 4 * S + 8 * A * (ep["negatives"] + 2),
-                   "reduce": U * d * (2 * s_el + 16)}
+                   "reduce": 12 * items + (U * d * 4 if split else U * d * (2 * s_el + 16)),
+                   "adam": U * d * (2 * s_el + 20) if split else 0.0}
+    kernel_of = {"forward": "k_fwd_gather+k_fwd_loss", "adam": "k_adam_dense",
+                 "reduce": "k_reduce (gradient rows)" if split else "k_reduce (Adam fused, cp.async queue)"}
     dom = max(stage_ms, key=stage_ms.get)
     peak, peak_kind = load_peaks()
-    rf_stage = "forward" if stage_ms["forward"] >= stage_ms["reduce"] else "reduce"
+    rf_stage = max(("forward", "reduce", "adam"), key=lambda k: stage_ms[k])
     achieved = stage_bytes[rf_stage] / (stage_ms[rf_stage] / 1e3) / 1e9
     step_bytes = pst["alg_bytes"] / B
     step_ms = st["ms"] / max(st["batches"], 1)
-    roofline = {"bound": "hbm", "kernel": {"forward": "k_forward", "reduce": "k_reduce+k_fixup"}[rf_stage],
+    roofline = {"bound": "hbm", "kernel": kernel_of[rf_stage],
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)",
                 "traffic": load_traffic(args.workload), "alg_bytes_per_launch": stage_bytes[rf_stage],
                 "stage_ms": stage_ms, "dominant_stage": dom,
+                "stage_gbs": {k: stage_bytes[k] / (stage_ms[k] / 1e3) / 1e9 for k in stage_bytes if stage_bytes[k]},
                 "step": {"achieved": step_bytes / (step_ms / 1e3) / 1e9, "alg_bytes_per_step": step_bytes,
                          "frac": step_bytes / (step_ms / 1e3) / 1e9 / peak},
-                "per_batch": {"G": G, "U": U, "S": S, "items": pst["items"] / B}}
+                "per_batch": {"G": G, "U": U, "S": S, "items": items}}
     log(f"[bench] stages (ms/batch): " + ", ".join(f"{k} {v:.3f}" for k, v in stage_ms.items()))
 
     # --- plain FP32 ---

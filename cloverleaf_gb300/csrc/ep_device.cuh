@@ -53,6 +53,16 @@ __host__ __device__ __forceinline__ uint32_t rand_u32(uint64_t seed, uint32_t a,
     switch (i & 3u) { case 0: return r.x; case 1: return r.y; case 2: return r.z; default: return r.w; }
 }
 
+// 32-bit finalizer of MurmurHash3 (Appleby): a bijective avalanche mix.
+__host__ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x85ebca6bu;
+    x ^= x >> 13;
+    x *= 0xc2b2ae35u;
+    x ^= x >> 16;
+    return x;
+}
+
 // Uniform integer in [0, n) by multiply-high (bias < n / 2^32).
 __host__ __device__ __forceinline__ uint32_t below(uint32_t r, uint32_t n) {
     return (uint32_t)(((uint64_t)r * (uint64_t)n) >> 32);

@@ -28,17 +28,12 @@ enum { LW_NONE = 0, LW_LOG = 1, LW_EXP = 2 };
 // to [0, n) by cycle walking.  Replaces the host shuffle of mod.rs:173 with an
 // O(1)-per-position permutation that needs no buffer and no sort.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t fmix32(uint32_t x) {
-    x ^= x >> 16; x *= 0x85ebca6bu; x ^= x >> 13; x *= 0xc2b2ae35u; x ^= x >> 16;
-    return x;
-}
-
 __device__ __forceinline__ uint32_t feistel(uint32_t x, uint32_t h, const uint32_t* k) {
     const uint32_t mask = h >= 32 ? 0xffffffffu : ((1u << h) - 1u);
     uint32_t L = (h >= 32) ? 0 : (x >> h), Rr = x & mask;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        uint32_t F = fmix32(Rr ^ k[r]) & mask;
+        uint32_t F = mix32(Rr ^ k[r]) & mask;
         uint32_t nL = Rr;
         Rr = L ^ F;
         L = nL;
@@ -232,22 +227,29 @@ __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
 }
 
 // ---------------------------------------------------------------------------
-// k_scan_occ: exclusive scan of the per-anchor item counts (one CTA).
+// k_scan_occ: exclusive scan of the per-anchor item counts (one CTA).  Each
+// thread scans 8 consecutive counts in registers, so a batch of up to 8192
+// anchors is one sweep: loads, a block scan of the thread totals, stores.
 // ---------------------------------------------------------------------------
+constexpr int SCAN_PER_THREAD = 8;
+
 __global__ void __launch_bounds__(1024) k_scan_occ(BatchState* st, uint32_t* occ, uint64_t items_cap) {
     __shared__ unsigned long long warp_tot[32];
-    __shared__ unsigned long long carry;
     const uint32_t n = st->n_anchors;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    if (tid == 0) carry = 0;
-    __syncthreads();
-    for (uint32_t base = 0; base < n; base += 1024) {
-        uint32_t i = base + tid;
-        unsigned long long x = i < n ? occ[i] : 0;
-        unsigned long long incl = x;
+    unsigned long long carry = 0;
+    for (uint32_t base = 0; base < n; base += 1024 * SCAN_PER_THREAD) {
+        const uint32_t i0 = base + (uint32_t)tid * SCAN_PER_THREAD;
+        uint32_t x[SCAN_PER_THREAD];
+#pragma unroll
+        for (int k = 0; k < SCAN_PER_THREAD; ++k) x[k] = i0 + k < n ? occ[i0 + k] : 0u;
+        unsigned long long tsum = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_PER_THREAD; ++k) tsum += x[k];
+        unsigned long long incl = tsum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            unsigned long long t = __shfl_up_sync(FULL, incl, o);
+            const unsigned long long t = __shfl_up_sync(FULL, incl, o);
             if (lane >= o) incl += t;
         }
         if (lane == 31) warp_tot[w] = incl;
@@ -256,16 +258,19 @@ __global__ void __launch_bounds__(1024) k_scan_occ(BatchState* st, uint32_t* occ
             unsigned long long s = warp_tot[lane];
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                unsigned long long t = __shfl_up_sync(FULL, s, o);
+                const unsigned long long t = __shfl_up_sync(FULL, s, o);
                 if (lane >= o) s += t;
             }
             warp_tot[lane] = s;
         }
         __syncthreads();
-        unsigned long long excl = carry + (w ? warp_tot[w - 1] : 0) + incl - x;
-        if (i < n) occ[i] = (uint32_t)min(excl, (unsigned long long)0xffffffffu);
-        __syncthreads();
-        if (tid == 1023) carry = excl + x;
+        unsigned long long run = carry + (w ? warp_tot[w - 1] : 0ull) + incl - tsum;
+#pragma unroll
+        for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+            if (i0 + k < n) occ[i0 + k] = (uint32_t)min(run, 0xffffffffull);
+            run += x[k];
+        }
+        carry += warp_tot[31];
         __syncthreads();
     }
     if (tid == 0) {
@@ -810,13 +815,29 @@ __global__ void __launch_bounds__(1024) k_batch_end(BatchState* st, const A* los
     const uint32_t n = st->n_anchors;
     double sum = 0;
     unsigned long long cnt = 0, nan = 0, smp = 0;
-    for (uint32_t i = tid; i < n; i += 1024) {
-        const int s = status[i];
-        const double l = (double)loss[i];
-        if (eval) sum += l;
-        else if (s == 0) { sum += l; ++cnt; }
-        nan += (s == 2);
-        smp += nbr_cnt[i];
+    // eight anchors per thread, all loads issued before the sums
+    constexpr int PT = 8;
+    for (uint32_t base = 0; base < n; base += 1024 * PT) {
+        int sv[PT];
+        A lv[PT];
+        uint32_t cv[PT];
+#pragma unroll
+        for (int k = 0; k < PT; ++k) {
+            const uint32_t i = base + (uint32_t)k * 1024 + tid;
+            const bool in = i < n;
+            sv[k] = in ? status[i] : 3;
+            lv[k] = in ? loss[i] : (A)0;
+            cv[k] = in ? nbr_cnt[i] : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < PT; ++k) {
+            if (sv[k] == 3) continue;
+            const double l = (double)lv[k];
+            if (eval) sum += l;
+            else if (sv[k] == 0) { sum += l; ++cnt; }
+            nan += (sv[k] == 2);
+            smp += cv[k];
+        }
     }
     sum = warp_sum<double>(sum);
     cnt = warp_sum<unsigned long long>(cnt);

@@ -61,25 +61,24 @@ __device__ __forceinline__ void adam_apply(T* __restrict__ table, float* __restr
         vv[k] = b2 * vv[k] + (1.f - b2) * (gk * gk);
         const float mh = mm[k] * rb1;
         const float vh = vv[k] * rb2;
-        ee[k] -= lr * (mh / (sqrtf(vh) + eps));
+        // the denominator is >= eps = 1e-8, inside __fdividef's full-accuracy range
+        ee[k] -= lr * __fdividef(mh, sqrtf(vh) + eps);
     }
     RowIO<float, VPL>::store_raw(m + o, lane, mm);
     RowIO<float, VPL>::store_raw(v + o, lane, vv);
     if constexpr (std::is_same<T, float>::value) {
         RowIO<float, VPL>::store_raw(table + o, lane, ee);
     } else {
-        // BF16 table: stochastic rounding, 16 random bits per element from
-        // one Philox block per 8 elements.
+        // BF16 table: stochastic rounding, 16 random bits per element; one
+        // 32-bit hash (murmur3 finalizer of the element pair's coordinates
+        // row, step, column) per pair of elements.
         __nv_bfloat16 out[VPL];
+        const uint32_t key = (uint32_t)seed ^ (uint32_t)(seed >> 32) ^ (f * 0x9E3779B1u) ^ (step * 0x85EBCA77u);
 #pragma unroll
-        for (int k0 = 0; k0 < VPL; k0 += 8) {
-            const u32x4 r = philox(u32x4{f, step, (ST_ROUND << 24) | (uint32_t)lane, (uint32_t)k0}, seed);
-            const uint32_t w[4] = {r.x, r.y, r.z, r.w};
-#pragma unroll
-            for (int k = k0; k < k0 + 8 && k < VPL; ++k) {
-                const uint32_t bits = (k & 1) ? (w[(k - k0) >> 1] >> 16) : (w[(k - k0) >> 1] & 0xffffu);
-                out[k] = bf16_stochastic(ee[k], bits);
-            }
+        for (int k = 0; k < VPL; k += 2) {
+            const uint32_t h = mix32(key ^ ((uint32_t)(lane * VPL + k) * 0xC2B2AE3Du));
+            out[k] = bf16_stochastic(ee[k], h & 0xffffu);
+            if (k + 1 < VPL) out[k + 1] = bf16_stochastic(ee[k + 1], h >> 16);
         }
         RowIO<__nv_bfloat16, VPL>::store_raw(table + o, lane, out);
     }
