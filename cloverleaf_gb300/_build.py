@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libep_gb300.so")
 
 CU_SOURCES = ("ep_fwd.cu", "ep_sort.cu", "ep_red.cu", "ep_ctx.cu")
 CPP_SOURCES = ("ep_host.cpp",)
-HEADERS = ("ep_internal.h", "ep_device.cuh")
+HEADERS = ("ep_internal.h", "ep_device.cuh", "ep_launch.cuh")
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = ["-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE]

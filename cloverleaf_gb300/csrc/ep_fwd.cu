@@ -16,6 +16,7 @@
 
 #include "ep_device.cuh"
 #include "ep_internal.h"
+#include "ep_launch.cuh"
 
 namespace ep {
 
@@ -57,6 +58,8 @@ __device__ __forceinline__ uint32_t permute(uint32_t pos, uint32_t n, uint32_t h
 // ---------------------------------------------------------------------------
 __global__ void k_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, uint64_t total,
                               uint64_t warmup, float alpha, int injected) {
+    pdl_wait();
+    pdl_trigger();
     if (threadIdx.x != 0) return;
     if (!injected) {
         uint32_t b0 = st->batch * cap;
@@ -85,6 +88,8 @@ __global__ void k_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, ui
 // k_sample: one warp per anchor.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     BatchState* st = p.st;
@@ -234,6 +239,8 @@ __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
 constexpr int SCAN_PER_THREAD = 8;
 
 __global__ void __launch_bounds__(1024) k_scan_occ(BatchState* st, uint32_t* occ, uint64_t items_cap) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ unsigned long long warp_tot[32];
     const uint32_t n = st->n_anchors;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -581,6 +588,8 @@ __device__ __forceinline__ bool warp_all_finite(const A (&x)[VPL]) {
 // produce identical items, means and totals.
 template <typename T, typename A, int VPL, bool STAGED>
 __global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 4 : 3) : 1) k_fwd_gather(ForwardParams p) {
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t n = p.st->n_anchors;
@@ -628,6 +637,8 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 4 : 3) : 1) k_fwd_ga
 template <typename T, typename A, int VPL>
 __global__ void __launch_bounds__(128) k_fwd_loss(ForwardParams p) {
     using D = typename DirOf<T, A>::type;
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t n = p.st->n_anchors;
@@ -809,6 +820,8 @@ __global__ void __launch_bounds__(128) k_fwd_loss(ForwardParams p) {
 template <typename A>
 __global__ void __launch_bounds__(1024) k_batch_end(BatchState* st, const A* loss, const int32_t* status,
                                                     const uint32_t* nbr_cnt, uint32_t steps_per_pass, int eval) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double s_sum[32];
     __shared__ unsigned long long s_cnt[32], s_nan[32], s_smp[32];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -967,17 +980,17 @@ void launch_split(uint32_t* train, uint32_t n_train, uint32_t* valid, uint32_t n
 void launch_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, uint32_t steps_per_pass,
                         uint64_t total, uint64_t warmup, float alpha, int injected, cudaStream_t s) {
     (void)steps_per_pass;
-    k_batch_begin<<<1, 32, 0, s>>>(st, n_order, cap, total, warmup, alpha, injected);
+    launch_chain(k_batch_begin, 1, 32, 0, s, st, n_order, cap, total, warmup, alpha, injected);
 }
 
 void launch_sample(const SampleParams& p, cudaStream_t s) {
     const uint32_t blocks = (p.batch_cap + 7) / 8;
-    k_sample<<<blocks, 256, 0, s>>>(p);
+    launch_chain(k_sample, blocks, 256, 0, s, p);
 }
 
 void launch_scan_occ(BatchState* st, uint32_t* occ, uint32_t cap, uint64_t items_cap, cudaStream_t s) {
     (void)cap;
-    k_scan_occ<<<1, 1024, 0, s>>>(st, occ, items_cap);
+    launch_chain(k_scan_occ, 1, 1024, 0, s, st, occ, items_cap);
 }
 
 template <typename T, typename A, int VPL>
@@ -989,9 +1002,9 @@ static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s) {
         cudaFuncSetAttribute(k_fwd_gather<T, A, VPL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
     }
-    k_fwd_gather<T, A, VPL, true><<<blocks, 32 * FWD_WARPS, smem, s>>>(p);
-    k_fwd_gather<T, A, VPL, false><<<blocks, 32 * FWD_WARPS, 0, s>>>(p);
-    k_fwd_loss<T, A, VPL><<<(cap + 3) / 4, 128, 0, s>>>(p);
+    launch_chain(k_fwd_gather<T, A, VPL, true>, blocks, 32 * FWD_WARPS, smem, s, p);
+    launch_chain(k_fwd_gather<T, A, VPL, false>, blocks, 32 * FWD_WARPS, 0, s, p);
+    launch_chain(k_fwd_loss<T, A, VPL>, (cap + 3) / 4, 128, 0, s, p);
 }
 
 template <typename T, typename A>
@@ -1014,8 +1027,8 @@ void launch_forward(int tt, int vpl, const ForwardParams& p, uint32_t cap, cudaS
 void launch_batch_end(BatchState* st, const void* loss, const int32_t* status, const uint32_t* nbr_cnt,
                       uint32_t cap, uint32_t steps_per_pass, int eval, int loss_f64, cudaStream_t s) {
     (void)cap;
-    if (loss_f64) k_batch_end<double><<<1, 1024, 0, s>>>(st, (const double*)loss, status, nbr_cnt, steps_per_pass, eval);
-    else k_batch_end<float><<<1, 1024, 0, s>>>(st, (const float*)loss, status, nbr_cnt, steps_per_pass, eval);
+    if (loss_f64) launch_chain(k_batch_end<double>, 1, 1024, 0, s, st, (const double*)loss, status, nbr_cnt, steps_per_pass, eval);
+    else launch_chain(k_batch_end<float>, 1, 1024, 0, s, st, (const float*)loss, status, nbr_cnt, steps_per_pass, eval);
 }
 
 void launch_init_table(int tt, void* table, uint64_t n_feat, uint32_t dims, uint32_t dpad, uint64_t seed,

@@ -27,6 +27,7 @@
 
 #include "ep_device.cuh"
 #include "ep_internal.h"
+#include "ep_launch.cuh"
 
 namespace ep {
 
@@ -314,6 +315,8 @@ template <typename T, typename A, int VPL, int MODE>
 __global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREADS,
                                   VPL >= 16 ? 1 : (MODE == OUT_DENSE ? 3 : (MODE == OUT_QUEUE ? 4 : 2)))
     k_reduce(ReduceParams p) {
+    pdl_wait();
+    pdl_trigger();
     using D = typename DirOf<T, A>::type;
     using IO = RowIO<D, VPL>;
     // rows in flight: about 24-32 registers of raw data in the rows-only mode,
@@ -585,6 +588,8 @@ __host__ __device__ constexpr int fixl_threads(int vpl) { return vpl >= 16 ? 256
 
 template <typename T, typename A, int VPL, int MODE>
 __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -646,6 +651,8 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
 // independent of timing and of the queue order.
 template <typename T, typename A, int VPL, int MODE>
 __global__ void __launch_bounds__(fixl_threads(VPL)) k_fixup_long(ReduceParams p) {
+    pdl_wait();
+    pdl_trigger();
     constexpr int NWARP = fixl_threads(VPL) / 32;
     extern __shared__ __align__(16) unsigned char fixl_smem[];
     A* wsum = reinterpret_cast<A*>(fixl_smem);          // [NWARP][dpad]
@@ -724,6 +731,8 @@ template <typename T, int VPL>
 __global__ void __launch_bounds__(RED_THREADS) k_adam_dense(BatchState* st, T* table, float* m, float* v,
                                                             const float* g, const uint32_t* touched,
                                                             const uint32_t* n_touched, uint32_t dpad, uint64_t seed) {
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -776,23 +785,23 @@ static void red_launch(const ReduceParams& p, uint64_t cap, cudaStream_t s, int 
     if (which == 0) {
         uint32_t ctas = (warps + RED_THREADS / 32 - 1) / (RED_THREADS / 32);
         if (ctas > RED_MAX_CTAS) ctas = RED_MAX_CTAS;
-        if (p.out_mode == OUT_DENSE) k_reduce<T, A, VPL, OUT_DENSE><<<ctas, RED_THREADS, 0, s>>>(p);
+        if (p.out_mode == OUT_DENSE) launch_chain(k_reduce<T, A, VPL, OUT_DENSE>, ctas, RED_THREADS, 0, s, p);
         else if (p.out_mode == OUT_QUEUE) {
             uint32_t qctas = (warps + QUEUE_THREADS / 32 - 1) / (QUEUE_THREADS / 32);
             if (qctas > 2 * RED_MAX_CTAS) qctas = 2 * RED_MAX_CTAS;
-            k_reduce<T, A, VPL, OUT_QUEUE><<<qctas, QUEUE_THREADS, queue_smem<T>(p.dpad), s>>>(p);
+            launch_chain(k_reduce<T, A, VPL, OUT_QUEUE>, qctas, QUEUE_THREADS, queue_smem<T>(p.dpad), s, p);
         }
-        else k_reduce<T, A, VPL, OUT_ADAM><<<ctas, RED_THREADS, 0, s>>>(p);
+        else launch_chain(k_reduce<T, A, VPL, OUT_ADAM>, ctas, RED_THREADS, 0, s, p);
     } else {
         uint32_t ctas = std::min<uint32_t>((warps + FIX_THREADS / 32 - 1) / (FIX_THREADS / 32), 152 * 16);
         constexpr int LT = fixl_threads(VPL);
         const size_t lsmem = (size_t)(LT / 32) * p.dpad * sizeof(A);
         if (p.out_mode == OUT_DENSE) {
-            k_fixup<T, A, VPL, OUT_DENSE><<<ctas, FIX_THREADS, 0, s>>>(p);
-            k_fixup_long<T, A, VPL, OUT_DENSE><<<152, LT, lsmem, s>>>(p);
+            launch_chain(k_fixup<T, A, VPL, OUT_DENSE>, ctas, FIX_THREADS, 0, s, p);
+            launch_chain(k_fixup_long<T, A, VPL, OUT_DENSE>, 152, LT, lsmem, s, p);
         } else {
-            k_fixup<T, A, VPL, OUT_ADAM><<<ctas, FIX_THREADS, 0, s>>>(p);
-            k_fixup_long<T, A, VPL, OUT_ADAM><<<152, LT, lsmem, s>>>(p);
+            launch_chain(k_fixup<T, A, VPL, OUT_ADAM>, ctas, FIX_THREADS, 0, s, p);
+            launch_chain(k_fixup_long<T, A, VPL, OUT_ADAM>, 152, LT, lsmem, s, p);
         }
     }
 }
@@ -862,11 +871,11 @@ static void adam_dispatch(int vpl, BatchState* st, T* table, float* m, float* v,
     if (ctas > RED_MAX_CTAS) ctas = RED_MAX_CTAS;
     if (ctas == 0) ctas = 1;
     switch (vpl) {
-        case 1: k_adam_dense<T, 1><<<ctas, RED_THREADS, 0, s>>>(st, table, m, v, g, touched, n_touched, dpad, seed); break;
-        case 2: k_adam_dense<T, 2><<<ctas, RED_THREADS, 0, s>>>(st, table, m, v, g, touched, n_touched, dpad, seed); break;
-        case 4: k_adam_dense<T, 4><<<ctas, RED_THREADS, 0, s>>>(st, table, m, v, g, touched, n_touched, dpad, seed); break;
-        case 8: k_adam_dense<T, 8><<<ctas, RED_THREADS, 0, s>>>(st, table, m, v, g, touched, n_touched, dpad, seed); break;
-        default: k_adam_dense<T, 16><<<ctas, RED_THREADS, 0, s>>>(st, table, m, v, g, touched, n_touched, dpad, seed); break;
+        case 1: launch_chain(k_adam_dense<T, 1>, ctas, RED_THREADS, 0, s, st, table, m, v, g, touched, n_touched, dpad, seed); break;
+        case 2: launch_chain(k_adam_dense<T, 2>, ctas, RED_THREADS, 0, s, st, table, m, v, g, touched, n_touched, dpad, seed); break;
+        case 4: launch_chain(k_adam_dense<T, 4>, ctas, RED_THREADS, 0, s, st, table, m, v, g, touched, n_touched, dpad, seed); break;
+        case 8: launch_chain(k_adam_dense<T, 8>, ctas, RED_THREADS, 0, s, st, table, m, v, g, touched, n_touched, dpad, seed); break;
+        default: launch_chain(k_adam_dense<T, 16>, ctas, RED_THREADS, 0, s, st, table, m, v, g, touched, n_touched, dpad, seed); break;
     }
 }
 

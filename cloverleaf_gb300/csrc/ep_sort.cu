@@ -21,6 +21,7 @@
 
 #include "ep_device.cuh"
 #include "ep_internal.h"
+#include "ep_launch.cuh"
 
 namespace ep {
 
@@ -36,6 +37,8 @@ size_t radix_hist_entries(uint64_t cap) {
 
 __global__ void __launch_bounds__(SORT_THREADS) k_radix_hist(const uint32_t* __restrict__ keys, const BatchState* st,
                                                              int shift, uint32_t* __restrict__ hist) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ uint32_t h[256];
     const uint32_t n = st->n_items;
     const uint32_t ntiles = (n + SORT_TILE - 1) / SORT_TILE;
@@ -55,6 +58,8 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_hist(const uint32_t* __r
 // One warp per digit: exclusive scan of hist[d * ntiles .. + ntiles) and the
 // digit's total in dtot[d].
 __global__ void __launch_bounds__(256) k_radix_colscan(const BatchState* st, uint32_t* hist, uint32_t* dtot) {
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const uint32_t d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (d >= 256) return;
@@ -81,6 +86,8 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(const uint32_t* 
                                                                 const BatchState* st, int shift,
                                                                 const uint32_t* __restrict__ hist,
                                                                 const uint32_t* __restrict__ dtot) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ uint32_t wcount[SORT_THREADS / 32][256];
     __shared__ uint32_t dbase[256];
     __shared__ uint32_t wtot[SORT_THREADS / 32];
@@ -167,9 +174,10 @@ void launch_radix_sort(BatchState* st, uint32_t* keys, uint32_t* keys_alt, const
         uint32_t* kout = K[(p + 1) & 1];
         vin = p == 0 ? nullptr : V[(p - 1) & 1];
         uint2* vout = V[p & 1];
-        k_radix_hist<<<grid, SORT_THREADS, 0, s>>>(kin, st, shift, hist);
-        k_radix_colscan<<<32, 256, 0, s>>>(st, hist, dtot);
-        k_radix_scatter<<<grid, SORT_THREADS, 0, s>>>(kin, vin, item_src, item_c, kout, vout, st, shift, hist, dtot);
+        launch_chain(k_radix_hist, grid, SORT_THREADS, 0, s, (const uint32_t*)kin, (const BatchState*)st, shift, hist);
+        launch_chain(k_radix_colscan, 32, 256, 0, s, (const BatchState*)st, hist, dtot);
+        launch_chain(k_radix_scatter, grid, SORT_THREADS, 0, s, (const uint32_t*)kin, (const uint2*)vin, item_src, item_c,
+                     kout, vout, (const BatchState*)st, shift, (const uint32_t*)hist, (const uint32_t*)dtot);
         kin = kout;
         vin = vout;
     }
