@@ -138,6 +138,7 @@ SIGNATURES = {
     "ep_batch_step": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), _F32, _U32]),
     "ep_get_table": (ctypes.c_int, [_P, _P]),
     "ep_get_table_static": (ctypes.c_int, [_P, _U64, _U64, _P]),
+    "ep_get_tuning": (ctypes.c_int, [_P, _P, _P, _P]),
     "ep_ag_forward": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), ctypes.c_int, _P, _P, _P]),
     "ep_ag_backward": (ctypes.c_int, [_P, _P, _P, _P]),
     "ep_synchronize": (ctypes.c_int, [_P]),
@@ -231,6 +232,14 @@ class Context:
     def set_table(self, table=None):
         t = None if table is None else np.ascontiguousarray(table, np.float32)
         check(lib().ep_set_table(self._h, ptr(t)), self._h, "ep_set_table")
+
+    def tuning(self):
+        """(tuned, chunk, fused_mode, graph_batches) of this context."""
+        ch, fm, gb = ctypes.c_uint32(), ctypes.c_int32(), ctypes.c_uint32()
+        rc = lib().ep_get_tuning(self._h, ctypes.byref(ch), ctypes.byref(fm), ctypes.byref(gb))
+        if rc < 0:
+            check(rc, self._h, "ep_get_tuning")
+        return rc == 0, ch.value, fm.value, gb.value
 
     def get_table(self, n_feat, dims):
         out = np.empty((n_feat, dims), np.float32)

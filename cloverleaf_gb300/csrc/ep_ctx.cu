@@ -88,8 +88,11 @@ struct ep_ctx {
     // closes; 1 = gradient rows, then a separate Adam kernel; 2 = queued in
     // the reducing warp's shared memory and updated four rows at a time
     int fused_mode = 2;
+    bool tuned = false;         // autotuner has chosen chunk / fused_mode
     bool prepared = false;
     cudaGraphExec_t gexec = nullptr;
+    cudaGraphExec_t gexec_run = nullptr;   // graph_batches consecutive batches
+    uint32_t graph_batches = 16;
     uint32_t* sorted_keys = nullptr;
     uint2* sorted_vals = nullptr;
     BatchState* h_st = nullptr;   // pinned mirror
@@ -107,6 +110,7 @@ struct ep_ctx {
 
     ~ep_ctx() {
         if (gexec) cudaGraphExecDestroy(gexec);
+        if (gexec_run) cudaGraphExecDestroy(gexec_run);
         if (h_st) cudaFreeHost(h_st);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -127,6 +131,7 @@ struct ep_ctx {
     }
     void drop_graph() {
         if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        if (gexec_run) { cudaGraphExecDestroy(gexec_run); gexec_run = nullptr; }
     }
 };
 
@@ -206,6 +211,10 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     c->tt = cfg->form == EP_FORM_FUSED_BF16 ? TT_BF16 : TT_F32;
     c->R = cfg->negatives;
     c->NR = c->R + 2;
+    if (const char* gb = getenv("EP_GRAPH_BATCHES")) {   // batches per replayed graph (tuning)
+        const long v = atol(gb);
+        if (v >= 1 && v <= 1024) c->graph_batches = (uint32_t)v;
+    }
     if (const char* fm = getenv("EP_FUSED_MODE")) {   // (tuning)
         const int v = atoi(fm);
         if (v >= 0 && v <= 2) c->fused_mode = v;
@@ -400,6 +409,11 @@ static uint32_t feistel_half(uint64_t n) {
     return (b + 1) / 2 ? (b + 1) / 2 : 1;
 }
 
+// Autotuner candidates: reducer chunk sizes (items per warp) and, for the
+// FUSED form, the Adam placement (2: queued in the reducer, 1: split off).
+constexpr uint32_t kTuneChunks[3] = {64, 128, 256};
+constexpr uint32_t kTuneWarm = 2, kTuneTimed = 8;
+
 static int prepare_train(ep_ctx* c) {
     if (!c->graph_ok || !c->feats_ok) return c->fail(EP_ERR_STATE, "upload the graph and the features first");
     if (!c->table_ok) return c->fail(EP_ERR_STATE, "set the table first");
@@ -433,7 +447,12 @@ static int prepare_train(ep_ctx* c) {
     uint64_t items = 0;
     for (uint32_t i = 0; i < top; ++i) items += hb[i];
     if (items > 0xfffffff0ull) return c->fail(EP_ERR_UNSUPPORTED, "a batch can emit more than 2^32 gradient items");
-    int rc = ensure_bufs(c, B, K, items, 4, c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_mode == 1);
+    // with the autotuner, size the reducer carries for its smallest chunk and
+    // keep the dense gradient buffers for the split Adam placement
+    const uint32_t chunk = c->chunk;
+    if (c->cfg.autotune) c->chunk = std::min<uint32_t>(c->chunk, kTuneChunks[0]);
+    int rc = ensure_bufs(c, B, K, items, 4, c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_mode == 1 || c->cfg.autotune);
+    c->chunk = chunk;
     if (rc) return rc;
     c->Bcap = B;
     c->Kcap = c->buf_K;
@@ -594,6 +613,97 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr) {
     c->launches += kernels_per_batch(c);
 }
 
+static void advance_host_batch(ep_ctx* c) {
+    if (++c->host_batch >= c->steps_per_pass) { c->host_batch = 0; ++c->host_pass; }
+}
+
+static int launch_train_batch(ep_ctx* c);
+
+// Issues n consecutive training batches.  With graphs, runs of graph_batches
+// batches replay one graph holding that many copies of the batch (the
+// device-resident BatchState moves each copy to the next batch, crossing pass
+// boundaries as the device would); the remainder replays the one-batch graph.
+// The autotuner (config.autotune): times kTuneTimed batches after kTuneWarm
+// warm-up batches under each candidate launch shape and keeps the fastest.
+// The batches it runs are ordinary training batches of the pass (they update
+// the table); it runs once per context, when at least all candidates' batches
+// are requested in one call.  Chosen values: ep_get_tuning.
+static int autotune(ep_ctx* c, uint32_t& n) {
+    struct Cand { uint32_t chunk; int mode; };
+    Cand cands[6];
+    int nc = 0;
+    const bool fused = c->cfg.form == EP_FORM_FUSED_BF16;
+    for (uint32_t ch : kTuneChunks) {
+        cands[nc++] = {ch, fused ? 2 : c->fused_mode};
+        if (fused) cands[nc++] = {ch, 1};
+    }
+    const uint32_t need = (uint32_t)nc * (kTuneWarm + kTuneTimed);
+    if (n < need) return EP_OK;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "tuning events");
+    CK(cudaEventCreate(&e1), "tuning events");
+    float best = 0.f;
+    Cand pick = {c->chunk, c->fused_mode};
+    int rc = EP_OK;
+    for (int i = 0; i < nc && !rc; ++i) {
+        c->chunk = cands[i].chunk;
+        c->fused_mode = cands[i].mode;
+        c->drop_graph();
+        for (uint32_t b = 0; b < kTuneWarm && !rc; ++b) rc = launch_train_batch(c);
+        cudaEventRecord(e0, c->stream);
+        for (uint32_t b = 0; b < kTuneTimed && !rc; ++b) rc = launch_train_batch(c);
+        cudaEventRecord(e1, c->stream);
+        if (rc) break;
+        if (cudaEventSynchronize(e1) != cudaSuccess) { rc = c->cuda_fail(cudaGetLastError(), "tuning"); break; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (i == 0 || ms < best) { best = ms; pick = cands[i]; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    n -= need;
+    c->chunk = pick.chunk;
+    c->fused_mode = pick.mode;
+    c->drop_graph();
+    c->tuned = true;
+    return EP_OK;
+}
+
+static int launch_train_run(ep_ctx* c, uint32_t n) {
+    if (c->cfg.autotune && !c->tuned) {
+        int rc = autotune(c, n);
+        if (rc) return rc;
+    }
+    const bool use_graph = c->cfg.use_graphs && c->cfg.form == EP_FORM_FUSED_BF16;
+    const uint32_t k = c->graph_batches;
+    while (n) {
+        if (use_graph && k > 1 && n >= k) {
+            if (!c->gexec_run) {
+                cudaGraph_t g = nullptr;
+                CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+                const uint64_t before = c->launches;
+                for (uint32_t i = 0; i < k; ++i) issue_train_batch(c);
+                c->launches = before;
+                cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+                if (e != cudaSuccess) return c->cuda_fail(e, "graph capture");
+                e = cudaGraphInstantiate(&c->gexec_run, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) { c->gexec_run = nullptr; return c->cuda_fail(e, "graph instantiate"); }
+            }
+            CK(cudaGraphLaunch(c->gexec_run, c->stream), "graph launch");
+            c->launches += (uint64_t)k * kernels_per_batch(c);
+            for (uint32_t i = 0; i < k; ++i) advance_host_batch(c);
+            n -= k;
+        } else {
+            int rc = launch_train_batch(c);
+            if (rc) return rc;
+            --n;
+        }
+    }
+    return EP_OK;
+}
+
 static int launch_train_batch(ep_ctx* c) {
     const bool use_graph = c->cfg.use_graphs && c->cfg.form == EP_FORM_FUSED_BF16;
     if (use_graph) {
@@ -615,7 +725,7 @@ static int launch_train_batch(ep_ctx* c) {
         issue_train_batch(c);
         CK(cudaGetLastError(), "batch launch");
     }
-    if (++c->host_batch >= c->steps_per_pass) { c->host_batch = 0; ++c->host_pass; }
+    advance_host_batch(c);
     return EP_OK;
 }
 
@@ -694,9 +804,7 @@ extern "C" int ep_train(ep_ctx* c, ep_pass_stats* stats, uint32_t stats_len) {
     for (uint32_t pass = 1; pass <= c->cfg.passes; ++pass) {
         if ((rc = clear_accumulators(c))) break;
         cudaEventRecord(e0, c->stream);
-        for (uint32_t b = 0; b < c->steps_per_pass; ++b)
-            if ((rc = launch_train_batch(c))) break;
-        if (rc) break;
+        if ((rc = launch_train_run(c, c->steps_per_pass))) break;
         cudaEventRecord(e1, c->stream);
         if ((rc = read_state(c))) break;
         float ms = 0.f;
@@ -721,7 +829,7 @@ extern "C" int ep_train_batches(ep_ctx* c, uint32_t n_batches, ep_pass_stats* st
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, c->stream);
-    for (uint32_t i = 0; i < n_batches && !rc; ++i) rc = launch_train_batch(c);
+    rc = launch_train_run(c, n_batches);
     cudaEventRecord(e1, c->stream);
     if (!rc) rc = read_state(c);
     float ms = 0.f;
@@ -942,6 +1050,14 @@ extern "C" int ep_ag_backward(ep_ctx* c, const void* dloss_dev, void* grad_dev, 
     CK(cudaGetLastError(), "gradient scatter");
     CK(cudaStreamSynchronize(s), "autograd backward");
     return EP_OK;
+}
+
+extern "C" int ep_get_tuning(ep_ctx* c, uint32_t* chunk, int32_t* fused_mode, uint32_t* graph_batches) {
+    if (!c) return EP_ERR_INVALID_ARG;
+    if (chunk) *chunk = c->chunk;
+    if (fused_mode) *fused_mode = c->fused_mode;
+    if (graph_batches) *graph_batches = c->graph_batches;
+    return c->tuned ? EP_OK : 1;
 }
 
 // ---------------------------------------------------------------------------

@@ -84,7 +84,9 @@ typedef struct ep_config {
     int32_t grad_mode;           /* EP_GRAD_* */
     int32_t device;              /* CUDA device ordinal */
     int32_t use_graphs;          /* replay each batch as a CUDA graph */
-    int32_t autotune;            /* pick launch shapes by timing candidates */
+    int32_t autotune;            /* pick launch shapes by timing candidates on the
+                                    first training batches (see ep_get_tuning);
+                                    results then depend on timing: default 0 */
 } ep_config;
 
 typedef struct ep_pass_stats {
@@ -191,6 +193,15 @@ int ep_batch_step(ep_ctx* ctx, const ep_batch_samples* samples, float lr, uint32
 /* Copies the table out as n_feat*dims FP32.  Replaces the EmbeddingStore
  * returned by learn (src/lib.rs:1362-1368). */
 int ep_get_table(ep_ctx* ctx, float* out);
+
+/* Launch shapes in use (no counterpart in the reference): the reducer's items
+ * per warp, the FUSED form's Adam placement (2 = queued in the reducer, 1 = a
+ * separate kernel, 0 = per row as each feature closes) and the batches per
+ * replayed CUDA graph.  With config.autotune the first training call that
+ * asks for enough batches times the candidates on real batches and keeps the
+ * fastest; returns EP_OK once that choice is made, 1 before (the values are
+ * then the defaults).  Any pointer may be NULL. */
+int ep_get_tuning(ep_ctx* ctx, uint32_t* chunk, int32_t* fused_mode, uint32_t* graph_batches);
 
 /* Row download without device allocation (no counterpart in the reference).
  * Writes rows [first_row, first_row + n_rows) of the table to out (host

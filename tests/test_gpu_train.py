@@ -140,3 +140,46 @@ def test_large_chung_lu_batches():
     assert s2["train_loss"] < s1["train_loss"]
     t = ctx.get_table(w["n_feat"], ep["dims"])
     assert np.isfinite(t).all()
+
+
+def _cl_ctx(w, form=_native.FORM_FUSED_BF16, autotune=0):
+    cfg = _native.default_config()
+    ep = w["ep"]
+    cfg.dims, cfg.negatives, cfg.loss, cfg.gamma = ep["dims"], ep["negatives"], _native.LOSS_STARSPACE, ep["gamma"]
+    cfg.batch_size, cfg.alpha, cfg.passes, cfg.valid_pct = 2048, ep["alpha"], 1, 0.0
+    cfg.max_nodes_kind, cfg.max_nodes = _native.SAMPLE_FIXED, float(ep["max_nodes"])
+    cfg.form, cfg.autotune = form, autotune
+    ctx = _native.Context(cfg)
+    ctx.upload_graph(w["rows"], w["cols"], None)
+    ctx.upload_features(w["fptr"], w["fids"], w["n_feat"])
+    ctx.set_table(None)
+    return ctx
+
+
+def test_multi_batch_graph_matches_single_batch_graphs(monkeypatch):
+    # runs of 16 batches replay one graph; the result must equal one graph
+    # replay per batch bit for bit (same kernels, same order)
+    w = datagen.workload("cl10m", scale=0.005)
+    tables = []
+    for gb in ("16", "1"):
+        monkeypatch.setenv("EP_GRAPH_BATCHES", gb)
+        ctx = _cl_ctx(w)
+        assert ctx.tuning()[3] == int(gb)
+        ctx.train_batches(37)
+        tables.append(ctx.get_table(w["n_feat"], w["ep"]["dims"]))
+    assert np.array_equal(tables[0], tables[1])
+
+
+@pytest.mark.parametrize("form", [_native.FORM_FUSED_BF16, _native.FORM_PLAIN_FP32])
+def test_autotune_picks_a_candidate_and_trains(form):
+    w = datagen.workload("cl10m", scale=0.01)
+    ctx = _cl_ctx(w, form=form, autotune=1)
+    assert ctx.tuning()[0] is False
+    s1 = ctx.train_batches(70)          # the candidates' batches, then 10 more
+    tuned, chunk, mode, _ = ctx.tuning()
+    assert tuned and chunk in (64, 128, 256)
+    assert mode in ((1, 2) if form == _native.FORM_FUSED_BF16 else (2,))
+    ctx.train_batches(120)
+    s2 = ctx.train_batches(10)
+    assert s2["train_loss"] < s1["train_loss"]
+    assert np.isfinite(ctx.get_table(w["n_feat"], w["ep"]["dims"])).all()
