@@ -78,7 +78,7 @@ class EpPassStats(ctypes.Structure):
         ("train_loss", ctypes.c_float),
         ("valid_loss", ctypes.c_float),
         ("lr_last", ctypes.c_float),
-        ("pad", ctypes.c_uint32),
+        ("noise_last", ctypes.c_float),
         ("anchors", ctypes.c_uint64),
         ("kept_anchors", ctypes.c_uint64),
         ("nan_anchors", ctypes.c_uint64),
@@ -92,7 +92,7 @@ class EpPassStats(ctypes.Structure):
     ]
 
     def as_dict(self):
-        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
         d["pass"] = d.pop("pass_")
         return d
 

@@ -184,7 +184,6 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     if (cfg->valid_pct < 0.f || cfg->valid_pct >= 1.f) { g_create_err = "valid_pct must be in [0, 1)"; return EP_ERR_INVALID_ARG; }
     if (cfg->max_features_kind != EP_SAMPLE_ALL) { g_create_err = "max_features sampling is not implemented on the GPU path"; return EP_ERR_UNSUPPORTED; }
     if (cfg->hard_negatives != 0) { g_create_err = "hard negatives are not implemented on the GPU path"; return EP_ERR_UNSUPPORTED; }
-    if (cfg->noise > 1e-9f) { g_create_err = "gradient noise is not implemented on the GPU path"; return EP_ERR_UNSUPPORTED; }
     if (cfg->weighted_neighbor_sampling && cfg->weighted_neighbor_averaging) {
         g_create_err = "weighted neighbour sampling with weighted averaging is not implemented on the GPU path";
         return EP_ERR_UNSUPPORTED;
@@ -460,6 +459,14 @@ static int prepare_train(ep_ctx* c) {
     return EP_OK;
 }
 
+// Per-step decay of the gradient-noise scale: from cfg.noise at step 0 to
+// 1e-9 after all updates (mod.rs:140-146), in f32 as the reference does.
+static float noise_decay(const ep_ctx* c) {
+    if (!(c->cfg.noise > 1e-9f) || c->total_steps == 0) return 1.f;
+    const float min_noise = 1e-9f;
+    return expf((logf(min_noise) - logf(c->cfg.noise)) / (float)c->total_steps);
+}
+
 static SampleParams sample_params(ep_ctx* c, BatchState* st, bool eval, bool injected) {
     SampleParams sp{};
     sp.st = st;
@@ -584,7 +591,8 @@ static uint32_t kernels_per_batch(const ep_ctx* c) {
 static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr) {
     BatchState* st = c->st.as<BatchState>();
     cudaStream_t s = c->stream;
-    launch_batch_begin(st, c->n_train, c->Bcap, c->steps_per_pass, c->total_steps, c->warmup, c->cfg.alpha, 0, s);
+    launch_batch_begin(st, c->n_train, c->Bcap, c->steps_per_pass, c->total_steps, c->warmup, c->cfg.alpha, 0,
+                       c->cfg.noise, noise_decay(c), s);
     SampleParams sp = sample_params(c, st, false, false);
     launch_sample(sp, s);
     launch_scan_occ(st, c->occ.as<uint32_t>(), c->Bcap, c->items_cap, s);
@@ -741,7 +749,7 @@ static int run_validation(ep_ctx* c, double* mean_out) {
     CK(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream), "eval state");
     const uint32_t nb = (c->n_valid + c->Bcap - 1) / c->Bcap;
     for (uint32_t b = 0; b < nb; ++b) {
-        launch_batch_begin(st, c->n_valid, c->Bcap, nb, 1, 0, c->cfg.alpha, 0, c->stream);
+        launch_batch_begin(st, c->n_valid, c->Bcap, nb, 1, 0, c->cfg.alpha, 0, 0.f, 1.f, c->stream);
         SampleParams sp = sample_params(c, st, true, false);
         launch_sample(sp, c->stream);
         ForwardParams fp = forward_params(c, st, c->table.p, false, true);
@@ -777,6 +785,7 @@ static void fill_stats(ep_ctx* c, ep_pass_stats* s, uint32_t pass, double ms, do
     s->train_loss = h.pass_batches ? (float)(h.pass_err_sum / (double)h.pass_batches) : 0.f;
     s->valid_loss = (float)valid;
     s->lr_last = h.lr;
+    s->noise_last = h.noise_sigma;
     s->anchors = h.anchors;
     s->kept_anchors = h.kept;
     s->nan_anchors = h.nan_anchors;
@@ -932,6 +941,7 @@ static int run_injected(ep_ctx* c, uint32_t B, int tt, const void* table, void* 
     h.lr = lr;
     h.bc1 = 1.f - powf(0.9f, (float)pass + 1.f);
     h.bc2 = 1.f - powf(0.999f, (float)pass + 1.f);
+    h.noise_sigma = c->cfg.noise > 1e-9f ? c->cfg.noise : 0.f;   // injected steps: the configured scale
     BatchState* st = c->st_inj.as<BatchState>();
     if (!c->st_inj.ensure(sizeof(BatchState))) return c->fail(EP_ERR_OOM, "state allocation failed");
     st = c->st_inj.as<BatchState>();

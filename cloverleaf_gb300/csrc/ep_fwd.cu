@@ -57,7 +57,7 @@ __device__ __forceinline__ uint32_t permute(uint32_t pos, uint32_t n, uint32_t h
 // k_batch_begin: batch range, learning rate and Adam bias corrections.
 // ---------------------------------------------------------------------------
 __global__ void k_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, uint64_t total,
-                              uint64_t warmup, float alpha, int injected) {
+                              uint64_t warmup, float alpha, int injected, float noise, float noise_decay) {
     pdl_wait();
     pdl_trigger();
     if (threadIdx.x != 0) return;
@@ -78,6 +78,9 @@ __global__ void k_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, ui
         lr = min_alpha + ratio * (alpha - min_alpha);
     }
     st->lr = lr;
+    // gradient noise: LRScheduler::exp_decay(0, noise, decay) at this step
+    // (mod.rs:140-146; scheduler.rs:50-52); injected batches keep their value
+    if (!injected) st->noise_sigma = noise > 1e-9f ? fmaxf(noise * powf(noise_decay, (float)s), 0.f) : 0.f;
     const float t = (float)st->pass + 1.f;
     st->bc1 = 1.f - powf(0.9f, t);
     st->bc2 = 1.f - powf(0.999f, t);
@@ -978,9 +981,10 @@ void launch_split(uint32_t* train, uint32_t n_train, uint32_t* valid, uint32_t n
 // Launchers
 // ---------------------------------------------------------------------------
 void launch_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, uint32_t steps_per_pass,
-                        uint64_t total, uint64_t warmup, float alpha, int injected, cudaStream_t s) {
+                        uint64_t total, uint64_t warmup, float alpha, int injected, float noise, float noise_decay,
+                        cudaStream_t s) {
     (void)steps_per_pass;
-    launch_chain(k_batch_begin, 1, 32, 0, s, st, n_order, cap, total, warmup, alpha, injected);
+    launch_chain(k_batch_begin, 1, 32, 0, s, st, n_order, cap, total, warmup, alpha, injected, noise, noise_decay);
 }
 
 void launch_sample(const SampleParams& p, cudaStream_t s) {

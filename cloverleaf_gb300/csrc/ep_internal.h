@@ -47,6 +47,7 @@ struct BatchState {
     float bc1, bc2;         // 1 - beta^t with t = pass + 1 (optimizer.rs:50)
     uint32_t error;         // ERR_* bits, sticky
     uint32_t n_items;       // items emitted by this batch
+    float noise_sigma;      // gradient-noise scale of this step (0 = off)
     // per-batch outputs of k_batch_end
     float batch_err;        // sum(loss kept) / n_anchors (0 when none kept)
     uint32_t batch_kept;
@@ -160,7 +161,7 @@ struct ReduceParams {
 // ---- launchers (defined in the kernel translation units) -----------------
 void launch_batch_begin(BatchState* st, uint32_t n_order, uint32_t batch_cap,
                         uint32_t steps_per_pass, uint64_t total_steps, uint64_t warmup,
-                        float alpha, int injected, cudaStream_t s);
+                        float alpha, int injected, float noise, float noise_decay, cudaStream_t s);
 void launch_sample(const SampleParams& p, cudaStream_t s);
 void launch_scan_occ(BatchState* st, uint32_t* occ, uint32_t cap, uint64_t items_cap,
                      cudaStream_t s);

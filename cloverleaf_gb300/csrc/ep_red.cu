@@ -43,6 +43,21 @@ constexpr uint32_t RED_MAX_CTAS = 152 * 8;
 
 uint32_t reduce_chunks(uint64_t cap, uint32_t chunk) { return (uint32_t)((cap + chunk - 1) / chunk); }
 
+// Per-batch Adam constants, read once per kernel from the batch state.
+struct AdamStep {
+    float lr, rb1, rb2, sigma;    // learning rate, 1/(1 - beta^t), gradient-noise scale
+    uint32_t step;
+    static __device__ __forceinline__ AdamStep load(const BatchState* st) {
+        AdamStep a;
+        a.lr = st->lr;
+        a.rb1 = 1.f / st->bc1;
+        a.rb2 = 1.f / st->bc2;
+        a.sigma = st->noise_sigma;
+        a.step = (uint32_t)st->step;
+        return a;
+    }
+};
+
 // Adam on one row (optimizer.rs:43-81): t = pass + 1, beta1 0.9, beta2 0.999,
 // eps 1e-8; rows containing NaN are skipped (optimizer.rs:56).  adam_apply
 // takes the row's loaded moments and weights (mm, vv, ee) and stores the
@@ -50,14 +65,33 @@ uint32_t reduce_chunks(uint64_t cap, uint32_t chunk) { return (uint32_t)((cap + 
 template <typename T, int VPL>
 __device__ __forceinline__ void adam_apply(T* __restrict__ table, float* __restrict__ m, float* __restrict__ v,
                                            uint32_t f, uint32_t dpad, const float (&g)[VPL], float (&mm)[VPL],
-                                           float (&vv)[VPL], float (&ee)[VPL], float lr, float bc1, float bc2,
-                                           uint64_t seed, uint32_t step, int lane) {
+                                           float (&vv)[VPL], float (&ee)[VPL], const AdamStep& as, uint64_t seed,
+                                           int lane) {
     const uint64_t o = (uint64_t)f * dpad;
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-    const float rb1 = 1.f / bc1, rb2 = 1.f / bc2;
+    const float lr = as.lr, rb1 = as.rb1, rb2 = as.rb2;
+    const uint32_t step = as.step;
+    float gn[VPL];
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) gn[k] = g[k];
+    if (as.sigma > 0.f) {
+        // gradient noise g += sigma * N(0, 1) (mod.rs:239-247): Box-Muller on
+        // two Philox draws per pair of elements, keyed by (row, step, column)
+#pragma unroll
+        for (int k = 0; k < VPL; k += 2) {
+            const u32x4 r = philox(u32x4{f, step, (ST_NOISE << 24) | (uint32_t)(lane * VPL + k), 0u}, seed);
+            const float u1 = ((float)(r.x >> 8) + 1.f) * (1.0f / 16777216.0f);   // (0, 1]
+            const float u2 = (float)(r.y >> 8) * (1.0f / 16777216.0f);
+            const float rad = sqrtf(-2.f * logf(u1));
+            float sn, cs;
+            sincosf(6.283185307179586f * u2, &sn, &cs);
+            gn[k] += as.sigma * rad * cs;
+            if (k + 1 < VPL) gn[k + 1] += as.sigma * rad * sn;
+        }
+    }
 #pragma unroll
     for (int k = 0; k < VPL; ++k) {
-        const float gk = g[k];
+        const float gk = gn[k];
         mm[k] = b1 * mm[k] + (1.f - b1) * gk;
         vv[k] = b2 * vv[k] + (1.f - b2) * (gk * gk);
         const float mh = mm[k] * rb1;
@@ -87,8 +121,8 @@ __device__ __forceinline__ void adam_apply(T* __restrict__ table, float* __restr
 
 template <typename T, int VPL, typename A>
 __device__ __forceinline__ void adam_row(T* __restrict__ table, float* __restrict__ m, float* __restrict__ v,
-                                         uint32_t f, uint32_t dpad, const A (&g)[VPL], float lr, float bc1, float bc2,
-                                         uint64_t seed, uint32_t step, int lane, bool lane_on) {
+                                         uint32_t f, uint32_t dpad, const A (&g)[VPL], const AdamStep& as,
+                                         uint64_t seed, int lane, bool lane_on) {
     bool bad = false;
 #pragma unroll
     for (int k = 0; k < VPL; ++k) bad = bad || (g[k] != g[k]);
@@ -103,7 +137,7 @@ __device__ __forceinline__ void adam_row(T* __restrict__ table, float* __restric
         RowIO<float, VPL>::load_cg(m + o, lane, mm);
         RowIO<float, VPL>::load_cg(v + o, lane, vv);
         RowIO<T, VPL>::load_cg(table + o, lane, ee);
-        adam_apply<T, VPL>(table, m, v, f, dpad, gg, mm, vv, ee, lr, bc1, bc2, seed, step, lane);
+        adam_apply<T, VPL>(table, m, v, f, dpad, gg, mm, vv, ee, as, seed, lane);
     }
 }
 
@@ -183,8 +217,8 @@ __device__ __forceinline__ void queue_slot_ptrs(const WarpQueue& q, uint32_t slo
 // Adam on the oldest slot (optimizer.rs:43-81).  The caller has waited for
 // that slot's copies.
 template <typename T, int VPL>
-__device__ __forceinline__ void queue_pop(const ReduceParams& p, WarpQueue& q, int lane, bool lane_on, float lr,
-                                          float bc1, float bc2, uint32_t step) {
+__device__ __forceinline__ void queue_pop(const ReduceParams& p, WarpQueue& q, int lane, bool lane_on,
+                                          const AdamStep& as) {
     if constexpr (sizeof(T) != 8) {
         const uint32_t dpad = p.dpad;
         float *gs, *ms, *vs;
@@ -204,7 +238,7 @@ __device__ __forceinline__ void queue_pop(const ReduceParams& p, WarpQueue& q, i
                 RowIO<float, VPL>::load_cg(p.v + o, lane, vv);
                 RowIO<T, VPL>::load_cg((const T*)p.table + o, lane, ee);
             }
-            adam_apply<T, VPL>((T*)p.table, p.m, p.v, f, dpad, gg, mm, vv, ee, lr, bc1, bc2, p.seed, step, lane);
+            adam_apply<T, VPL>((T*)p.table, p.m, p.v, f, dpad, gg, mm, vv, ee, as, p.seed, lane);
         }
     }
     q.head = q.head + 1 == QN ? 0u : q.head + 1;
@@ -214,11 +248,11 @@ __device__ __forceinline__ void queue_pop(const ReduceParams& p, WarpQueue& q, i
 // Queues a finished (NaN-free) row; updates the oldest slot first when full.
 template <typename T, typename A, int VPL>
 __device__ __forceinline__ void queue_push(const ReduceParams& p, WarpQueue& q, uint32_t f, const A (&acc)[VPL], int lane,
-                                           bool lane_on, float lr, float bc1, float bc2, uint32_t step) {
+                                           bool lane_on, const AdamStep& as) {
     if (q.n == QN) {
         cp_async_wait<QN - 1>();
         __syncwarp();
-        queue_pop<T, VPL>(p, q, lane, lane_on, lr, bc1, bc2, step);
+        queue_pop<T, VPL>(p, q, lane, lane_on, as);
     }
     uint32_t slot = q.head + q.n;
     if (slot >= QN) slot -= QN;
@@ -242,23 +276,23 @@ __device__ __forceinline__ void queue_push(const ReduceParams& p, WarpQueue& q, 
 
 // Updates every queued slot (end of the warp's work).
 template <typename T, int VPL>
-__device__ __forceinline__ void queue_flush(const ReduceParams& p, WarpQueue& q, int lane, bool lane_on, float lr,
-                                            float bc1, float bc2, uint32_t step) {
+__device__ __forceinline__ void queue_flush(const ReduceParams& p, WarpQueue& q, int lane, bool lane_on,
+                                            const AdamStep& as) {
     cp_async_wait<0>();
     __syncwarp();
-    while (q.n) queue_pop<T, VPL>(p, q, lane, lane_on, lr, bc1, bc2, step);
+    while (q.n) queue_pop<T, VPL>(p, q, lane, lane_on, as);
 }
 
 template <typename T, typename A, int VPL, int MODE>
 __device__ __forceinline__ void finish_row(const ReduceParams& p, uint32_t f, const A (&acc)[VPL], int lane,
-                                           bool lane_on, float lr, float bc1, float bc2, uint32_t step,
-                                           uint32_t* fin, uint32_t& n_fin, WarpQueue* q = nullptr) {
+                                           bool lane_on, const AdamStep& as, uint32_t* fin, uint32_t& n_fin,
+                                           WarpQueue* q = nullptr) {
     if constexpr (MODE == OUT_QUEUE) {
         // rows containing NaN get no Adam step (optimizer.rs:56): not queued
         bool bad = false;
 #pragma unroll
         for (int k = 0; k < VPL; ++k) bad = bad || (acc[k] != acc[k]);
-        if (!__any_sync(FULL, bad)) queue_push<T, A, VPL>(p, *q, f, acc, lane, lane_on, lr, bc1, bc2, step);
+        if (!__any_sync(FULL, bad)) queue_push<T, A, VPL>(p, *q, f, acc, lane, lane_on, as);
     } else if constexpr (MODE == OUT_DENSE) {
         if (lane_on) store_row<A, VPL, A>((A*)p.gdense + (uint64_t)f * p.dpad, lane, acc);
         if (fin) {
@@ -268,7 +302,7 @@ __device__ __forceinline__ void finish_row(const ReduceParams& p, uint32_t f, co
             p.touched[atomicAdd(p.n_touched, 1u)] = f;
         }
     } else {
-        adam_row<T, VPL, A>((T*)p.table, p.m, p.v, f, p.dpad, acc, lr, bc1, bc2, p.seed, step, lane, lane_on);
+        adam_row<T, VPL, A>((T*)p.table, p.m, p.v, f, p.dpad, acc, as, p.seed, lane, lane_on);
     }
 }
 
@@ -342,8 +376,7 @@ __global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREAD
     const uint32_t nchunks = (M + C - 1) / C;
     const uint32_t NR = p.NR;
     const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
-    const float lr = p.st->lr, bc1 = p.st->bc1, bc2 = p.st->bc2;
-    const uint32_t step = (uint32_t)p.st->step;
+    const AdamStep as = AdamStep::load(p.st);
     const D* dir = std::is_same<D, A>::value ? (const D*)p.dir : (const D*)p.dir16;
     const A* scale = (const A*)p.scale;
     unsigned long long g_cnt = 0, u_cnt = 0;
@@ -479,7 +512,7 @@ __global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREAD
             auto close_open = [&](int lo) {
                 if (started_here) {
                     if (any_kept) {
-                        finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step, fin, n_fin, &q);
+                        finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, as, fin, n_fin, &q);
                         ++u_cnt;
                     }
                 } else {
@@ -536,7 +569,7 @@ __global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREAD
         const bool cont = i1 < M && p.skey[i1] == cur_f;
         if (started_here && !cont) {
             if (any_kept) {
-                finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, lr, bc1, bc2, step, fin, n_fin, &q);
+                finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, as, fin, n_fin, &q);
                 ++u_cnt;
             }
         } else if (!started_here) {
@@ -550,7 +583,7 @@ __global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREAD
         if (lane == 0) p.carry_flags[c] = flags;
     }
     if constexpr (MODE == OUT_DENSE) fin_flush(p, fin, n_fin, lane);
-    if constexpr (MODE == OUT_QUEUE) queue_flush<T, VPL>(p, q, lane, lane_on, lr, bc1, bc2, step);
+    if constexpr (MODE == OUT_QUEUE) queue_flush<T, VPL>(p, q, lane, lane_on, as);
     g_cnt = warp_sum<unsigned long long>(g_cnt);
     if (lane == 0) {
         if (g_cnt) atomicAdd(&p.st->gathered, g_cnt);
@@ -597,8 +630,7 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
     const uint32_t C = p.chunk;
     const uint32_t nchunks = (M + C - 1) / C;
     const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
-    const float lr = p.st->lr, bc1 = p.st->bc1, bc2 = p.st->bc2;
-    const uint32_t step = (uint32_t)p.st->step;
+    const AdamStep as = AdamStep::load(p.st);
     unsigned long long u_cnt = 0;
     for (uint32_t c = gw; c < nchunks; c += nw) {
         const uint32_t fl = p.carry_flags[c];
@@ -638,7 +670,7 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
         }
         if (kept) {
             uint32_t none = 0;
-            finish_row<T, A, VPL, MODE>(p, f, acc, lane, lane_on, lr, bc1, bc2, step, nullptr, none);
+            finish_row<T, A, VPL, MODE>(p, f, acc, lane, lane_on, as, nullptr, none);
             ++u_cnt;
         }
     }
@@ -662,8 +694,7 @@ __global__ void __launch_bounds__(fixl_threads(VPL)) k_fixup_long(ReduceParams p
     const uint32_t C = p.chunk;
     const uint32_t n_long = p.st->n_long;
     const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
-    const float lr = p.st->lr, bc1 = p.st->bc1, bc2 = p.st->bc2;
-    const uint32_t step = (uint32_t)p.st->step;
+    const AdamStep as = AdamStep::load(p.st);
     unsigned long long u_cnt = 0;
     for (uint32_t q = blockIdx.x; q < n_long; q += gridDim.x) {
         const uint32_t c = p.long_list[q];
@@ -715,7 +746,7 @@ __global__ void __launch_bounds__(fixl_threads(VPL)) k_fixup_long(ReduceParams p
             }
             if ((fl & CF_TAIL_KEPT) || s_kept) {
                 uint32_t none = 0;
-                finish_row<T, A, VPL, MODE>(p, f, tot, lane, lane_on, lr, bc1, bc2, step, nullptr, none);
+                finish_row<T, A, VPL, MODE>(p, f, tot, lane, lane_on, as, nullptr, none);
                 ++u_cnt;
             }
         }
@@ -738,8 +769,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_adam_dense(BatchState* st, T* t
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t n = *n_touched;
     const bool lane_on = (uint32_t)(lane * VPL) < dpad;
-    const float lr = st->lr, bc1 = st->bc1, bc2 = st->bc2;
-    const uint32_t step = (uint32_t)st->step;
+    const AdamStep as = AdamStep::load(st);
     for (uint32_t r0 = 2 * gw; r0 < n; r0 += 2 * nw) {
         uint32_t f[2];
         bool on[2];
@@ -768,7 +798,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_adam_dense(BatchState* st, T* t
 #pragma unroll
             for (int k = 0; k < VPL; ++k) bad = bad || (gg[u][k] != gg[u][k]);
             if (on[u] && !__any_sync(FULL, bad) && lane_on)
-                adam_apply<T, VPL>(table, m, v, f[u], dpad, gg[u], mm[u], vv[u], ee[u], lr, bc1, bc2, seed, step, lane);
+                adam_apply<T, VPL>(table, m, v, f[u], dpad, gg[u], mm[u], vv[u], ee[u], as, seed, lane);
         }
     }
 }

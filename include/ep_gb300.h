@@ -95,7 +95,7 @@ typedef struct ep_pass_stats {
     float train_loss;            /* mean over batches of sum(loss)/batch_len (mod.rs:256-265) */
     float valid_loss;            /* NaN when valid_pct == 0 (mod.rs:267-283) */
     float lr_last;
-    uint32_t pad;
+    float noise_last;            /* gradient-noise scale of the last step (0 = off) */
     uint64_t anchors;            /* anchors processed */
     uint64_t kept_anchors;       /* finite loss > 0 */
     uint64_t nan_anchors;
