@@ -182,7 +182,10 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
         return EP_ERR_INVALID_ARG;
     }
     if (cfg->valid_pct < 0.f || cfg->valid_pct >= 1.f) { g_create_err = "valid_pct must be in [0, 1)"; return EP_ERR_INVALID_ARG; }
-    if (cfg->max_features_kind != EP_SAMPLE_ALL) { g_create_err = "max_features sampling is not implemented on the GPU path"; return EP_ERR_UNSUPPORTED; }
+    if (cfg->max_features_kind == EP_SAMPLE_PROB && !(cfg->max_features > 0.f && cfg->max_features < 1.f)) {
+        g_create_err = "probability max_features must be in (0, 1)";
+        return EP_ERR_INVALID_ARG;
+    }
     if (cfg->hard_negatives != 0) { g_create_err = "hard negatives are not implemented on the GPU path"; return EP_ERR_UNSUPPORTED; }
     if (cfg->weighted_neighbor_sampling && cfg->weighted_neighbor_averaging) {
         g_create_err = "weighted neighbour sampling with weighted averaging is not implemented on the GPU path";
@@ -459,6 +462,19 @@ static int prepare_train(ep_ctx* c) {
     return EP_OK;
 }
 
+static FeatDrop feat_drop(const ep_ctx* c) {
+    FeatDrop fd{};
+    fd.kind = c->cfg.max_features_kind;
+    fd.seed = c->cfg.seed;
+    if (fd.kind == EP_SAMPLE_FIXED) fd.k = (uint32_t)c->cfg.max_features;
+    if (fd.kind == EP_SAMPLE_PROB) {
+        fd.p = c->cfg.max_features;
+        const double t = (double)fd.p * 4294967296.0;
+        fd.thr = t >= 4294967295.0 ? 0xffffffffu : (uint32_t)t;
+    }
+    return fd;
+}
+
 // Per-step decay of the gradient-noise scale: from cfg.noise at step 0 to
 // 1e-9 after all updates (mod.rs:140-146), in f32 as the reference does.
 static float noise_decay(const ep_ctx* c) {
@@ -476,7 +492,7 @@ static SampleParams sample_params(ep_ctx* c, BatchState* st, bool eval, bool inj
     sp.cfg.Kcap = c->buf_K;
     sp.cfg.R = c->R;
     sp.cfg.weighted_avg = c->cfg.weighted_neighbor_averaging;
-    sp.cfg.feat_scalar = 1.f;
+    sp.cfg.fd = feat_drop(c);
     sp.cfg.seed = c->cfg.seed;
     sp.row_ptr = c->row.as<uint64_t>();
     sp.cols = c->cols.as<uint32_t>();
@@ -507,7 +523,8 @@ static ForwardParams forward_params(ep_ctx* c, BatchState* st, const void* table
     fp.neg_margin = c->cfg.neg_margin;
     fp.loss_weighting = eval ? EP_LW_NONE : c->cfg.loss_weighting;   // validation reports the raw loss
     fp.lw_exp = c->cfg.loss_weighting_exp;
-    fp.feat_scalar = 1.f;
+    fp.fd = feat_drop(c);
+    fp.eval = eval;
     fp.R = c->R;
     fp.Kcap = c->buf_K;
     fp.dims = c->dims;

@@ -25,6 +25,97 @@ enum { S_ALL = 0, S_FIXED = 1, S_PROB = 2 };
 enum { LW_NONE = 0, LW_LOG = 1, LW_EXP = 2 };
 
 // ---------------------------------------------------------------------------
+// Feature dropout (max_features; model.rs:257-278 with Sample::sample,
+// utils.rs:193-216).  Node u in slot q of anchor v (q = 0 the anchor, then
+// its sampled neighbours, then its negatives) keeps a subset of its n
+// features and adds the sample's scalar to its count weight:
+//   Fixed(k)  the min(k, n) positions with the smallest keys (equal keys in
+//             position order): a uniform k-subset; scalar n / min(k, n)
+//   Prob(p)   the positions whose key < p * 2^32 (Bernoulli(p) each); if
+//             none, the one with the smallest key, scalar (1 - p^n) / p;
+//             else scalar 1 / p
+//   All       every position; scalar 1
+// Keys are Philox draws of (v, step, q, position).  k_sample counts the kept
+// positions and the gathers enumerate them from the same keys, so the item
+// offsets and the emitted items agree exactly.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t fd_key(const FeatDrop& fd, uint32_t v, uint32_t salt, uint32_t q, uint32_t j) {
+    return rand_u32(fd.seed, v, salt, ST_FSEL, ((q & 0x3ffu) << 16) | (j & 0xffffu));
+}
+
+// Kept count of one node (one thread) and the scalar added to its weight.
+__device__ __forceinline__ uint32_t fd_kept(const FeatDrop& fd, uint32_t v, uint32_t salt, uint32_t q, uint32_t n,
+                                            float& scalar) {
+    scalar = 1.f;
+    if (fd.kind == S_ALL || n == 0) return n;
+    if (fd.kind == S_FIXED) {
+        const uint32_t k = min(fd.k, n);
+        scalar = (float)n / (float)k;
+        return k;
+    }
+    uint32_t c = 0;
+    for (uint32_t j = 0; j < n; ++j) c += fd_key(fd, v, salt, q, j) < fd.thr;
+    if (c == 0) {
+        scalar = (1.f - powf(fd.p, (float)n)) / fd.p;
+        return 1;
+    }
+    scalar = 1.f / fd.p;
+    return c;
+}
+
+// Probability sampling of one node (warp): whether no position passed, and
+// the position with the smallest key.
+struct FdNode {
+    bool none;
+    uint32_t argmin;
+};
+
+__device__ __forceinline__ FdNode fd_node(const FeatDrop& fd, uint32_t v, uint32_t salt, uint32_t q, uint32_t n,
+                                          int lane) {
+    FdNode r{false, 0u};
+    if (fd.kind != S_PROB || n == 0) return r;
+    uint32_t cnt = 0;
+    unsigned long long best = ~0ull;
+    for (uint32_t j0 = 0; j0 < n; j0 += 32) {
+        const uint32_t j = j0 + lane;
+        const bool in = j < n;
+        const uint32_t key = in ? fd_key(fd, v, salt, q, j) : 0xffffffffu;
+        cnt += __popc(__ballot_sync(FULL, in && key < fd.thr));
+        if (in) best = min(best, ((unsigned long long)key << 32) | j);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(FULL, best, o));
+    r.none = cnt == 0;
+    r.argmin = (uint32_t)best;
+    return r;
+}
+
+// Kept positions j0 .. j0+31 of one node as a lane mask (warp).
+__device__ __forceinline__ unsigned fd_mask(const FeatDrop& fd, const FdNode& nd, uint32_t v, uint32_t salt,
+                                            uint32_t q, uint32_t n, uint32_t j0, int lane) {
+    const uint32_t j = j0 + lane;
+    const bool in = j < n;
+    bool sel = in;
+    if (fd.kind == S_PROB) {
+        sel = in && (nd.none ? j == nd.argmin : fd_key(fd, v, salt, q, j) < fd.thr);
+    } else if (fd.kind == S_FIXED && min(fd.k, n) < n) {
+        const uint32_t k = min(fd.k, n);
+        const uint32_t kj = in ? fd_key(fd, v, salt, q, j) : 0xffffffffu;
+        uint32_t rank = 0;
+        for (uint32_t i0 = 0; i0 < n; i0 += 32) {
+            const uint32_t ki = i0 + lane < n ? fd_key(fd, v, salt, q, i0 + lane) : 0xffffffffu;
+            for (int t = 0; t < 32; ++t) {
+                const uint32_t kt = __shfl_sync(FULL, ki, t);
+                const uint32_t it = i0 + (uint32_t)t;
+                rank += (it < n) && (kt < kj || (kt == kj && it < j));
+            }
+        }
+        sel = in && rank < k;
+    }
+    return __ballot_sync(FULL, sel);
+}
+
+// ---------------------------------------------------------------------------
 // Per-pass anchor order: a keyed Feistel bijection on [0, 2^(2h)) restricted
 // to [0, n) by cycle walking.  Replaces the host shuffle of mod.rs:173 with an
 // O(1)-per-position permutation that needs no buffer and no sort.
@@ -222,14 +313,21 @@ __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
             p.neg[(uint64_t)a * c.R + i] = p.pool[below(rand_u32(c.seed, v, salt, ST_NEG, i), p.n_pool)];
         __syncwarp();
     }
-    // --- item count of this anchor: sum of feature counts over its roles ---
+    // --- item count of this anchor: kept feature counts over its roles ---
     const uint32_t cnt = p.nbr_cnt[a];
     uint64_t occ = 0;
-    if (lane == 0) occ += p.fptr[v + 1] - p.fptr[v];
+    float unused;
+    if (lane == 0) occ += fd_kept(c.fd, v, salt, 0, (uint32_t)(p.fptr[v + 1] - p.fptr[v]), unused);
     const uint32_t* nb = p.nbr + (uint64_t)a * c.Kcap;
-    for (uint32_t q = lane; q < cnt; q += 32) { uint32_t u = nb[q]; occ += p.fptr[u + 1] - p.fptr[u]; }
+    for (uint32_t q = lane; q < cnt; q += 32) {
+        const uint32_t u = nb[q];
+        occ += fd_kept(c.fd, v, salt, 1 + q, (uint32_t)(p.fptr[u + 1] - p.fptr[u]), unused);
+    }
     const uint32_t* ng = p.neg + (uint64_t)a * c.R;
-    for (uint32_t q = lane; q < c.R; q += 32) { uint32_t u = ng[q]; occ += p.fptr[u + 1] - p.fptr[u]; }
+    for (uint32_t q = lane; q < c.R; q += 32) {
+        const uint32_t u = ng[q];
+        occ += fd_kept(c.fd, v, salt, 1 + cnt + q, (uint32_t)(p.fptr[u + 1] - p.fptr[u]), unused);
+    }
     occ = warp_sum<unsigned long long>((unsigned long long)occ);
     if (lane == 0) p.occ[a] = (uint32_t)min(occ, (uint64_t)0xffffffffu);
 }
@@ -323,7 +421,7 @@ __device__ A gather_role(const ForwardParams& p, const T* __restrict__ table, co
             const uint32_t u = nodes[q];
             fs = p.fptr[u];
             fn = (uint32_t)(p.fptr[u + 1] - fs);
-            c = (w ? w[q] : 1.f) + p.feat_scalar;
+            c = (w ? w[q] : 1.f) + 1.f;   // Sample::All features: scalar 1
         }
         const uint32_t incl = warp_incl_scan(fn, lane);
         const uint32_t total = __shfl_sync(FULL, incl, 31);
@@ -383,6 +481,63 @@ __device__ A gather_role(const ForwardParams& p, const T* __restrict__ table, co
     return ntot;
 }
 
+// gather_role with feature dropout: node by node, the kept positions (the
+// keys k_sample counted) in position order, four rows in flight.
+template <typename T, typename A, int VPL>
+__device__ A gather_role_fd(const ForwardParams& p, const T* __restrict__ table, const uint32_t* nodes, const float* w,
+                            uint32_t count, uint32_t slot0, uint32_t v, uint32_t salt, uint32_t src, uint64_t& pos,
+                            bool emit, A (&acc)[VPL], int lane, bool lane_on) {
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) acc[k] = 0;
+    A ntot = 0;
+    for (uint32_t idx = 0; idx < count; ++idx) {
+        const uint32_t u = nodes[idx];
+        const uint64_t fs = p.fptr[u];
+        const uint32_t nall = (uint32_t)(p.fptr[u + 1] - fs);
+        const uint32_t q = slot0 + idx;
+        float scal;
+        const uint32_t kept = fd_kept(p.fd, v, salt, q, nall, scal);
+        const float c = (w ? w[idx] : 1.f) + scal;
+        ntot += (A)c * (A)kept;
+        const FdNode nd = fd_node(p.fd, v, salt, q, nall, lane);
+        for (uint32_t j0 = 0; j0 < nall; j0 += 32) {
+            const unsigned m = fd_mask(p.fd, nd, v, salt, q, nall, j0, lane);
+            uint32_t f = 0;
+            if ((m >> lane) & 1u) {
+                f = p.fids[fs + j0 + lane];
+                if (emit) {
+                    const uint64_t oo = pos + __popc(m & ((1u << lane) - 1u));
+                    p.item_f[oo] = f;
+                    p.item_src[oo] = src;
+                    p.item_c[oo] = c;
+                }
+            }
+            unsigned mm = m;
+            while (mm) {
+                uint32_t fr[4];
+                int nr = 0;
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int b = mm ? __ffs(mm) - 1 : 0;
+                    fr[t] = __shfl_sync(FULL, f, b);
+                    if (mm) { mm &= mm - 1; nr = t + 1; }
+                }
+                if (lane_on) {
+                    A r4[4][VPL];
+#pragma unroll
+                    for (int t = 0; t < 4; ++t)
+                        if (t < nr) RowIO<T, VPL>::load(table + (uint64_t)fr[t] * p.dpad, lane, r4[t]);
+#pragma unroll
+                    for (int t = 0; t < 4; ++t)
+                        if (t < nr) fma_row<T, A, VPL>(acc, (A)c, r4[t]);
+                }
+            }
+            pos += __popc(m);
+        }
+    }
+    return ntot;
+}
+
 // ---------------------------------------------------------------------------
 // Staged gather (the common case): per-warp shared-memory tables of the
 // anchor's role nodes and of all their feature occurrences, so that the row
@@ -396,6 +551,7 @@ constexpr int FWD_WARPS = 8;
 
 struct WarpTables {
     uint32_t node_fs[NODE_CAP];       // first feature index (fptr) of the node
+    uint32_t node_n[NODE_CAP];        // feature count of the node (before dropout)
     uint32_t node_incl[NODE_CAP];     // inclusive prefix of feature counts
     float node_c[NODE_CAP];           // count weight of the node's occurrences
     uint32_t role_ob[ROLE_CAP + 1];   // first occurrence of each role
@@ -412,7 +568,7 @@ __device__ __forceinline__ uint32_t node_role(uint32_t q, uint32_t cnt) {
 // the tables; nothing has been emitted then.
 template <typename A>
 __device__ bool stage_anchor(const ForwardParams& p, WarpTables& W, uint32_t a, uint32_t v, uint32_t cnt,
-                             uint64_t pos, bool emit, uint32_t sbase, int lane) {
+                             uint64_t pos, bool emit, uint32_t sbase, uint32_t salt, int lane) {
     const uint32_t R = p.R;
     const uint32_t n_nodes = 1 + cnt + R;
     if (n_nodes > NODE_CAP || R + 2 > ROLE_CAP) return false;
@@ -431,11 +587,14 @@ __device__ bool stage_anchor(const ForwardParams& p, WarpTables& W, uint32_t a, 
             if (q == 0) { u = v; c = 1.f; }
             else if (q <= cnt) { u = nb[q - 1]; c = nw[q - 1]; }
             else { u = ng[q - 1 - cnt]; c = 1.f; }
-            c += p.feat_scalar;
             const uint64_t fs = p.fptr[u];
-            fn = (uint32_t)(p.fptr[u + 1] - fs);
-            big = big || (fs + fn) > 0xffffffffull;
+            const uint32_t nall = (uint32_t)(p.fptr[u + 1] - fs);
+            float scal;
+            fn = fd_kept(p.fd, v, salt, q, nall, scal);
+            c += scal;
+            big = big || (fs + nall) > 0xffffffffull;
             W.node_fs[q] = (uint32_t)fs;
+            W.node_n[q] = nall;
             W.node_c[q] = c;
             const uint32_t r = node_role(q, cnt);
             const float wsum = c * (float)fn;
@@ -457,6 +616,35 @@ __device__ bool stage_anchor(const ForwardParams& p, WarpTables& W, uint32_t a, 
         W.role_ob[1] = W.node_incl[0];
         W.role_ob[2] = W.node_incl[cnt];
         for (uint32_t i = 1; i <= R; ++i) W.role_ob[2 + i] = W.node_incl[cnt + i];
+    }
+    if (p.fd.kind != S_ALL) {
+        // phase B with feature dropout: node by node, the kept positions in
+        // position order (the same keys k_sample counted)
+        __syncwarp();
+        uint32_t o = 0;
+        for (uint32_t q = 0; q < n_nodes; ++q) {
+            const uint32_t nall = W.node_n[q], fs = W.node_fs[q];
+            const float c = W.node_c[q];
+            const uint32_t src = sbase + node_role(q, cnt);
+            const FdNode nd = fd_node(p.fd, v, salt, q, nall, lane);
+            for (uint32_t j0 = 0; j0 < nall; j0 += 32) {
+                const unsigned m = fd_mask(p.fd, nd, v, salt, q, nall, j0, lane);
+                if ((m >> lane) & 1u) {
+                    const uint32_t oo = o + __popc(m & ((1u << lane) - 1u));
+                    const uint32_t f = p.fids[(uint64_t)fs + j0 + lane];
+                    W.occ_f[oo] = f;
+                    W.occ_c[oo] = c;
+                    if (emit) {
+                        p.item_f[pos + oo] = f;
+                        p.item_src[pos + oo] = src;
+                        p.item_c[pos + oo] = c;
+                    }
+                }
+                o += __popc(m);
+            }
+        }
+        __syncwarp();
+        return true;
     }
     // phase B: one feature id per lane, four batches of loads in flight
     for (uint32_t o0 = 0; o0 < total; o0 += 128) {
@@ -605,10 +793,11 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 4 : 3) : 1) k_fwd_ga
     uint64_t pos = emit ? p.occ_off[a] : 0;
     const uint64_t sbase = (uint64_t)a * NR;
     const uint32_t cnt = p.nbr_cnt[a];
+    const uint32_t salt = p.eval ? 0xffffffffu : (uint32_t)p.st->step;   // as k_sample
     if constexpr (STAGED) {
         extern __shared__ __align__(16) unsigned char fwd_smem[];
         WarpTables& W = reinterpret_cast<WarpTables*>(fwd_smem)[threadIdx.x >> 5];
-        const bool staged = stage_anchor<A>(p, W, a, v, cnt, pos, emit, (uint32_t)sbase, lane);
+        const bool staged = stage_anchor<A>(p, W, a, v, cnt, pos, emit, (uint32_t)sbase, salt, lane);
         if (lane == 0) p.deferred[a] = staged ? 0 : 1;
         if (!staged) return;
         roles_from_table<T, A, VPL>(p, table, W, NR, sbase, lane, lane_on);
@@ -620,9 +809,13 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 4 : 3) : 1) k_fwd_ga
             const uint32_t* nodes = r == 0 ? &v : (r == 1 ? p.nbr + (uint64_t)a * p.Kcap : p.neg + (uint64_t)a * R + (r - 2));
             const float* w = r == 1 ? p.nbr_w + (uint64_t)a * p.Kcap : nullptr;
             const uint32_t count = r == 1 ? cnt : 1u;
+            const uint32_t slot0 = r == 0 ? 0u : (r == 1 ? 1u : 1u + cnt + (r - 2));
             A acc[VPL];
-            const A nr = gather_role<T, A, VPL>(p, table, nodes, w, count, (uint32_t)(sbase + r), pos, emit, acc,
-                                                lane, lane_on);
+            const A nr = p.fd.kind == S_ALL
+                             ? gather_role<T, A, VPL>(p, table, nodes, w, count, (uint32_t)(sbase + r), pos, emit, acc,
+                                                      lane, lane_on)
+                             : gather_role_fd<T, A, VPL>(p, table, nodes, w, count, slot0, v, salt,
+                                                         (uint32_t)(sbase + r), pos, emit, acc, lane, lane_on);
             if (lane_on) {
                 const A rn = (A)1 / nr;
 #pragma unroll

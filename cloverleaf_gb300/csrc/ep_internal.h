@@ -59,6 +59,16 @@ struct BatchState {
     double valid_sum;
 };
 
+// Feature dropout (max_features): EP_SAMPLE_* kind, Fixed count k,
+// Probability p and its key threshold p * 2^32, and the Philox key.
+struct FeatDrop {
+    int kind;
+    uint32_t k;
+    float p;
+    uint32_t thr;
+    uint64_t seed;
+};
+
 struct SampleCfg {
     int nodes_kind;         // EP_SAMPLE_*
     float nodes_val;
@@ -66,7 +76,7 @@ struct SampleCfg {
     uint32_t Kcap;          // neighbour slots per anchor
     uint32_t R;             // negatives
     int weighted_avg;       // weighted_neighbor_averaging
-    float feat_scalar;      // s_u for Sample::All features
+    FeatDrop fd;            // feature dropout of every role node
     uint64_t seed;
 };
 
@@ -101,7 +111,8 @@ struct ForwardParams {
     float gamma, neg_margin;
     int loss_weighting;
     float lw_exp;
-    float feat_scalar;
+    FeatDrop fd;            // feature dropout (same keys as the sampler's counts)
+    int eval;               // validation batch (fixed sampling salt)
     uint32_t R, Kcap, dims, dpad;
     const uint64_t* row_ptr;
     const uint64_t* fptr;

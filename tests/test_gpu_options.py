@@ -1,5 +1,6 @@
 """Reference options off the default path, on the GPU: gradient noise
-(src/algos/ep/mod.rs:140-146, 239-247)."""
+(src/algos/ep/mod.rs:140-146, 239-247) and feature dropout (max_features,
+src/algos/ep/model.rs:257-278 with src/algos/utils.rs:193-216)."""
 import math
 
 import numpy as np
@@ -11,10 +12,12 @@ from tests._cases import random_problem, sample_batch
 pytestmark = pytest.mark.gpu
 
 
-def _ctx(prob, form=_native.FORM_PLAIN_FP32, noise=0.0, passes=1, batch_size=64):
+def _ctx(prob, form=_native.FORM_PLAIN_FP32, noise=0.0, passes=1, batch_size=64, max_features=None):
     cfg = _native.default_config()
     cfg.dims, cfg.loss, cfg.gamma, cfg.negatives = prob["dims"], _native.LOSS_STARSPACE, 0.5, 4
     cfg.form, cfg.noise, cfg.passes, cfg.batch_size, cfg.valid_pct = form, noise, passes, batch_size, 0.0
+    if max_features is not None:
+        cfg.max_features_kind, cfg.max_features = max_features
     ctx = _native.Context(cfg)
     ctx.upload_graph(prob["rows"], prob["cols"], None)
     ctx.upload_features(prob["fptr"], prob["fids"], prob["n_feat"])
@@ -61,3 +64,66 @@ def test_noise_is_applied_to_the_update():
     again = _ctx(prob, noise=1e3)
     again.batch_step(s, lr, 1)
     assert np.array_equal(again.get_table(prob["n_feat"], prob["dims"]), t_noisy)   # same stream, same result
+
+
+def _grad(ctx, prob, smp):
+    s = _native.Context.samples(smp["anchors"], smp["nbr_ptr"], smp["nbr"], smp["nbr_w"], smp["neg"])
+    return ctx.batch_grad(s, prob["n_feat"], prob["dims"])
+
+
+def test_feature_dropout_fixed_k_at_least_n_is_no_dropout():
+    # Fixed(k) with k >= every node's feature count keeps everything with
+    # scalar n / n = 1: the same weights as All, bit for bit
+    prob = random_problem(21, n=300, n_feat=200, dims=64, feats=(1, 6))
+    smp = sample_batch(22, prob, B=96, K=5, R=4)
+    a = _grad(_ctx(prob), prob, smp)
+    b = _grad(_ctx(prob, max_features=(_native.SAMPLE_FIXED, 6.0)), prob, smp)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_feature_dropout_item_counts():
+    prob = random_problem(23, n=2000, n_feat=500, dims=32, feats=(1, 8))
+    full = _ctx(prob).train_batches(4)
+    one = _ctx(prob, max_features=(_native.SAMPLE_FIXED, 1.0)).train_batches(4)
+    # Fixed(1): one item per role node (every node has a feature)
+    assert one["items"] == one["anchors"] * (1 + 4) + one["sampled_neighbors"]
+    half = _ctx(prob, max_features=(_native.SAMPLE_PROB, 0.5)).train_batches(4)
+    ratio = half["items"] / full["items"]
+    assert 0.45 < ratio < 0.65, ratio        # E[max(Bin(n, 1/2), 1)] / E[n] = 0.53 for n uniform in 1..8
+    for s in (one, half):
+        assert np.isfinite(s["train_loss"]) and s["kept_anchors"] > 0
+
+
+def test_feature_dropout_gradient_touches_a_subset():
+    prob = random_problem(25, n=300, n_feat=200, dims=32, feats=(2, 8))
+    smp = sample_batch(26, prob, B=96, K=5, R=4)
+    _, _, ids_all, _ = _grad(_ctx(prob), prob, smp)
+    _, st, ids, rows = _grad(_ctx(prob, max_features=(_native.SAMPLE_FIXED, 2.0)), prob, smp)
+    assert set(ids.tolist()) < set(ids_all.tolist())
+    assert np.isfinite(rows).all() and (st == 0).any()
+
+
+def test_feature_dropout_recall_matches_cpu_reference(oracle):
+    # both sides train with Fixed(3) feature dropout (their own random
+    # streams); community recall@10 within 1 point, as for the default path
+    import cloverleaf_gb300 as cl
+    from cloverleaf_gb300 import datagen
+    from tests._eval import community_recall
+    w = datagen.workload("sbm10k")
+    ep = w["ep"]
+    g = cl.Graph.from_csr(w["rows"], w["cols"], w["weights"])
+    fs = cl.FeatureSet.from_csr(g, w["fptr"], w["fids"], w["n_feat"])
+    prop = cl.EmbeddingPropagator(alpha=ep["alpha"], loss=cl.EPLoss.starspace(ep["gamma"], ep["negatives"]),
+                                  batch_size=ep["batch_size"], dims=ep["dims"], passes=ep["passes"],
+                                  max_nodes=ep["max_nodes"], max_features=3, valid_pct=0.0, indicator=False,
+                                  form="fused")
+    emb = prop.learn_features(g, fs)
+    r_gpu = community_recall(w["fptr"], w["fids"], emb.table, w["community"])
+    table, _ = oracle.train(w["rows"], w["cols"], w["weights"], w["fptr"], w["fids"], w["n_feat"], dims=ep["dims"],
+                            alpha=ep["alpha"], loss=oracle.LOSS_STARSPACE, gamma=ep["gamma"],
+                            negatives=ep["negatives"], batch_size=ep["batch_size"], passes=ep["passes"],
+                            max_nodes=(oracle.SAMPLE_FIXED, ep["max_nodes"]),
+                            max_features=(oracle.SAMPLE_FIXED, 3.0), threads=0)
+    r_cpu = community_recall(w["fptr"], w["fids"], table, w["community"])
+    assert abs(r_gpu - r_cpu) <= 0.01, (r_gpu, r_cpu)

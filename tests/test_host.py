@@ -47,7 +47,12 @@ def test_create_rejects_bad_config(native):
         _native.Context(cfg)
     assert e.value.code == -1
     cfg = _native.default_config()
-    cfg.max_features_kind, cfg.max_features = _native.SAMPLE_FIXED, 3
+    cfg.max_features_kind, cfg.max_features = _native.SAMPLE_PROB, 1.5
+    with pytest.raises(_native.NativeError) as e:
+        _native.Context(cfg)
+    assert e.value.code == -1
+    cfg = _native.default_config()
+    cfg.hard_negatives = 2
     with pytest.raises(_native.UnsupportedOption):
         _native.Context(cfg)
 
