@@ -139,6 +139,7 @@ SIGNATURES = {
     "ep_get_table": (ctypes.c_int, [_P, _P]),
     "ep_get_table_static": (ctypes.c_int, [_P, _U64, _U64, _P]),
     "ep_get_tuning": (ctypes.c_int, [_P, _P, _P, _P]),
+    "ep_sample": (ctypes.c_int, [_P, _P, _U32, _U32, _U32, _P, _P, _P, _P]),
     "ep_ag_forward": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), ctypes.c_int, _P, _P, _P]),
     "ep_ag_backward": (ctypes.c_int, [_P, _P, _P, _P]),
     "ep_synchronize": (ctypes.c_int, [_P]),
@@ -232,6 +233,19 @@ class Context:
     def set_table(self, table=None):
         t = None if table is None else np.ascontiguousarray(table, np.float32)
         check(lib().ep_set_table(self._h, ptr(t)), self._h, "ep_set_table")
+
+    def sample(self, anchors, step, stride):
+        """Device sampler output for given anchors: (nbr_cnt, nbr[n, stride],
+        nbr_w[n, stride], neg[n, R])."""
+        anchors = np.ascontiguousarray(anchors, np.uint32)
+        n = len(anchors)
+        cnt = np.zeros(n, np.uint32)
+        nbr = np.zeros((n, stride), np.uint32)
+        w = np.zeros((n, stride), np.float32)
+        neg = np.zeros((n, self.cfg.negatives), np.uint32)
+        check(lib().ep_sample(self._h, ptr(anchors), n, int(step), int(stride), ptr(cnt), ptr(nbr), ptr(w), ptr(neg)),
+              self._h, "ep_sample")
+        return cnt, nbr, w, neg
 
     def tuning(self):
         """(tuned, chunk, fused_mode, graph_batches) of this context."""

@@ -186,7 +186,6 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
         g_create_err = "probability max_features must be in (0, 1)";
         return EP_ERR_INVALID_ARG;
     }
-    if (cfg->hard_negatives != 0) { g_create_err = "hard negatives are not implemented on the GPU path"; return EP_ERR_UNSUPPORTED; }
     if (cfg->weighted_neighbor_sampling && cfg->weighted_neighbor_averaging) {
         g_create_err = "weighted neighbour sampling with weighted averaging is not implemented on the GPU path";
         return EP_ERR_UNSUPPORTED;
@@ -483,7 +482,7 @@ static float noise_decay(const ep_ctx* c) {
     return expf((logf(min_noise) - logf(c->cfg.noise)) / (float)c->total_steps);
 }
 
-static SampleParams sample_params(ep_ctx* c, BatchState* st, bool eval, bool injected) {
+static SampleParams sample_params(ep_ctx* c, BatchState* st, bool eval, int injected) {
     SampleParams sp{};
     sp.st = st;
     sp.cfg.nodes_kind = c->cfg.max_nodes_kind;
@@ -493,6 +492,7 @@ static SampleParams sample_params(ep_ctx* c, BatchState* st, bool eval, bool inj
     sp.cfg.R = c->R;
     sp.cfg.weighted_avg = c->cfg.weighted_neighbor_averaging;
     sp.cfg.fd = feat_drop(c);
+    sp.cfg.hard = c->cfg.hard_negatives;
     sp.cfg.seed = c->cfg.seed;
     sp.row_ptr = c->row.as<uint64_t>();
     sp.cols = c->cols.as<uint32_t>();
@@ -980,6 +980,49 @@ static int run_injected(ep_ctx* c, uint32_t B, int tt, const void* table, void* 
     CK(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s), "read state");
     CK(cudaStreamSynchronize(s), "injected batch");
     if (h.error) return c->fail(EP_ERR_DEVICE, "device error flags 0x%x", h.error);
+    return EP_OK;
+}
+
+extern "C" int ep_sample(ep_ctx* c, const uint32_t* anchors, uint32_t n, uint32_t step, uint32_t stride,
+                         uint32_t* nbr_cnt, uint32_t* nbr, float* nbr_w, uint32_t* neg) {
+    if (!c) return EP_ERR_INVALID_ARG;
+    if (n && (!anchors || !nbr_cnt || !nbr || !nbr_w || !neg)) return c->fail(EP_ERR_INVALID_ARG, "null array");
+    cudaSetDevice(c->device);
+    int rc = prepare_train(c);
+    if (rc) return rc;
+    if (n > c->Bcap) return c->fail(EP_ERR_INVALID_ARG, "%u anchors exceed the batch size %u", n, c->Bcap);
+    if (stride < c->Kcap)
+        return c->fail(EP_ERR_INVALID_ARG, "neighbour stride %u below the %u slots an anchor can fill", stride, c->Kcap);
+    for (uint32_t i = 0; i < n; ++i)
+        if (anchors[i] >= c->n_nodes) return c->fail(EP_ERR_INVALID_ARG, "anchor id out of range");
+    if (!n) return EP_OK;
+    BatchState h{};
+    h.pass = 1;
+    h.step = step;
+    h.n_anchors = n;
+    if (!c->st_inj.ensure(sizeof(BatchState))) return c->fail(EP_ERR_OOM, "state allocation failed");
+    BatchState* st = c->st_inj.as<BatchState>();
+    cudaStream_t s = c->stream;
+    CK(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s), "inject state");
+    CK(cudaMemcpyAsync(c->anchors.p, anchors, (size_t)n * 4, cudaMemcpyHostToDevice, s), "stage anchors");
+    launch_sample(sample_params(c, st, false, 2), s);
+    CK(cudaGetLastError(), "sample launch");
+    std::vector<uint32_t> hn((size_t)n * c->Kcap), hc(n);
+    std::vector<float> hw((size_t)n * c->Kcap);
+    CK(cudaMemcpyAsync(hc.data(), c->nbr_cnt.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s), "read samples");
+    CK(cudaMemcpyAsync(hn.data(), c->nbr.p, hn.size() * 4, cudaMemcpyDeviceToHost, s), "read samples");
+    CK(cudaMemcpyAsync(hw.data(), c->nbr_w.p, hw.size() * 4, cudaMemcpyDeviceToHost, s), "read samples");
+    CK(cudaMemcpyAsync(neg, c->neg.p, (size_t)n * c->R * 4, cudaMemcpyDeviceToHost, s), "read samples");
+    CK(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s), "read state");
+    CK(cudaStreamSynchronize(s), "sample");
+    if (h.error) return c->fail(EP_ERR_DEVICE, "device error flags 0x%x", h.error);
+    for (uint32_t a = 0; a < n; ++a) {
+        nbr_cnt[a] = hc[a];
+        for (uint32_t k = 0; k < hc[a]; ++k) {
+            nbr[(size_t)a * stride + k] = hn[(size_t)a * c->Kcap + k];
+            nbr_w[(size_t)a * stride + k] = hw[(size_t)a * c->Kcap + k];
+        }
+    }
     return EP_OK;
 }
 

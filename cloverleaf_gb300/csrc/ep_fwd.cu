@@ -192,19 +192,23 @@ __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
     const SampleCfg& c = p.cfg;
     const uint32_t salt = p.eval ? 0xffffffffu : (uint32_t)st->step;
     uint32_t v;
-    if (p.injected) {
+    if (p.injected == 1) {
         v = p.anchors[a];
     } else {
-        const uint32_t pos = st->b0 + a;
-        uint32_t idx = pos;
-        if (!p.eval) {
-            uint32_t k[4];
-            u32x4 kk = philox(u32x4{st->pass, 0x9e3779b9u, 0x7f4a7c15u, 0x1234567u}, c.seed);
-            k[0] = kk.x; k[1] = kk.y; k[2] = kk.z; k[3] = kk.w;
-            idx = permute(pos, p.n_order, p.feistel_half, k, &st->error);
+        if (p.injected == 2) {
+            v = p.anchors[a];
+        } else {
+            const uint32_t pos = st->b0 + a;
+            uint32_t idx = pos;
+            if (!p.eval) {
+                uint32_t k[4];
+                u32x4 kk = philox(u32x4{st->pass, 0x9e3779b9u, 0x7f4a7c15u, 0x1234567u}, c.seed);
+                k[0] = kk.x; k[1] = kk.y; k[2] = kk.z; k[3] = kk.w;
+                idx = permute(pos, p.n_order, p.feistel_half, k, &st->error);
+            }
+            v = p.order[idx];
+            if (lane == 0) p.anchors[a] = v;
         }
-        v = p.order[idx];
-        if (lane == 0) p.anchors[a] = v;
 
         // --- neighbours (reconstruct_node_embedding, model.rs:342-386) ---
         const uint64_t rs = p.row_ptr[v];
@@ -308,9 +312,62 @@ __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
             outw[q] = w;
         }
         if (lane == 0) p.nbr_cnt[a] = cnt;
-        // --- negatives: uniform over the pool, with replacement ---
-        for (uint32_t i = lane; i < c.R; i += 32)
-            p.neg[(uint64_t)a * c.R + i] = p.pool[below(rand_u32(c.seed, v, salt, ST_NEG, i), p.n_pool)];
+        // --- negatives: first up to min(hard, R) hard negatives, the end nodes
+        // of random walks from the anchor (RandomWalkHardSampler,
+        // node_sampler.rs:83-145), then uniform over the pool, with replacement
+        uint32_t* negs = p.neg + (uint64_t)a * c.R;
+        uint32_t nh = 0;
+        const uint32_t H = min(c.hard, c.R);
+        if (H) {
+            const uint32_t walks = 2 * H;
+            const uint64_t ae = rs + deg;
+            for (uint32_t w0 = 0; w0 < walks && nh < H; w0 += 32) {
+                const uint32_t t = w0 + lane;
+                uint32_t node = v;
+                bool ok = false;
+                if (t < walks) {
+                    // restart probability 0.25 after the second step, at most
+                    // 10 moves (random_walk, node_sampler.rs:109-145)
+                    for (uint32_t i = 1; i <= 11; ++i) {
+                        const uint64_t ns = p.row_ptr[node];
+                        const uint32_t nd = (uint32_t)(p.row_ptr[node + 1] - ns);
+                        if (nd == 0 || i > 10) break;
+                        node = p.cols[ns + below(rand_u32(c.seed, v, salt, ST_HARD, t * 32 + 2 * i), nd)];
+                        if (i > 1 && node != v && unit_f32(rand_u32(c.seed, v, salt, ST_HARD, t * 32 + 2 * i + 1)) < 0.25f)
+                            break;
+                    }
+                    ok = node != v;
+                }
+                // not one of the anchor's neighbours: the warp scans the row,
+                // each lane tests its own end node
+                bool hit = false;
+                for (uint64_t b = rs; b < ae; b += 32) {
+                    const uint32_t x = b + lane < ae ? p.cols[b + lane] : 0u;
+                    const uint32_t m = (uint32_t)min((uint64_t)32, ae - b);
+                    for (uint32_t s2 = 0; s2 < m; ++s2) {
+                        const uint32_t y = __shfl_sync(FULL, x, s2);   // every lane takes part
+                        hit = hit || y == node;
+                    }
+                }
+                ok = ok && !hit;
+                // keep the first occurrence among valid end nodes, in walk order
+                bool dup = false;
+                for (int s2 = 0; s2 < 32; ++s2) {
+                    const uint32_t ns2 = __shfl_sync(FULL, node, s2);
+                    const bool ok2 = __shfl_sync(FULL, ok, s2);
+                    dup = dup || (s2 < lane && ok2 && ns2 == node);
+                }
+                for (uint32_t k2 = 0; k2 < nh; ++k2) dup = dup || negs[k2] == node;
+                const bool acc = ok && !dup;
+                const unsigned am = __ballot_sync(FULL, acc);
+                const uint32_t rank = __popc(am & ((1u << lane) - 1u));
+                if (acc && nh + rank < H) negs[nh + rank] = node;
+                __syncwarp();
+                nh = min(H, nh + (uint32_t)__popc(am));
+            }
+        }
+        for (uint32_t i = nh + lane; i < c.R; i += 32)
+            negs[i] = p.pool[below(rand_u32(c.seed, v, salt, ST_NEG, i), p.n_pool)];
         __syncwarp();
     }
     // --- item count of this anchor: kept feature counts over its roles ---

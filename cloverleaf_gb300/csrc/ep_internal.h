@@ -77,6 +77,7 @@ struct SampleCfg {
     uint32_t R;             // negatives
     int weighted_avg;       // weighted_neighbor_averaging
     FeatDrop fd;            // feature dropout of every role node
+    uint32_t hard;          // hard negatives from random walks (0 = off)
     uint64_t seed;
 };
 
@@ -92,7 +93,8 @@ struct SampleParams {
     const uint32_t* pool;   // negative pool (train or valid ids)
     uint32_t n_pool;
     uint32_t batch_cap;     // anchors per batch
-    int injected;           // samples provided by the host: only count
+    int injected;           // 1: samples provided by the host (only count);
+                            // 2: anchors provided, neighbours and negatives sampled
     int eval;               // validation: fixed sampling stream, no shuffle
     uint32_t feistel_half;  // half-width in bits of the permutation domain
     uint32_t feistel_key[4];

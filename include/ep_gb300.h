@@ -186,6 +186,16 @@ int ep_profile_batches(ep_ctx* ctx, uint32_t n_batches, double* stage_ms, ep_pas
  * current table, without updating it (mod.rs:183-233 for one batch). */
 int ep_batch_grad(ep_ctx* ctx, const ep_batch_samples* samples, ep_sparse_grad* out);
 
+/* Inspection hook (no counterpart in the reference): runs the device sampler
+ * for n given anchors (n <= batch_size) at optimizer step `step` (the
+ * sampler's random streams are keyed by anchor and step): anchor a's sampled
+ * neighbours go to nbr[a*stride .. a*stride + nbr_cnt[a]) with their weights
+ * in nbr_w, its negatives (hard ones first, then uniform) to
+ * neg[a*R .. a*R + R).  stride must be at least the neighbours an anchor can
+ * take (min(max_nodes, max degree) for Fixed, the max degree otherwise). */
+int ep_sample(ep_ctx* ctx, const uint32_t* anchors, uint32_t n, uint32_t step, uint32_t stride,
+              uint32_t* nbr_cnt, uint32_t* nbr, float* nbr_w, uint32_t* neg);
+
 /* Parity hook: one full optimizer step for explicit samples with learning
  * rate lr and Adam time pass+1 (optimizer.rs:43-81). */
 int ep_batch_step(ep_ctx* ctx, const ep_batch_samples* samples, float lr, uint32_t pass);

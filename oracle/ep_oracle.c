@@ -363,6 +363,27 @@ static void collect_node(fmap_t* m, const uint64_t* fptr, const uint32_t* fids, 
     free(idx);
 }
 
+/* random_walk (node_sampler.rs:109-145): from the anchor, uniform neighbour
+ * steps; after the second step each step ends the walk with probability p
+ * when off the anchor; at most max_steps steps.  Yields the end node when it
+ * is neither the anchor nor one of the anchor's neighbours. */
+static int random_walk(uint32_t anchor, const uint64_t* rows, const uint32_t* cols, rng_t* r, float p,
+                       uint32_t max_steps, uint32_t* out) {
+    uint32_t node = anchor;
+    for (uint32_t i = 1;; ++i) {
+        const uint64_t s = rows[node], n = rows[(uint64_t)node + 1] - s;
+        if (n == 0 || i > max_steps) break;
+        node = cols[s + rng_below(r, n)];
+        if (i > 1 && rng_f32(r) < p && node != anchor) break;
+    }
+    if (node == anchor) return 0;
+    const uint64_t as = rows[anchor], an = rows[(uint64_t)anchor + 1] - as;
+    for (uint64_t j = 0; j < an; ++j)
+        if (cols[as + j] == node) return 0;
+    *out = node;
+    return 1;
+}
+
 /* run_forward_pass (mod.rs:289-327) building the role maps for anchor v. */
 static void build_roles(uint32_t v, const uint64_t* rows, const uint32_t* cols,
                         const uint64_t* fptr, const uint32_t* fids,
@@ -392,9 +413,21 @@ static void build_roles(uint32_t v, const uint64_t* rows, const uint32_t* cols,
         }
         for (uint64_t j = 0; j < filled; ++j) collect_node(&s->maps[1], fptr, fids, s->idx[j], sw, cfg, r, s);
     }
-    /* negatives: uniform over the pool (node_sampler.rs:243-246) */
+    /* negatives (RandomWalkHardSampler, node_sampler.rs:83-107): up to
+     * min(hard, R) distinct walk end nodes from 2 * that many walks, then
+     * uniform over the pool */
     uint32_t negs[4096];
-    for (uint32_t i = 0; i < R; ++i) negs[i] = neg_pool[rng_below(r, neg_pool_n)];
+    uint32_t nneg = 0;
+    const uint32_t H = cfg->hard_negatives < R ? cfg->hard_negatives : R;
+    for (uint32_t t = 0; t < 2 * H && nneg < H; ++t) {
+        uint32_t u;
+        if (random_walk(v, rows, cols, r, 0.25f, 10, &u)) {
+            int dup = 0;
+            for (uint32_t k = 0; k < nneg; ++k) dup |= negs[k] == u;
+            if (!dup) negs[nneg++] = u;
+        }
+    }
+    while (nneg < R) negs[nneg++] = neg_pool[rng_below(r, neg_pool_n)];
     for (uint32_t i = 0; i < R; ++i) collect_node(&s->maps[2 + i], fptr, fids, negs[i], 1.f, cfg, r, s);
 }
 

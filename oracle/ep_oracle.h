@@ -105,6 +105,7 @@ typedef struct orc_train_cfg {
     float valid_pct;
     int32_t threads;        /* OpenMP threads, <= 0 means all */
     uint64_t max_batches;   /* stop after this many batches in total (0 = all) */
+    uint32_t hard_negatives; /* random-walk negatives per anchor (node_sampler.rs:83-145) */
 } orc_train_cfg;
 
 typedef struct orc_train_stats {

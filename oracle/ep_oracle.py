@@ -78,6 +78,7 @@ class TrainCfg(ctypes.Structure):
         ("valid_pct", ctypes.c_float),
         ("threads", ctypes.c_int32),
         ("max_batches", ctypes.c_uint64),
+        ("hard_negatives", ctypes.c_uint32),
     ]
 
 
@@ -204,7 +205,7 @@ def adam(table, m, v, grad, touched, lr, pass_idx):
 def train(rows, cols, wcdf, fptr, fids, n_feat, *, dims, alpha, loss=LOSS_STARSPACE, gamma=0.5,
           neg_margin=0.0, negatives=5, batch_size=256, passes=5, seed=20222022,
           max_nodes=(SAMPLE_ALL, 0.0), max_features=(SAMPLE_ALL, 0.0), valid_pct=0.0,
-          loss_weighting=LW_NONE, lw_exp=1.0, threads=0, max_batches=0, init_table=None):
+          loss_weighting=LW_NONE, lw_exp=1.0, threads=0, max_batches=0, init_table=None, hard_negatives=0):
     """The whole reference training loop (mod.rs:92-287) on host cores.
     Returns (table[n_feat, dims], TrainStats)."""
     rows = _c(rows, np.uint64)
@@ -225,6 +226,7 @@ def train(rows, cols, wcdf, fptr, fids, n_feat, *, dims, alpha, loss=LOSS_STARSP
     cfg.valid_pct = valid_pct
     cfg.threads = threads
     cfg.max_batches = max_batches
+    cfg.hard_negatives = hard_negatives
     if init_table is not None:
         table = _c(init_table, np.float32).copy()
         given = 1

@@ -127,3 +127,74 @@ def test_feature_dropout_recall_matches_cpu_reference(oracle):
                             max_features=(oracle.SAMPLE_FIXED, 3.0), threads=0)
     r_cpu = community_recall(w["fptr"], w["fids"], table, w["community"])
     assert abs(r_gpu - r_cpu) <= 0.01, (r_gpu, r_cpu)
+
+
+def _bfs(rows, cols, src, limit=10):
+    dist = {src: 0}
+    frontier = [src]
+    for d in range(1, limit + 1):
+        nxt = []
+        for u in frontier:
+            for x in cols[int(rows[u]):int(rows[u + 1])].tolist():
+                if x not in dist:
+                    dist[x] = d
+                    nxt.append(x)
+        frontier = nxt
+    return dist
+
+
+def test_hard_negatives_are_walk_ends_off_the_neighbourhood():
+    # RandomWalkHardSampler (node_sampler.rs:83-145): the first negatives are
+    # distinct end nodes of short restart walks, neither the anchor nor one
+    # of its neighbours; the rest are uniform over the training ids
+    prob = random_problem(31, n=4000, n_feat=300, dims=16, deg=(2, 4))
+    H, R, B = 3, 6, 256
+    cfg = _native.default_config()
+    cfg.dims, cfg.negatives, cfg.hard_negatives, cfg.batch_size, cfg.valid_pct = 16, R, H, B, 0.0
+    cfg.max_nodes_kind, cfg.max_nodes = _native.SAMPLE_FIXED, 3.0
+    ctx = _native.Context(cfg)
+    ctx.upload_graph(prob["rows"], prob["cols"], None)
+    ctx.upload_features(prob["fptr"], prob["fids"], prob["n_feat"])
+    ctx.set_table(None)
+    rows, cols = prob["rows"], prob["cols"]
+    stride = int(np.diff(rows).max())
+    anchors = np.arange(B, dtype=np.uint32) * 7
+    cnt, nbr, _, neg = ctx.sample(anchors, 5, stride)
+    again = ctx.sample(anchors, 5, stride)
+    assert all(np.array_equal(x, y) for x, y in zip((cnt, nbr, neg), (again[0], again[1], again[3])))
+    other = ctx.sample(anchors, 6, stride)
+    assert not np.array_equal(neg, other[3])
+    good, d_hard, d_uni = 0, [], []
+    for a, v in enumerate(anchors.tolist()):
+        nb = set(cols[int(rows[v]):int(rows[v + 1])].tolist())
+        dist = _bfs(rows, cols, v, 10)
+        hard = neg[a, :H].tolist()
+        ok = len(set(hard)) == H and all(u != v and u not in nb and u in dist for u in hard)
+        good += ok
+        if ok:
+            d_hard += [dist[u] for u in hard]
+            d_uni += [dist.get(u, 11) for u in neg[a, H:].tolist()]
+    assert good >= 0.9 * B, good
+    assert np.mean(d_hard) + 1.0 < np.mean(d_uni), (np.mean(d_hard), np.mean(d_uni))
+
+
+def test_hard_negatives_recall_matches_cpu_reference(oracle):
+    import cloverleaf_gb300 as cl
+    from cloverleaf_gb300 import datagen
+    from tests._eval import community_recall
+    w = datagen.workload("sbm10k")
+    ep = w["ep"]
+    g = cl.Graph.from_csr(w["rows"], w["cols"], w["weights"])
+    fs = cl.FeatureSet.from_csr(g, w["fptr"], w["fids"], w["n_feat"])
+    prop = cl.EmbeddingPropagator(alpha=ep["alpha"], loss=cl.EPLoss.starspace(ep["gamma"], ep["negatives"]),
+                                  batch_size=ep["batch_size"], dims=ep["dims"], passes=ep["passes"],
+                                  max_nodes=ep["max_nodes"], hard_negatives=2, valid_pct=0.0, indicator=False,
+                                  form="fused")
+    emb = prop.learn_features(g, fs)
+    r_gpu = community_recall(w["fptr"], w["fids"], emb.table, w["community"])
+    table, _ = oracle.train(w["rows"], w["cols"], w["weights"], w["fptr"], w["fids"], w["n_feat"], dims=ep["dims"],
+                            alpha=ep["alpha"], loss=oracle.LOSS_STARSPACE, gamma=ep["gamma"],
+                            negatives=ep["negatives"], batch_size=ep["batch_size"], passes=ep["passes"],
+                            max_nodes=(oracle.SAMPLE_FIXED, ep["max_nodes"]), hard_negatives=2, threads=0)
+    r_cpu = community_recall(w["fptr"], w["fids"], table, w["community"])
+    assert abs(r_gpu - r_cpu) <= 0.01, (r_gpu, r_cpu)

@@ -52,7 +52,7 @@ def test_create_rejects_bad_config(native):
         _native.Context(cfg)
     assert e.value.code == -1
     cfg = _native.default_config()
-    cfg.hard_negatives = 2
+    cfg.weighted_neighbor_sampling = cfg.weighted_neighbor_averaging = 1
     with pytest.raises(_native.UnsupportedOption):
         _native.Context(cfg)
 
