@@ -186,8 +186,9 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
         g_create_err = "probability max_features must be in (0, 1)";
         return EP_ERR_INVALID_ARG;
     }
-    if (cfg->weighted_neighbor_sampling && cfg->weighted_neighbor_averaging) {
-        g_create_err = "weighted neighbour sampling with weighted averaging is not implemented on the GPU path";
+    if (cfg->weighted_neighbor_sampling && cfg->weighted_neighbor_averaging &&
+        (cfg->max_nodes_kind == EP_SAMPLE_PROB || (cfg->max_nodes_kind == EP_SAMPLE_FIXED && cfg->max_nodes > 32.f))) {
+        g_create_err = "weighted neighbour sampling with weighted averaging is implemented for max_nodes <= 32 (Fixed) or all";
         return EP_ERR_UNSUPPORTED;
     }
     int ndev = 0;
@@ -491,6 +492,7 @@ static SampleParams sample_params(ep_ctx* c, BatchState* st, bool eval, int inje
     sp.cfg.Kcap = c->buf_K;
     sp.cfg.R = c->R;
     sp.cfg.weighted_avg = c->cfg.weighted_neighbor_averaging;
+    sp.cfg.weighted_sampling = c->cfg.weighted_neighbor_sampling;
     sp.cfg.fd = feat_drop(c);
     sp.cfg.hard = c->cfg.hard_negatives;
     sp.cfg.seed = c->cfg.seed;

@@ -225,6 +225,53 @@ __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
             sw = (float)deg / (float)r;
             if (r == deg) {
                 take_all = 1;
+            } else if (c.weighted_sampling && c.weighted_avg && p.wcdf && r <= 32) {
+                // weighted_reservoir_sample (utils.rs:147-161) with the
+                // averaging weights w_i = scale * p_i * deg: the r positions
+                // with the largest U_i^(1/w_i) (Efraimidis-Spirakis A-Res),
+                // compared as log(U_i) / w_i.  Lane t < r holds one member of
+                // the running set; 32 candidates at a time enter while they
+                // beat the set's smallest key.
+                auto key = [&](uint32_t i) -> float {
+                    const float pi = p.wcdf[rs + i] - (i ? p.wcdf[rs + i - 1] : 0.f);
+                    const float wi = sw * pi * (float)deg;
+                    const float u = ((float)(rand_u32(c.seed, v, salt, ST_WRES, i) >> 8) + 0.5f) * (1.0f / 16777216.0f);
+                    return wi > 0.f ? __logf(u) / wi : -INFINITY;
+                };
+                float skey = -INFINITY;
+                uint32_t spos = 0xffffffffu;
+                if ((uint32_t)lane < r) { spos = (uint32_t)lane; skey = key(lane); }
+                for (uint32_t base = r; base < deg; base += 32) {
+                    const uint32_t i = base + lane;
+                    float ck = i < deg ? key(i) : -INFINITY;
+                    for (uint32_t guard = 0; guard <= 32; ++guard) {
+                        // the set's smallest key and the lane holding it
+                        float mk = (uint32_t)lane < r ? skey : INFINITY;
+                        int ml = lane;
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) {
+                            const float ok2 = __shfl_xor_sync(FULL, mk, o);
+                            const int ol = __shfl_xor_sync(FULL, ml, o);
+                            if (ok2 < mk || (ok2 == mk && ol < ml)) { mk = ok2; ml = ol; }
+                        }
+                        const bool better = ck > mk;
+                        if (!__ballot_sync(FULL, better)) break;
+                        // the best candidate replaces the smallest member
+                        float bk = better ? ck : -INFINITY;
+                        int bl = lane;
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) {
+                            const float ok2 = __shfl_xor_sync(FULL, bk, o);
+                            const int ol = __shfl_xor_sync(FULL, bl, o);
+                            if (ok2 > bk || (ok2 == bk && ol < bl)) { bk = ok2; bl = ol; }
+                        }
+                        const uint32_t bpos = __shfl_sync(FULL, i, bl);
+                        if (lane == ml) { skey = bk; spos = bpos; }
+                        if (lane == bl) ck = -INFINITY;
+                    }
+                }
+                if ((uint32_t)lane < r) { out[lane] = p.cols[rs + spos]; outw[lane] = __uint_as_float(spos); }
+                cnt = r;
             } else if (r <= 32) {
                 // Floyd's algorithm: a uniform r-subset of [0, deg); lane i
                 // holds the i-th chosen position.

@@ -76,6 +76,7 @@ struct SampleCfg {
     uint32_t Kcap;          // neighbour slots per anchor
     uint32_t R;             // negatives
     int weighted_avg;       // weighted_neighbor_averaging
+    int weighted_sampling;  // weighted_neighbor_sampling (with weighted averaging: A-Res)
     FeatDrop fd;            // feature dropout of every role node
     uint32_t hard;          // hard negatives from random walks (0 = off)
     uint64_t seed;

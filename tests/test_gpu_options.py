@@ -198,3 +198,52 @@ def test_hard_negatives_recall_matches_cpu_reference(oracle):
                             max_nodes=(oracle.SAMPLE_FIXED, ep["max_nodes"]), hard_negatives=2, threads=0)
     r_cpu = community_recall(w["fptr"], w["fids"], table, w["community"])
     assert abs(r_gpu - r_cpu) <= 0.01, (r_gpu, r_cpu)
+
+
+def test_weighted_sampling_matches_a_res_inclusion_probabilities():
+    # weighted_neighbor_sampling + weighted_neighbor_averaging: the sampled
+    # neighbours are weighted_reservoir_sample (utils.rs:147-161) by the
+    # averaging weights.  256 anchors share the same 40 neighbours with
+    # weights (j+1)^2; K = 5.  The device's inclusion frequency of each
+    # neighbour over 2048 samples matches a numpy Monte-Carlo of the same
+    # A-Res rule (keys U^(1/w), the K largest kept).
+    A, D, K = 256, 40, 5
+    n = A + D
+    rows = np.zeros(n + 1, np.uint64)
+    rows[1:A + 1] = np.arange(1, A + 1) * D
+    rows[A + 1:] = A * D
+    cols = np.tile(np.arange(A, A + D, dtype=np.uint32), A)
+    wts = np.tile(((np.arange(D) + 1.0) ** 2).astype(np.float32), A)
+    wcdf = _native.cdf_convert(rows, wts.copy())
+    fptr = np.arange(n + 1, dtype=np.uint64)
+    fids = (np.arange(n) % 50).astype(np.uint32)
+    cfg = _native.default_config()
+    cfg.dims, cfg.negatives, cfg.batch_size, cfg.valid_pct = 16, 2, A, 0.0
+    cfg.max_nodes_kind, cfg.max_nodes = _native.SAMPLE_FIXED, float(K)
+    cfg.weighted_neighbor_sampling = cfg.weighted_neighbor_averaging = 1
+    ctx = _native.Context(cfg)
+    ctx.upload_graph(rows, cols, wcdf)
+    ctx.upload_features(fptr, fids, 50)
+    ctx.set_table(None)
+    counts = np.zeros(D)
+    anchors = np.arange(A, dtype=np.uint32)
+    for step in range(1, 9):
+        cnt, nbr, w, _ = ctx.sample(anchors, step, D)
+        assert (cnt == K).all()
+        for a in range(A):
+            got = nbr[a, :K].astype(np.int64) - A
+            assert len(set(got.tolist())) == K
+            counts[got] += 1
+            # weights are the averaging weights scale * p_i * deg
+            p = ((got + 1.0) ** 2) / ((np.arange(D) + 1.0) ** 2).sum()
+            assert np.allclose(w[a, :K], (D / K) * p * D, rtol=1e-4)   # p from float32 CDF differences
+    freq = counts / (8 * A)
+    rng = np.random.default_rng(0)
+    u = rng.random((100000, D))
+    keys = u ** (1.0 / ((np.arange(D) + 1.0) ** 2))
+    top = np.argsort(-keys, axis=1)[:, :K]
+    want = np.bincount(top.ravel(), minlength=D) / 100000
+    assert np.abs(freq - want).max() < 0.045, np.abs(freq - want).max()
+    # far from uniform (K / D each): the heaviest 2.7x, the lightest rarely
+    assert freq[-1] > 2 * K / D and want[-1] > 2 * K / D
+    assert freq[0] < 0.25 * K / D

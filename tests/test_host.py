@@ -53,6 +53,7 @@ def test_create_rejects_bad_config(native):
     assert e.value.code == -1
     cfg = _native.default_config()
     cfg.weighted_neighbor_sampling = cfg.weighted_neighbor_averaging = 1
+    cfg.max_nodes_kind, cfg.max_nodes = _native.SAMPLE_PROB, 0.5
     with pytest.raises(_native.UnsupportedOption):
         _native.Context(cfg)
 
