@@ -19,7 +19,7 @@ OBJ_DIR = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libep_gb300.so")
 
-CU_SOURCES = ("ep_fwd.cu", "ep_sort.cu", "ep_red.cu", "ep_ctx.cu")
+CU_SOURCES = ("ep_fwd.cu", "ep_sort.cu", "ep_red.cu", "ep_ctx.cu", "ep_knn.cu")
 CPP_SOURCES = ("ep_host.cpp",)
 HEADERS = ("ep_internal.h", "ep_device.cuh", "ep_launch.cuh")
 

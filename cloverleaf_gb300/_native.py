@@ -140,6 +140,9 @@ SIGNATURES = {
     "ep_get_table_static": (ctypes.c_int, [_P, _U64, _U64, _P]),
     "ep_get_tuning": (ctypes.c_int, [_P, _P, _P, _P]),
     "ep_sample": (ctypes.c_int, [_P, _P, _U32, _U32, _U32, _P, _P, _P, _P]),
+    "ep_embed_features": (ctypes.c_int, [ctypes.c_int, _U64, _P, _P, _P, _U32, _U32, _P, _P]),
+    "ep_knn_cosine": (ctypes.c_int, [ctypes.c_int, _U64, _U32, _P, _U64, _P, _P, _U32, _P, _P]),
+    "ep_knn_last_error": (ctypes.c_char_p, []),
     "ep_ag_forward": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), ctypes.c_int, _P, _P, _P]),
     "ep_ag_backward": (ctypes.c_int, [_P, _P, _P, _P]),
     "ep_synchronize": (ctypes.c_int, [_P]),
@@ -336,3 +339,36 @@ def cdf_convert(rows, w):
     w = np.ascontiguousarray(w, np.float32).copy()
     check(lib().ep_cdf_convert(len(rows) - 1, ptr(rows), ptr(w)), None, "ep_cdf_convert")
     return w
+
+
+def _knn_check(rc, what):
+    if rc != EP_OK:
+        msg = lib().ep_knn_last_error().decode(errors="replace")
+        raise NativeError(rc, f"{what}: {msg}")
+
+
+def embed_features(fptr, fids, table, weights=None, device=0):
+    """GPU NodeEmbedder: weighted mean of each node's feature rows
+    (``ep_embed_features``)."""
+    fptr = np.ascontiguousarray(fptr, np.uint64)
+    fids = np.ascontiguousarray(fids, np.uint32)
+    table = np.ascontiguousarray(table, np.float32)
+    w = None if weights is None else np.ascontiguousarray(weights, np.float32)
+    n = len(fptr) - 1
+    out = np.zeros((n, table.shape[1]), np.float32)
+    _knn_check(lib().ep_embed_features(int(device), n, ptr(fptr), ptr(fids), ptr(w), table.shape[0], table.shape[1],
+                                       ptr(table), ptr(out)), "ep_embed_features")
+    return out
+
+
+def knn_cosine(db, queries, k, q_self=None, device=0):
+    """Exact cosine top-k on the tensor cores (``ep_knn_cosine``):
+    (ids[n_q, k], similarities[n_q, k]) in decreasing similarity."""
+    db = np.ascontiguousarray(db, np.float32)
+    q = np.ascontiguousarray(queries, np.float32)
+    qs = None if q_self is None else np.ascontiguousarray(q_self, np.uint64)
+    idx = np.zeros((len(q), k), np.uint32)
+    sim = np.zeros((len(q), k), np.float32)
+    _knn_check(lib().ep_knn_cosine(int(device), len(db), db.shape[1], ptr(db), len(q), ptr(q), ptr(qs), int(k),
+                                   ptr(idx), ptr(sim)), "ep_knn_cosine")
+    return idx, sim

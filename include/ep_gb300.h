@@ -252,6 +252,31 @@ const char* ep_last_error(const ep_ctx* ctx);
 
 void ep_destroy(ep_ctx* ctx);
 
+/* ---- evaluation: node embeddings and nearest neighbours ---------------- */
+
+/* NodeEmbedder.embed_feature_set (src/lib.rs:2092-2124) with AvgAggregator
+ * (fweight NULL) or WeightedAggregator (fweight[f] = alpha / (alpha + p_f)),
+ * src/algos/aggregator.rs:17-120: out[v] (n_nodes x dims FP32) = the
+ * weighted mean of the table rows of v's features fids[fptr[v]..fptr[v+1])
+ * in f32 as the reference sums them; featureless nodes get zeros.  Host
+ * buffers; dims <= 512.  Errors: ep_knn_last_error(). */
+int ep_embed_features(int device, uint64_t n_nodes, const uint64_t* fptr, const uint32_t* fids,
+                      const float* fweight, uint32_t n_feat, uint32_t dims, const float* table, float* out);
+
+/* Exact cosine top-k of every query row against every database row
+ * (NodeEmbeddings.nearest_neighbor with EDist::Cosine, src/embeddings.rs:
+ * 149-173, for n_q queries at once).  Rows are normalised and rounded to
+ * BF16; similarities accumulate in FP32 on the tensor cores.  idx_out /
+ * sim_out (n_q x k) get the k most similar database rows per query in
+ * decreasing similarity; q_self (optional) names a database row to skip per
+ * query (~0 = none).  dims <= 256, k <= 32.  Host buffers. */
+int ep_knn_cosine(int device, uint64_t n_db, uint32_t dims, const float* db, uint64_t n_q, const float* q,
+                  const uint64_t* q_self, uint32_t k, uint32_t* idx_out, float* sim_out);
+
+/* Message of the last failing ep_embed_features / ep_knn_cosine call of this
+ * host thread. */
+const char* ep_knn_last_error(void);
+
 /* ---- host-side graph construction (src/graph.rs) --------------------- */
 
 /* CSR::construct_from_edges (src/graph.rs:70-142): optional deduplication

@@ -1,0 +1,96 @@
+"""GPU NodeEmbedder and exact cosine top-k (src/lib.rs:2092-2124,
+src/algos/aggregator.rs:17-120, src/embeddings.rs:149-173) through the C ABI.
+
+The embedder is compared bit for bit with a restatement of the reference's
+f32 arithmetic.  The top-k rounds unit rows to BF16 (FP32 accumulation), so
+it is checked against exact FP64 cosines up to that rounding: every returned
+row's exact similarity is within 0.02 of the exact k-th best, returned
+similarities within 0.02 of exact, and well separated neighbours exactly."""
+import numpy as np
+import pytest
+
+from cloverleaf_gb300 import _native
+
+pytestmark = pytest.mark.gpu
+TOL_BF16 = 0.02
+
+
+def _features(rng, n, n_feat, empty_every=7):
+    k = rng.integers(1, 9, n)
+    k[::empty_every] = 0
+    fptr = np.zeros(n + 1, np.uint64)
+    fptr[1:] = np.cumsum(k)
+    fids = rng.integers(0, n_feat, int(fptr[-1])).astype(np.uint32)
+    return fptr, fids
+
+
+def _ref_embed(fptr, fids, table, w):
+    n, d = len(fptr) - 1, table.shape[1]
+    out = np.zeros((n, d), np.float32)
+    for v in range(n):
+        b, e = int(fptr[v]), int(fptr[v + 1])
+        if b == e:
+            continue
+        acc = np.zeros(d, np.float32)
+        ws = np.float32(0)
+        for f in fids[b:e]:
+            wf = np.float32(1) if w is None else np.float32(w[f])
+            ws = np.float32(ws + wf)
+            acc = acc + (table[f] if w is None else wf * table[f])
+        out[v] = acc / ws
+    return out
+
+
+@pytest.mark.parametrize("dims", [64, 100])
+@pytest.mark.parametrize("weighted", [False, True])
+def test_embed_features_matches_reference_arithmetic(dims, weighted):
+    rng = np.random.default_rng(dims + weighted)
+    n, n_feat = 400, 250
+    fptr, fids = _features(rng, n, n_feat)
+    table = rng.standard_normal((n_feat, dims)).astype(np.float32)
+    w = None
+    if weighted:
+        p = rng.random(n_feat).astype(np.float32)
+        p /= p.sum()
+        w = (np.float32(1e-3) / (np.float32(1e-3) + p)).astype(np.float32)
+    got = _native.embed_features(fptr, fids, table, w)
+    assert np.array_equal(got, _ref_embed(fptr, fids, table, w))
+
+
+def _exact(db, q):
+    dn = db / np.maximum(np.linalg.norm(db, axis=1, keepdims=True), 1e-300)
+    qn = q / np.maximum(np.linalg.norm(q, axis=1, keepdims=True), 1e-300)
+    return qn.astype(np.float64) @ dn.astype(np.float64).T
+
+
+@pytest.mark.parametrize("dims,k", [(32, 10), (100, 16), (256, 10), (256, 32)])
+def test_knn_cosine_matches_exact_up_to_bf16(dims, k):
+    rng = np.random.default_rng(dims * 100 + k)
+    n_db, n_q = 1000, 300
+    db = rng.standard_normal((n_db, dims)).astype(np.float32)
+    q = db[:n_q].copy()
+    idx, sim = _native.knn_cosine(db, q, k, q_self=np.arange(n_q))
+    S = _exact(db, q)
+    S[np.arange(n_q), np.arange(n_q)] = -np.inf
+    kth = -np.sort(-S, axis=1)[:, k - 1]
+    assert (idx < n_db).all()
+    assert (idx != np.arange(n_q)[:, None]).all()
+    assert all(len(set(r)) == k for r in idx.tolist())
+    assert (np.diff(sim, axis=1) <= 0).all()
+    ex = S[np.arange(n_q)[:, None], idx.astype(np.int64)]
+    assert (ex >= kth[:, None] - TOL_BF16).all()
+    assert np.abs(ex - sim).max() < TOL_BF16
+    top = np.argsort(-S, axis=1)[:, :k]
+    overlap = np.mean([len(set(a) & set(b)) / k for a, b in zip(idx.tolist(), top.tolist())])
+    assert overlap > 0.9, overlap
+
+
+def test_knn_cosine_separated_clusters_exact():
+    # 40 tight clusters of 25 points: each point's 24 cluster mates are its
+    # 24 nearest rows by a wide margin
+    rng = np.random.default_rng(7)
+    c = rng.standard_normal((40, 64))
+    db = (np.repeat(c, 25, axis=0) + 0.01 * rng.standard_normal((1000, 64))).astype(np.float32)
+    idx, _ = _native.knn_cosine(db, db, 24, q_self=np.arange(1000))
+    want = np.arange(1000) // 25
+    assert (idx.astype(np.int64) // 25 == want[:, None]).all()
