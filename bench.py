@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-knn", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--profile-steps", type=int, default=100)
     return p.parse_args()
@@ -199,6 +200,25 @@ def load_traffic(workload):
             return json.load(f).get(workload)
     except Exception:
         return None
+
+
+def knn_leg(peak_tflops):
+    """Exact cosine top-10 on the tensor cores (ep_knn_cosine): 19,456
+    queries (128 per SM) against 262,144 rows of 256 dims.  GEMM FLOP =
+    2 * n_q * n_db * 256; time = the top-k kernel's CUDA-event time."""
+    from cloverleaf_gb300 import _native
+
+    rng = np.random.default_rng(11)
+    n_db, n_q, d, k = 262144, 19456, 256, 10
+    db = rng.standard_normal((n_db, d), dtype=np.float32)
+    q = db[:n_q]
+    _native.knn_cosine(db[:4096], q[:256], k)          # warm-up
+    _native.knn_cosine(db, q, k)
+    ms = float(_native.lib().ep_knn_last_kernel_ms())
+    tflops = 2.0 * n_q * n_db * d / (ms / 1e3) / 1e12
+    return {"kernel": "k_cos_topk (tcgen05, BF16 x BF16 -> FP32 TMEM, fused top-k)", "n_db": n_db, "n_q": n_q,
+            "dims": d, "k": k, "kernel_ms": ms, "tflops": tflops, "peak_bf16_tflops": peak_tflops,
+            "frac": tflops / peak_tflops if peak_tflops else None}
 
 
 def make_config(ep, form, loss, passes=1):
@@ -385,12 +405,23 @@ def main():
         log(f"[bench] cpu reference: {cv / 1e3:.1f} k nodes/s on {cores} threads")
 
     if rank == 0:
+        knn = None
+        if not args.no_knn:
+            try:
+                with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                    pk_bf16 = float(json.load(f)["bf16_tflops"])
+            except Exception:
+                pk_bf16 = 1900.0
+            knn = knn_leg(pk_bf16)
+            log(f"[bench] knn: {knn['tflops']:.1f} TFLOP/s ({knn['kernel_ms']:.2f} ms) = "
+                f"{100 * knn['frac']:.1f}% of {pk_bf16:.0f}")
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / max(st["batches"], 1), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(st["launches"]),
                 "clocks": clocks, "plain_fp32": plain,
-                "speedup_vs_cpu": (value / cpu["value"]) if cpu else None}
+                "speedup_vs_cpu": (value / cpu["value"]) if cpu else None,
+                "eval_knn": knn}
         print(json.dumps(line), flush=True)
     return 0
 

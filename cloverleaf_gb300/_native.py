@@ -143,6 +143,7 @@ SIGNATURES = {
     "ep_embed_features": (ctypes.c_int, [ctypes.c_int, _U64, _P, _P, _P, _U32, _U32, _P, _P]),
     "ep_knn_cosine": (ctypes.c_int, [ctypes.c_int, _U64, _U32, _P, _U64, _P, _P, _U32, _P, _P]),
     "ep_knn_last_error": (ctypes.c_char_p, []),
+    "ep_knn_last_kernel_ms": (ctypes.c_float, []),
     "ep_ag_forward": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), ctypes.c_int, _P, _P, _P]),
     "ep_ag_backward": (ctypes.c_int, [_P, _P, _P, _P]),
     "ep_synchronize": (ctypes.c_int, [_P]),

@@ -26,6 +26,7 @@ namespace ep {
 namespace {
 
 thread_local std::string g_knn_err;
+thread_local float g_knn_ms = 0.f;     // CUDA-event time of the last top-k kernel
 
 int knn_fail(int code, const char* msg) {
     g_knn_err = msg;
@@ -84,36 +85,61 @@ __global__ void __launch_bounds__(256) k_embed(uint64_t n, const uint64_t* __res
     }
 }
 
-// Rows scaled to unit L2 norm (zero rows stay zero), as BF16 padded to dpad.
-__global__ void __launch_bounds__(256) k_norm_bf16(uint64_t n, uint32_t d, uint32_t dpad, const float* __restrict__ x,
-                                                   __nv_bfloat16* __restrict__ y) {
+// Rows scaled to unit L2 norm (zero rows stay zero), rounded to BF16 and
+// written straight into the tile image the tensor core reads (see below):
+// tiles of 2^tlog rows; per tile, per 64-element K block, 8-row atoms of
+// 1024 B in which the 16-byte chunk c of row r sits at chunk c ^ (r % 8).
+// Rows from n up to the tile boundary are written as zeros.
+__device__ __forceinline__ uint64_t swz_offset(uint64_t row, uint32_t k, uint32_t nkb, uint32_t tlog) {
+    const uint64_t tile = row >> tlog;
+    const uint32_t r = (uint32_t)row & ((1u << tlog) - 1u), kb = k >> 6, c = (k & 63u) >> 3, e = k & 7u;
+    const uint64_t kb_bytes = (uint64_t)128u << tlog;
+    return tile * nkb * kb_bytes + kb * kb_bytes + (r >> 3) * 1024u + (r & 7u) * 128u + ((c ^ (r & 7u)) << 4) + e * 2u;
+}
+
+__global__ void __launch_bounds__(256) k_norm_swz(uint64_t n, uint64_t n_tiled, uint32_t d, uint32_t dpad,
+                                                  uint32_t tlog, const float* __restrict__ x,
+                                                  unsigned char* __restrict__ y) {
     const int lane = threadIdx.x & 31;
     const uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (r >= n) return;
+    if (r >= n_tiled) return;
+    const bool in = r < n;
     float ss = 0.f;
-    for (uint32_t k = lane; k < d; k += 32) {
-        const float t = x[r * d + k];
-        ss += t * t;
-    }
+    if (in)
+        for (uint32_t k = lane; k < d; k += 32) {
+            const float t = x[r * d + k];
+            ss += t * t;
+        }
     ss = warp_sum<float>(ss);
     const float inv = ss > 0.f ? 1.f / sqrtf(ss) : 0.f;
-    for (uint32_t k = lane; k < dpad; k += 32) y[r * dpad + k] = __float2bfloat16_rn(k < d ? x[r * d + k] * inv : 0.f);
+    const uint32_t nkb = dpad / 64;
+    for (uint32_t k = lane; k < dpad; k += 32) {
+        const float v = (in && k < d) ? x[r * d + k] * inv : 0.f;
+        *reinterpret_cast<__nv_bfloat16*>(y + swz_offset(r, k, nkb, tlog)) = __float2bfloat16_rn(v);
+    }
 }
 
 // ---------------------------------------------------------------------------
-// Cosine top-k: one CTA (4 warps) per 128 queries.
+// Cosine top-k: one CTA per 128 queries, warp-specialised.
 //
-// Operand tiles live in shared memory in the K-major 128-byte-swizzled
-// layout the tensor core reads: per 64-element K block, rows of 128 B in
-// 8-row atoms of 1024 B; the 16-byte chunk c of row r sits at chunk position
-// c ^ (r % 8).  A (queries, M = 128) is loaded once; B (database rows,
-// N = 128) once per tile.  One thread issues the MMAs of a tile into a
-// 128 x 128 FP32 accumulator in tensor memory and commits them to an
-// mbarrier; then thread t of the CTA reads row t (its query) with tcgen05.ld
-// and merges the 128 similarities into its sorted top-KMAX in registers.
+// Producer warp (warp 8, one lane): copies the query tile (M = 128) and keeps
+// KNN_STAGES database tiles (N = 64 rows) in flight with cp.async.bulk from
+// their tile images (completion counted in bytes on mbarriers), and issues
+// each tile's MMAs (K = 16 per instruction, BF16 x BF16 -> FP32) into one of
+// KNN_STAGES 64-column accumulators in tensor memory, committed to an
+// mbarrier.  A buffer is refilled once the MMAs that read it have completed;
+// an accumulator is reused once the epilogue has released it.
+// Epilogue warps 0-7: warp w reads TMEM lane quarter w % 4 (lane = query row)
+// and the 32-column half w / 4 of each tile; each thread keeps a sorted
+// top-KMAX of its columns in registers, skipping 32-value blocks whose
+// maximum cannot enter; the two halves' lists are merged per query at the
+// end.  Operands sit in shared memory as K-major, 128-byte-swizzled tiles.
+// All waits are bounded; a timeout sets an abort flag that ends every role's
+// loop, and the error word.
 // ---------------------------------------------------------------------------
-constexpr int KNN_BM = 128, KNN_BN = 128, KNN_THREADS = 128;
-constexpr uint32_t KNN_TMEM_COLS = 128;
+constexpr int KNN_BM = 128, KNN_BN = 64, KNN_STAGES = 4;
+constexpr int KNN_EPI_WARPS = 8, KNN_THREADS = 32 * (KNN_EPI_WARPS + 1);
+constexpr uint32_t KNN_TMEM_COLS = KNN_BN * KNN_STAGES;    // 256
 constexpr uint32_t KNN_WAIT_LIMIT = 1u << 22;    // mbarrier polls (32 ns sleeps) before giving up
 enum : uint32_t { KNN_ERR_TIMEOUT = 1u };
 
@@ -135,29 +161,14 @@ __host__ __device__ constexpr uint32_t umma_idesc(uint32_t M, uint32_t N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
 
-// Stages rows [row0, row0 + nrows) of a [n x dpad] BF16 matrix (rows >= n
-// zero-filled) into the swizzled layout at s (1024-byte aligned).
-__device__ __forceinline__ void stage_rows(unsigned char* s, const __nv_bfloat16* __restrict__ g, uint64_t n,
-                                           uint64_t row0, int nrows, uint32_t dpad) {
-    const uint32_t chunks = dpad / 8;                  // 16-byte chunks per row
-    const uint32_t total = (uint32_t)nrows * chunks;
-    for (uint32_t i = threadIdx.x; i < total; i += KNN_THREADS) {
-        const uint32_t r = i / chunks, c = i % chunks;
-        const uint32_t kb = c / 8, cc = c % 8;
-        const uint32_t off = kb * (uint32_t)nrows * 128u + (r / 8) * 1024u + (r % 8) * 128u + ((cc ^ (r % 8)) * 16u);
-        const uint64_t row = row0 + r;
-        const bool in = row < n;
-        const void* src = in ? (const void*)(g + row * dpad + (uint64_t)c * 8) : (const void*)g;
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(s + off)), "l"(src),
-                     "r"(in ? 16 : 0)
-                     : "memory");
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
+__device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count) : "memory");
 }
 
 // Polls the mbarrier for the completion of the phase with the given parity:
-// at most KNN_WAIT_LIMIT polls, 32 ns apart.  Returns 1 when it completed.
-__device__ __forceinline__ uint32_t mbar_wait(uint64_t* mbar, uint32_t parity) {
+// at most KNN_WAIT_LIMIT polls, 32 ns apart, and none once *abort is set.
+// Returns 1 when the phase completed.
+__device__ __forceinline__ uint32_t mbar_wait(uint64_t* mbar, uint32_t parity, volatile uint32_t* abort) {
     uint32_t done = 0;
     for (uint32_t it = 0; it < KNN_WAIT_LIMIT; ++it) {
         asm volatile(
@@ -165,15 +176,54 @@ __device__ __forceinline__ uint32_t mbar_wait(uint64_t* mbar, uint32_t parity) {
             : "=r"(done)
             : "r"(smem_u32(mbar)), "r"(parity)
             : "memory");
-        if (done) break;
+        if (done || *abort) break;
         __nanosleep(32);
     }
     return done;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
+// One thread: `pieces` bulk copies of `bytes` each, from src + i * src_stride
+// to dst + i * bytes, all counted on mbar.
+__device__ __forceinline__ void bulk_load(unsigned char* dst, const unsigned char* src, uint32_t pieces,
+                                          uint32_t bytes, uint64_t src_stride, uint64_t* mbar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(pieces * bytes)
+                 : "memory");
+    for (uint32_t i = 0; i < pieces; ++i)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(dst + i * bytes)),
+                     "l"(src + i * src_stride), "r"(bytes), "r"(smem_u32(mbar))
+                     : "memory");
+}
+
+// One thread: the MMAs of one tile into the accumulator at tmem_d,
+// committed to mbar.  A: 16-KB K blocks of 128 rows; B: 8-KB K blocks of 64.
+__device__ __forceinline__ void issue_tile_mma(const unsigned char* sA, const unsigned char* sB, uint32_t nkb,
+                                               uint32_t tmem_d, uint64_t* mbar) {
+    constexpr uint32_t idesc = umma_idesc(KNN_BM, KNN_BN);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    for (uint32_t kb = 0; kb < nkb; ++kb) {
+#pragma unroll
+        for (uint32_t s = 0; s < 4; ++s) {          // 32 bytes along the 128-byte rows
+            const uint64_t ad = umma_desc(smem_u32(sA + kb * (KNN_BM * 128u)) + s * 32u);
+            const uint64_t bd = umma_desc(smem_u32(sB + kb * (KNN_BN * 128u)) + s * 32u);
+            const uint32_t acc = (kb | s) ? 1u : 0u;
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                : "memory");
+        }
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
+                 : "memory");
+}
+
 template <int KMAX>
 __device__ __forceinline__ void topk_push(float (&vals)[KMAX], uint32_t (&ids)[KMAX], float v, uint32_t id) {
-    if (!(v > vals[KMAX - 1])) return;
     vals[KMAX - 1] = v;
     ids[KMAX - 1] = id;
 #pragma unroll
@@ -191,17 +241,20 @@ __device__ __forceinline__ void topk_push(float (&vals)[KMAX], uint32_t (&ids)[K
 
 template <int KMAX>
 __global__ void __launch_bounds__(KNN_THREADS, 1)
-    k_cos_topk(const __nv_bfloat16* __restrict__ Q, uint64_t nq, const __nv_bfloat16* __restrict__ D, uint64_t ndb,
+    k_cos_topk(const unsigned char* __restrict__ Q, uint64_t nq, const unsigned char* __restrict__ D, uint64_t ndb,
                uint32_t dpad, const uint64_t* __restrict__ qself, uint32_t k, uint32_t* __restrict__ idx_out,
                float* __restrict__ sim_out, uint32_t* __restrict__ err) {
     extern __shared__ unsigned char knn_smem_raw[];
-    __shared__ uint64_t mbar;
+    __shared__ uint64_t bar_a, bar_full[KNN_STAGES], bar_mma[KNN_STAGES], bar_free[KNN_STAGES];
     __shared__ uint32_t tmem_slot;
+    __shared__ volatile uint32_t abort_flag;
     unsigned char* smem = (unsigned char*)(((uintptr_t)knn_smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t nkb = dpad / 64;
+    const uint32_t a_bytes = nkb * (KNN_BM * 128u), b_bytes = nkb * (KNN_BN * 128u);
     unsigned char* sA = smem;
-    unsigned char* sB = smem + (size_t)KNN_BM * dpad * 2;
-    const int warp = threadIdx.x >> 5;
-    const uint64_t q0 = (uint64_t)blockIdx.x * KNN_BM;
+    auto sB = [&](uint32_t st) { return smem + a_bytes + st * b_bytes; };
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint64_t ntiles = (ndb + KNN_BN - 1) / KNN_BN;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -209,110 +262,192 @@ __global__ void __launch_bounds__(KNN_THREADS, 1)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (threadIdx.x == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+    if (threadIdx.x == 0) {
+        abort_flag = 0;
+        mbar_init(&bar_a, 1);
+        for (int i = 0; i < KNN_STAGES; ++i) {
+            mbar_init(&bar_full[i], 1);
+            mbar_init(&bar_mma[i], 1);
+            mbar_init(&bar_free[i], KNN_EPI_WARPS);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_slot;
 
-    stage_rows(sA, Q, nq, q0, KNN_BM, dpad);
-
+    // per-thread top-k (epilogue warps)
     float vals[KMAX];
     uint32_t ids[KMAX];
 #pragma unroll
     for (int i = 0; i < KMAX; ++i) { vals[i] = -INFINITY; ids[i] = 0xffffffffu; }
-    const uint64_t myq = q0 + threadIdx.x;              // TMEM lane = accumulator row = query
-    const uint64_t self = (qself && myq < nq) ? qself[myq] : ~0ull;
-    const uint32_t idesc = umma_idesc(KNN_BM, KNN_BN);
-    const uint32_t nkb = dpad / 64;
-    bool timed_out = false;
-    uint32_t phase = 0;
+    const int quarter = warp & 3, half = (warp >> 2) & 1;
+    const uint32_t qrow = 32u * quarter + lane;                 // TMEM lane = accumulator row = query
+    const uint64_t myq = (uint64_t)blockIdx.x * KNN_BM + qrow;
+    const uint64_t self = (warp < KNN_EPI_WARPS && qself && myq < nq) ? qself[myq] : ~0ull;
+    // producer bookkeeping, used to drain the copies and MMAs in flight on abort
+    uint64_t j_end = 0, loaded = 0, landed = 0;    // tiles: MMAs issued, copies issued, copies seen complete
+    bool a_landed = false;
 
-    for (uint64_t t0 = 0; t0 < ndb && !timed_out; t0 += KNN_BN) {
-        stage_rows(sB, D, ndb, t0, KNN_BN, dpad);
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // staged tiles -> tensor core
-        __syncthreads();
-        if (threadIdx.x == 0) {
+    if (warp == KNN_EPI_WARPS) {
+        // ---- producer ----
+        if (lane == 0 && ntiles) {
+            bulk_load(sA, Q + (uint64_t)blockIdx.x * a_bytes, nkb, KNN_BM * 128u, KNN_BM * 128u, &bar_a);
+            for (; loaded < (uint64_t)KNN_STAGES && loaded < ntiles; ++loaded)
+                bulk_load(sB((uint32_t)loaded), D + loaded * b_bytes, nkb, KNN_BN * 128u, KNN_BN * 128u,
+                          &bar_full[loaded]);
+            bool ok = a_landed = mbar_wait(&bar_a, 0, &abort_flag) != 0;
+            for (uint64_t j = 0; ok && j < ntiles; ++j) {
+                const uint32_t st = (uint32_t)(j % KNN_STAGES), use = (uint32_t)(j / KNN_STAGES);
+                if (!mbar_wait(&bar_full[st], use & 1u, &abort_flag)) { ok = false; break; }
+                landed = j + 1;
+                if (j >= (uint64_t)KNN_STAGES && !mbar_wait(&bar_free[st], (use - 1u) & 1u, &abort_flag)) {
+                    ok = false;
+                    break;
+                }
+                issue_tile_mma(sA, sB(st), nkb, tmem + st * (uint32_t)KNN_BN, &bar_mma[st]);
+                j_end = j + 1;
+                // refill tile j-1's buffer with tile j+KNN_STAGES-1 once its MMAs completed
+                if (j >= 1 && loaded < ntiles) {
+                    const uint32_t sp = (uint32_t)((j - 1) % KNN_STAGES), up = (uint32_t)((j - 1) / KNN_STAGES);
+                    if (!mbar_wait(&bar_mma[sp], up & 1u, &abort_flag)) { ok = false; break; }
+                    bulk_load(sB(sp), D + loaded * b_bytes, nkb, KNN_BN * 128u, KNN_BN * 128u, &bar_full[sp]);
+                    ++loaded;
+                }
+            }
+            if (!ok) abort_flag = 1;
+        }
+    } else {
+        // ---- epilogue ----
+        float thr = -INFINITY;
+        for (uint64_t j = 0; j < ntiles; ++j) {
+            const uint32_t st = (uint32_t)(j % KNN_STAGES), use = (uint32_t)(j / KNN_STAGES);
+            // warp-uniform decision: the loads below are .sync.aligned
+            if (!__all_sync(0xffffffffu, mbar_wait(&bar_mma[st], use & 1u, &abort_flag))) {
+                abort_flag = 1;
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (uint32_t kb = 0; kb < nkb; ++kb) {
+            __syncwarp();
+            uint32_t r[32];
+            const uint32_t taddr = tmem + st * (uint32_t)KNN_BN + (uint32_t)half * 32u + ((uint32_t)(32 * quarter) << 16);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                  "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                  "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                : "r"(taddr)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            // release the accumulator: the values are in registers now
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bar_free[st]);
+            // the block's largest similarity first: most blocks cannot enter
+            float mx[16];
 #pragma unroll
-                for (uint32_t s = 0; s < 4; ++s) {          // K = 16 per MMA: 32 bytes within the 128-byte row
-                    const uint64_t ad = umma_desc(smem_u32(sA + kb * KNN_BM * 128u) + s * 32u);
-                    const uint64_t bd = umma_desc(smem_u32(sB + kb * KNN_BN * 128u) + s * 32u);
-                    const uint32_t acc = (kb | s) ? 1u : 0u;
-                    asm volatile(
-                        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-                        : "memory");
-                }
+            for (int t = 0; t < 16; ++t) mx[t] = fmaxf(__uint_as_float(r[2 * t]), __uint_as_float(r[2 * t + 1]));
+#pragma unroll
+            for (int w2 = 8; w2 >= 1; w2 >>= 1) {
+#pragma unroll
+                for (int t = 0; t < w2; ++t) mx[t] = fmaxf(mx[t], mx[t + w2]);
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_u32(&mbar))
-                         : "memory");
-        }
-        // wait for the tile's MMAs (bounded); the outcome is made CTA-wide
-        uint32_t done = mbar_wait(&mbar, phase);
-        if (__syncthreads_or(!done)) {
-            timed_out = true;
-            if (threadIdx.x == 0) atomicOr(err, KNN_ERR_TIMEOUT);
-            // give the committed MMAs a second bounded wait before TMEM is freed
-            if (!done) mbar_wait(&mbar, phase);
-            done = 0;
-        }
-        phase ^= 1u;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (done) {
-            for (uint32_t c0 = 0; c0 < (uint32_t)KNN_BN; c0 += 32) {
-                uint32_t r[32];
-                const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + c0;
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                      "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                      "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
-                      "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
-                      "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                    : "r"(taddr)
-                    : "memory");
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (mx[0] > thr) {
+                unsigned cand = 0;
 #pragma unroll
-                for (int t = 0; t < 32; ++t) {
-                    const uint64_t col = t0 + c0 + (uint32_t)t;
-                    if (col < ndb && col != self) topk_push<KMAX>(vals, ids, __uint_as_float(r[t]), (uint32_t)col);
+                for (int t = 0; t < 32; ++t) cand |= (__uint_as_float(r[t]) > thr ? 1u : 0u) << t;
+                const uint64_t col0 = j * KNN_BN + (uint32_t)half * 32u;
+                while (cand) {
+                    const int t = __ffs(cand) - 1;
+                    cand &= cand - 1;
+                    float v = __uint_as_float(r[0]);
+#pragma unroll
+                    for (int u = 1; u < 32; ++u) v = t == u ? __uint_as_float(r[u]) : v;
+                    const uint64_t col = col0 + (uint32_t)t;
+                    if (v > thr && col < ndb && col != self) {
+                        topk_push<KMAX>(vals, ids, v, (uint32_t)col);
+                        thr = vals[KMAX - 1];
+                    }
                 }
-            }
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();       // TMEM and the B tile are free for the next tile
-    }
-    if (myq < nq && !timed_out) {
-#pragma unroll
-        for (int i = 0; i < KMAX; ++i) {
-            if ((uint32_t)i < k) {
-                idx_out[myq * k + i] = ids[i];
-                sim_out[myq * k + i] = vals[i];
             }
         }
     }
     __syncthreads();
-    if (warp == 0)
+    const bool aborted = abort_flag != 0;
+    if (aborted) {
+        if (threadIdx.x == 0) atomicOr(err, KNN_ERR_TIMEOUT);
+        if (warp == KNN_EPI_WARPS && lane == 0 && ntiles) {
+            // last bounded waits for the copies and MMAs that may still be in flight
+            volatile uint32_t never = 0;
+            if (!a_landed) mbar_wait(&bar_a, 0, &never);
+            for (uint64_t j = landed; j < loaded; ++j)
+                mbar_wait(&bar_full[j % KNN_STAGES], (uint32_t)((j / KNN_STAGES) & 1), &never);
+            for (uint64_t j = j_end > KNN_STAGES ? j_end - KNN_STAGES : 0; j < j_end; ++j)
+                mbar_wait(&bar_mma[j % KNN_STAGES], (uint32_t)((j / KNN_STAGES) & 1), &never);
+        }
+    } else {
+        // merge the two halves' sorted lists per query (tile buffers are free now)
+        float* pv = reinterpret_cast<float*>(smem);                         // [2][128][KMAX]
+        uint32_t* pi = reinterpret_cast<uint32_t*>(smem + (size_t)2 * KNN_BM * KMAX * 4);
+        if (warp < KNN_EPI_WARPS) {
+            const size_t base = ((size_t)half * KNN_BM + qrow) * KMAX;
+#pragma unroll
+            for (int i = 0; i < KMAX; ++i) { pv[base + i] = vals[i]; pi[base + i] = ids[i]; }
+        }
+        __syncthreads();
+        if (warp < 4 && myq < nq) {
+            const size_t b2 = ((size_t)KNN_BM + qrow) * KMAX;
+            for (int i = 0; i < KMAX; ++i) {
+                const float v = pv[b2 + i];
+                if (!(v > vals[KMAX - 1])) break;     // sorted: the rest cannot enter
+                topk_push<KMAX>(vals, ids, v, pi[b2 + i]);
+            }
+#pragma unroll
+            for (int i = 0; i < KMAX; ++i) {
+                if ((uint32_t)i < k) {
+                    idx_out[myq * k + i] = ids[i];
+                    sim_out[myq * k + i] = vals[i];
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0) {
+        __syncwarp();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(KNN_TMEM_COLS)
                      : "memory");
+    }
 }
 
 // compile-time selection by k
 template <int KMAX>
-int knn_run(const __nv_bfloat16* Q, uint64_t nq, const __nv_bfloat16* D, uint64_t ndb, uint32_t dpad,
+int knn_run(const unsigned char* Q, uint64_t nq, const unsigned char* D, uint64_t ndb, uint32_t dpad,
             const uint64_t* qself, uint32_t k, uint32_t* idx, float* sim, uint32_t* err, cudaStream_t s) {
-    const size_t smem = (size_t)(KNN_BM + KNN_BN) * dpad * 2 + 1024;
+    // query tile + KNN_STAGES database tiles (reused at the end for the two halves' lists)
+    const size_t tiles = (size_t)(dpad / 64) * 128 * (KNN_BM + KNN_STAGES * KNN_BN);
+    const size_t lists = (size_t)2 * KNN_BM * KMAX * 8;
+    const size_t smem = std::max(tiles, lists) + 1024;
     KCK(cudaFuncSetAttribute(k_cos_topk<KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
         "knn shared memory");
     const unsigned grid = (unsigned)((nq + KNN_BM - 1) / KNN_BM);
+    cudaEvent_t e0, e1;
+    KCK(cudaEventCreate(&e0), "events");
+    KCK(cudaEventCreate(&e1), "events");
+    cudaEventRecord(e0, s);
     k_cos_topk<KMAX><<<grid, KNN_THREADS, smem, s>>>(Q, nq, D, ndb, dpad, qself, k, idx, sim, err);
-    KCK(cudaGetLastError(), "knn launch");
+    cudaEventRecord(e1, s);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) cudaEventElapsedTime(&g_knn_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    KCK(e, "knn launch");
     return EP_OK;
 }
 
@@ -368,14 +503,16 @@ extern "C" int ep_knn_cosine(int device, uint64_t n_db, uint32_t dims, const flo
     KCK(cudaSetDevice(device), "select device");
     if (!n_q) return EP_OK;
     const uint32_t dpad = (dims + 63) / 64 * 64;
+    const uint64_t q_tile_bytes = (uint64_t)(dpad / 64) * 128 * KNN_BM, db_tile_bytes = (uint64_t)(dpad / 64) * 128 * KNN_BN;
+    const uint64_t db_tiles = (n_db + KNN_BN - 1) / KNN_BN, q_tiles = (n_q + KNN_BM - 1) / KNN_BM;
     cudaStream_t s;
     KCK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
     struct SG { cudaStream_t s; ~SG() { cudaStreamDestroy(s); } } sg{s};
     DevMem draw, dq, dD, dQ, dself, didx, dsim, derr;
     const uint64_t nmax = std::max(n_db, n_q);
     KCK(draw.alloc(nmax * dims * 4), "alloc");
-    KCK(dD.alloc(std::max<uint64_t>(n_db, 1) * dpad * 2), "alloc");
-    KCK(dQ.alloc(n_q * dpad * 2), "alloc");
+    KCK(dD.alloc(std::max<uint64_t>(db_tiles, 1) * db_tile_bytes), "alloc");
+    KCK(dQ.alloc(q_tiles * q_tile_bytes), "alloc");
     KCK(didx.alloc(n_q * k * 4), "alloc");
     KCK(dsim.alloc(n_q * k * 4), "alloc");
     KCK(derr.alloc(4), "alloc");
@@ -386,18 +523,19 @@ extern "C" int ep_knn_cosine(int device, uint64_t n_db, uint32_t dims, const flo
     }
     if (n_db) {
         KCK(cudaMemcpyAsync(draw.p, db, n_db * dims * 4, cudaMemcpyHostToDevice, s), "upload");
-        k_norm_bf16<<<(unsigned)((n_db * 32 + 255) / 256), 256, 0, s>>>(n_db, dims, dpad, (const float*)draw.p,
-                                                                       (__nv_bfloat16*)dD.p);
+        k_norm_swz<<<(unsigned)((db_tiles * KNN_BN * 32 + 255) / 256), 256, 0, s>>>(
+            n_db, db_tiles * KNN_BN, dims, dpad, 6, (const float*)draw.p, (unsigned char*)dD.p);
         KCK(cudaGetLastError(), "normalise");
     }
     KCK(cudaMemcpyAsync(draw.p, q, n_q * dims * 4, cudaMemcpyHostToDevice, s), "upload");
-    k_norm_bf16<<<(unsigned)((n_q * 32 + 255) / 256), 256, 0, s>>>(n_q, dims, dpad, (const float*)draw.p,
-                                                                   (__nv_bfloat16*)dQ.p);
+    k_norm_swz<<<(unsigned)((q_tiles * KNN_BM * 32 + 255) / 256), 256, 0, s>>>(n_q, q_tiles * KNN_BM, dims, dpad, 7,
+                                                                              (const float*)draw.p,
+                                                                              (unsigned char*)dQ.p);
     KCK(cudaGetLastError(), "normalise");
     const uint64_t* qs = q_self ? (const uint64_t*)dself.p : nullptr;
-    int rc = k <= 16 ? knn_run<16>((const __nv_bfloat16*)dQ.p, n_q, (const __nv_bfloat16*)dD.p, n_db, dpad, qs, k,
+    int rc = k <= 16 ? knn_run<16>((const unsigned char*)dQ.p, n_q, (const unsigned char*)dD.p, n_db, dpad, qs, k,
                                    (uint32_t*)didx.p, (float*)dsim.p, (uint32_t*)derr.p, s)
-                     : knn_run<32>((const __nv_bfloat16*)dQ.p, n_q, (const __nv_bfloat16*)dD.p, n_db, dpad, qs, k,
+                     : knn_run<32>((const unsigned char*)dQ.p, n_q, (const unsigned char*)dD.p, n_db, dpad, qs, k,
                                    (uint32_t*)didx.p, (float*)dsim.p, (uint32_t*)derr.p, s);
     if (rc) return rc;
     uint32_t herr = 0;
@@ -410,3 +548,5 @@ extern "C" int ep_knn_cosine(int device, uint64_t n_db, uint32_t dims, const flo
 }
 
 extern "C" const char* ep_knn_last_error(void) { return g_knn_err.c_str(); }
+
+extern "C" float ep_knn_last_kernel_ms(void) { return g_knn_ms; }

@@ -277,6 +277,10 @@ int ep_knn_cosine(int device, uint64_t n_db, uint32_t dims, const float* db, uin
  * host thread. */
 const char* ep_knn_last_error(void);
 
+/* Measurement hook (no counterpart in the reference): CUDA-event time in ms
+ * of the top-k kernel of this host thread's last ep_knn_cosine call. */
+float ep_knn_last_kernel_ms(void);
+
 /* ---- host-side graph construction (src/graph.rs) --------------------- */
 
 /* CSR::construct_from_edges (src/graph.rs:70-142): optional deduplication
