@@ -122,23 +122,29 @@ __global__ void __launch_bounds__(256) k_norm_swz(uint64_t n, uint64_t n_tiled, 
 // ---------------------------------------------------------------------------
 // Cosine top-k: one CTA per 128 queries, warp-specialised.
 //
-// Producer warp (warp 8, one lane): copies the query tile (M = 128) and keeps
+// Copy warp (warp 8): copies the query tile (M = 128) once and keeps
 // KNN_STAGES database tiles (N = 64 rows) in flight with cp.async.bulk from
-// their tile images (completion counted in bytes on mbarriers), and issues
-// each tile's MMAs (K = 16 per instruction, BF16 x BF16 -> FP32) into one of
-// KNN_STAGES 64-column accumulators in tensor memory, committed to an
-// mbarrier.  A buffer is refilled once the MMAs that read it have completed;
-// an accumulator is reused once the epilogue has released it.
+// their tile images, completion counted in bytes on mbarriers; a buffer is
+// refilled once the MMAs that read it have completed.
+// MMA warp (warp 9): once a tile has landed and its accumulator is free,
+// lane 0 issues the tile's MMAs (K = 16 per instruction, BF16 x BF16 ->
+// FP32) into one of KNN_STAGES 64-column accumulators in tensor memory and
+// commits them to an mbarrier.  Both loops run warp-uniform; the MMA
+// descriptors are built once and advanced by adds.
 // Epilogue warps 0-7: warp w reads TMEM lane quarter w % 4 (lane = query row)
-// and the 32-column half w / 4 of each tile; each thread keeps a sorted
-// top-KMAX of its columns in registers, skipping 32-value blocks whose
-// maximum cannot enter; the two halves' lists are merged per query at the
-// end.  Operands sit in shared memory as K-major, 128-byte-swizzled tiles.
+// and the 32-column half w / 4 of each tile, then releases the accumulator
+// through an mbarrier.  Each thread keeps a sorted top-KMAX of its columns in
+// registers and admits a value only above its k-th best so far, skipping
+// 32-value blocks whose maximum cannot enter; the two halves' lists are
+// merged per query at the end.  Operands sit in shared memory as K-major,
+// 128-byte-swizzled tiles.
 // All waits are bounded; a timeout sets an abort flag that ends every role's
-// loop, and the error word.
+// loop, the copies and MMAs still in flight are waited for, and the error
+// word is set.
 // ---------------------------------------------------------------------------
 constexpr int KNN_BM = 128, KNN_BN = 64, KNN_STAGES = 4;
-constexpr int KNN_EPI_WARPS = 8, KNN_THREADS = 32 * (KNN_EPI_WARPS + 1);
+constexpr int KNN_EPI_WARPS = 8, KNN_COPY_WARP = KNN_EPI_WARPS, KNN_MMA_WARP = KNN_EPI_WARPS + 1;
+constexpr int KNN_THREADS = 32 * (KNN_EPI_WARPS + 2);
 constexpr uint32_t KNN_TMEM_COLS = KNN_BN * KNN_STAGES;    // 256
 constexpr uint32_t KNN_WAIT_LIMIT = 1u << 22;    // mbarrier polls (32 ns sleeps) before giving up
 enum : uint32_t { KNN_ERR_TIMEOUT = 1u };
@@ -199,27 +205,33 @@ __device__ __forceinline__ void bulk_load(unsigned char* dst, const unsigned cha
                      : "memory");
 }
 
-// One thread: the MMAs of one tile into the accumulator at tmem_d,
-// committed to mbar.  A: 16-KB K blocks of 128 rows; B: 8-KB K blocks of 64.
-__device__ __forceinline__ void issue_tile_mma(const unsigned char* sA, const unsigned char* sB, uint32_t nkb,
-                                               uint32_t tmem_d, uint64_t* mbar) {
+// The MMAs of one tile into the accumulator at tmem_d, committed to mbar.
+// Every lane of the (converged) MMA warp runs the loop; the instructions are
+// predicated on `leader`, so one thread issues them and the commit.  ad / bd:
+// descriptors of K block 0; a K block is 16 KB of A (128 rows) and 8 KB of B
+// (64 rows); a K step of 16 elements moves the start address by 32 B.
+__device__ __forceinline__ void issue_tile_mma(uint64_t ad, uint64_t bd, uint32_t nkb, uint32_t tmem_d,
+                                               uint64_t* mbar, uint32_t leader) {
     constexpr uint32_t idesc = umma_idesc(KNN_BM, KNN_BN);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     for (uint32_t kb = 0; kb < nkb; ++kb) {
 #pragma unroll
-        for (uint32_t s = 0; s < 4; ++s) {          // 32 bytes along the 128-byte rows
-            const uint64_t ad = umma_desc(smem_u32(sA + kb * (KNN_BM * 128u)) + s * 32u);
-            const uint64_t bd = umma_desc(smem_u32(sB + kb * (KNN_BN * 128u)) + s * 32u);
+        for (uint32_t s = 0; s < 4; ++s) {
+            const uint64_t a = ad + kb * ((KNN_BM * 128u) >> 4) + s * 2u;
+            const uint64_t b = bd + kb * ((KNN_BN * 128u) >> 4) + s * 2u;
             const uint32_t acc = (kb | s) ? 1u : 0u;
             asm volatile(
-                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
-                "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                "{\n .reg .pred p, l;\n setp.ne.b32 p, %4, 0;\n setp.ne.b32 l, %5, 0;\n"
+                " @l tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
+                "l"(a), "l"(b), "r"(idesc), "r"(acc), "r"(leader)
                 : "memory");
         }
     }
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
-                 : "memory");
+    asm volatile(
+        "{\n .reg .pred l;\n setp.ne.b32 l, %1, 0;\n"
+        " @l tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}" ::"r"(smem_u32(mbar)),
+        "r"(leader)
+        : "memory");
 }
 
 template <int KMAX>
@@ -239,6 +251,17 @@ __device__ __forceinline__ void topk_push(float (&vals)[KMAX], uint32_t (&ids)[K
     }
 }
 
+// k-th largest of a list sorted in descending order (k in [1, KMAX]): the
+// minimum of its first k entries, written so that the registers are never
+// indexed at run time
+template <int KMAX>
+__device__ __forceinline__ float kth_value(const float (&vals)[KMAX], uint32_t k) {
+    float t = vals[0];
+#pragma unroll
+    for (int i = 1; i < KMAX; ++i) t = fminf(t, (uint32_t)i < k ? vals[i] : INFINITY);
+    return t;
+}
+
 template <int KMAX>
 __global__ void __launch_bounds__(KNN_THREADS, 1)
     k_cos_topk(const unsigned char* __restrict__ Q, uint64_t nq, const unsigned char* __restrict__ D, uint64_t ndb,
@@ -246,7 +269,8 @@ __global__ void __launch_bounds__(KNN_THREADS, 1)
                float* __restrict__ sim_out, uint32_t* __restrict__ err) {
     extern __shared__ unsigned char knn_smem_raw[];
     __shared__ uint64_t bar_a, bar_full[KNN_STAGES], bar_mma[KNN_STAGES], bar_free[KNN_STAGES];
-    __shared__ uint32_t tmem_slot;
+    __shared__ uint64_t s_loaded, s_landed, s_issued;    // tiles copied / seen landed / MMAs issued
+    __shared__ uint32_t tmem_slot, s_a_landed;
     __shared__ volatile uint32_t abort_flag;
     unsigned char* smem = (unsigned char*)(((uintptr_t)knn_smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t nkb = dpad / 64;
@@ -264,6 +288,8 @@ __global__ void __launch_bounds__(KNN_THREADS, 1)
     }
     if (threadIdx.x == 0) {
         abort_flag = 0;
+        s_loaded = s_landed = s_issued = 0;
+        s_a_landed = 0;
         mbar_init(&bar_a, 1);
         for (int i = 0; i < KNN_STAGES; ++i) {
             mbar_init(&bar_full[i], 1);
@@ -286,41 +312,59 @@ __global__ void __launch_bounds__(KNN_THREADS, 1)
     const uint32_t qrow = 32u * quarter + lane;                 // TMEM lane = accumulator row = query
     const uint64_t myq = (uint64_t)blockIdx.x * KNN_BM + qrow;
     const uint64_t self = (warp < KNN_EPI_WARPS && qself && myq < nq) ? qself[myq] : ~0ull;
-    // producer bookkeeping, used to drain the copies and MMAs in flight on abort
-    uint64_t j_end = 0, loaded = 0, landed = 0;    // tiles: MMAs issued, copies issued, copies seen complete
-    bool a_landed = false;
 
-    if (warp == KNN_EPI_WARPS) {
-        // ---- producer ----
-        if (lane == 0 && ntiles) {
-            bulk_load(sA, Q + (uint64_t)blockIdx.x * a_bytes, nkb, KNN_BM * 128u, KNN_BM * 128u, &bar_a);
-            for (; loaded < (uint64_t)KNN_STAGES && loaded < ntiles; ++loaded)
-                bulk_load(sB((uint32_t)loaded), D + loaded * b_bytes, nkb, KNN_BN * 128u, KNN_BN * 128u,
-                          &bar_full[loaded]);
-            bool ok = a_landed = mbar_wait(&bar_a, 0, &abort_flag) != 0;
+    if (warp == KNN_COPY_WARP) {
+        // ---- copies ----
+        uint64_t loaded = 0;
+        if (ntiles) {
+            if (lane == 0) bulk_load(sA, Q + (uint64_t)blockIdx.x * a_bytes, nkb, KNN_BM * 128u, KNN_BM * 128u, &bar_a);
+            for (uint64_t j = 0; j < ntiles; ++j) {
+                const uint32_t st = (uint32_t)(j % KNN_STAGES), use = (uint32_t)(j / KNN_STAGES);
+                // the buffer is free once the MMAs of its previous tile completed
+                if (j >= (uint64_t)KNN_STAGES &&
+                    !__all_sync(0xffffffffu, mbar_wait(&bar_mma[st], (use - 1u) & 1u, &abort_flag))) {
+                    abort_flag = 1;
+                    break;
+                }
+                if (lane == 0)
+                    bulk_load(sB(st), D + j * b_bytes, nkb, KNN_BN * 128u, KNN_BN * 128u, &bar_full[st]);
+                loaded = j + 1;
+            }
+        }
+        if (lane == 0) s_loaded = loaded;
+    } else if (warp == KNN_MMA_WARP) {
+        // ---- MMA issue ----
+        uint64_t landed = 0, issued = 0;
+        uint32_t a_ok = 0;
+        if (ntiles) {
+            const uint64_t ad = umma_desc(smem_u32(sA)), bd0 = umma_desc(smem_u32(sB(0)));
+            bool ok = a_ok = __all_sync(0xffffffffu, mbar_wait(&bar_a, 0, &abort_flag));
             for (uint64_t j = 0; ok && j < ntiles; ++j) {
                 const uint32_t st = (uint32_t)(j % KNN_STAGES), use = (uint32_t)(j / KNN_STAGES);
-                if (!mbar_wait(&bar_full[st], use & 1u, &abort_flag)) { ok = false; break; }
-                landed = j + 1;
-                if (j >= (uint64_t)KNN_STAGES && !mbar_wait(&bar_free[st], (use - 1u) & 1u, &abort_flag)) {
+                if (!__all_sync(0xffffffffu, mbar_wait(&bar_full[st], use & 1u, &abort_flag))) {
                     ok = false;
                     break;
                 }
-                issue_tile_mma(sA, sB(st), nkb, tmem + st * (uint32_t)KNN_BN, &bar_mma[st]);
-                j_end = j + 1;
-                // refill tile j-1's buffer with tile j+KNN_STAGES-1 once its MMAs completed
-                if (j >= 1 && loaded < ntiles) {
-                    const uint32_t sp = (uint32_t)((j - 1) % KNN_STAGES), up = (uint32_t)((j - 1) / KNN_STAGES);
-                    if (!mbar_wait(&bar_mma[sp], up & 1u, &abort_flag)) { ok = false; break; }
-                    bulk_load(sB(sp), D + loaded * b_bytes, nkb, KNN_BN * 128u, KNN_BN * 128u, &bar_full[sp]);
-                    ++loaded;
+                landed = j + 1;
+                if (j >= (uint64_t)KNN_STAGES &&
+                    !__all_sync(0xffffffffu, mbar_wait(&bar_free[st], (use - 1u) & 1u, &abort_flag))) {
+                    ok = false;
+                    break;
                 }
+                issue_tile_mma(ad, bd0 + st * (b_bytes >> 4), nkb, tmem + st * (uint32_t)KNN_BN, &bar_mma[st],
+                               lane == 0);
+                issued = j + 1;
             }
             if (!ok) abort_flag = 1;
         }
+        if (lane == 0) {
+            s_landed = landed;
+            s_issued = issued;
+            s_a_landed = a_ok;
+        }
     } else {
         // ---- epilogue ----
-        float thr = -INFINITY;
+        float thr = -INFINITY;                     // k-th best so far
         for (uint64_t j = 0; j < ntiles; ++j) {
             const uint32_t st = (uint32_t)(j % KNN_STAGES), use = (uint32_t)(j / KNN_STAGES);
             // warp-uniform decision: the loads below are .sync.aligned
@@ -370,7 +414,7 @@ __global__ void __launch_bounds__(KNN_THREADS, 1)
                     const uint64_t col = col0 + (uint32_t)t;
                     if (v > thr && col < ndb && col != self) {
                         topk_push<KMAX>(vals, ids, v, (uint32_t)col);
-                        thr = vals[KMAX - 1];
+                        thr = kth_value<KMAX>(vals, k);
                     }
                 }
             }
@@ -380,13 +424,13 @@ __global__ void __launch_bounds__(KNN_THREADS, 1)
     const bool aborted = abort_flag != 0;
     if (aborted) {
         if (threadIdx.x == 0) atomicOr(err, KNN_ERR_TIMEOUT);
-        if (warp == KNN_EPI_WARPS && lane == 0 && ntiles) {
+        if (warp == KNN_MMA_WARP && lane == 0 && ntiles) {
             // last bounded waits for the copies and MMAs that may still be in flight
             volatile uint32_t never = 0;
-            if (!a_landed) mbar_wait(&bar_a, 0, &never);
-            for (uint64_t j = landed; j < loaded; ++j)
+            if (!s_a_landed) mbar_wait(&bar_a, 0, &never);
+            for (uint64_t j = s_landed; j < s_loaded; ++j)
                 mbar_wait(&bar_full[j % KNN_STAGES], (uint32_t)((j / KNN_STAGES) & 1), &never);
-            for (uint64_t j = j_end > KNN_STAGES ? j_end - KNN_STAGES : 0; j < j_end; ++j)
+            for (uint64_t j = s_issued > KNN_STAGES ? s_issued - KNN_STAGES : 0; j < s_issued; ++j)
                 mbar_wait(&bar_mma[j % KNN_STAGES], (uint32_t)((j / KNN_STAGES) & 1), &never);
         }
     } else {
@@ -401,10 +445,12 @@ __global__ void __launch_bounds__(KNN_THREADS, 1)
         __syncthreads();
         if (warp < 4 && myq < nq) {
             const size_t b2 = ((size_t)KNN_BM + qrow) * KMAX;
-            for (int i = 0; i < KMAX; ++i) {
+            float thr = kth_value<KMAX>(vals, k);
+            for (uint32_t i = 0; i < k; ++i) {
                 const float v = pv[b2 + i];
-                if (!(v > vals[KMAX - 1])) break;     // sorted: the rest cannot enter
+                if (!(v > thr)) break;     // sorted: the rest cannot enter
                 topk_push<KMAX>(vals, ids, v, pi[b2 + i]);
+                thr = kth_value<KMAX>(vals, k);
             }
 #pragma unroll
             for (int i = 0; i < KMAX; ++i) {
