@@ -122,32 +122,41 @@ __global__ void __launch_bounds__(256) k_norm_swz(uint64_t n, uint64_t n_tiled, 
 // ---------------------------------------------------------------------------
 // Cosine top-k: one CTA per 128 queries, warp-specialised.
 //
-// Copy warp (warp 8): copies the query tile (M = 128) once and keeps
-// KNN_STAGES database tiles (N = 64 rows) in flight with cp.async.bulk from
-// their tile images, completion counted in bytes on mbarriers; a buffer is
-// refilled once the MMAs that read it have completed.
-// MMA warp (warp 9): once a tile has landed and its accumulator is free,
-// lane 0 issues the tile's MMAs (K = 16 per instruction, BF16 x BF16 ->
-// FP32) into one of KNN_STAGES 64-column accumulators in tensor memory and
-// commits them to an mbarrier.  Both loops run warp-uniform; the MMA
-// descriptors are built once and advanced by adds.
-// Epilogue warps 0-7: warp w reads TMEM lane quarter w % 4 (lane = query row)
-// and the 32-column half w / 4 of each tile, then releases the accumulator
-// through an mbarrier.  Each thread keeps a sorted top-KMAX of its columns in
-// registers and admits a value only above its k-th best so far, skipping
-// 32-value blocks whose maximum cannot enter; the two halves' lists are
+// Copy warp: copies the query tile (M = 128 rows, all of K) once, then
+// streams the database through KNN_STAGES shared-memory stages, one stage
+// per 64-element K block of a 256-row tile, with cp.async.bulk from the tile
+// images (completion counted in bytes on mbarriers).  A stage is refilled
+// once the MMAs that read it have completed.
+// MMA warp: per database tile, once its accumulator is free, lane 0 issues
+// 4 MMAs per K block (M = 128, N = 256, K = 16; BF16 x BF16 -> FP32) into one
+// of two 256-column accumulators in tensor memory, frees each stage through
+// a commit, and signals the finished tile through another.  Both loops run
+// warp-uniform; the MMA descriptors are built once and advanced by adds.
+// Epilogue warps: warp w reads TMEM lane quarter w % 4 (lane = query row)
+// and the column slice w / 4 of each tile, 32 columns per load, then
+// releases the accumulator.  Each thread keeps a sorted top-KMAX of its
+// columns in registers and admits a value only above its k-th best so far,
+// skipping 32-value blocks whose maximum cannot enter; the slices' lists are
 // merged per query at the end.  Operands sit in shared memory as K-major,
 // 128-byte-swizzled tiles.
 // All waits are bounded; a timeout sets an abort flag that ends every role's
 // loop, the copies and MMAs still in flight are waited for, and the error
 // word is set.
 // ---------------------------------------------------------------------------
-constexpr int KNN_BM = 128, KNN_BN = 64, KNN_STAGES = 4;
-constexpr int KNN_EPI_WARPS = 8, KNN_COPY_WARP = KNN_EPI_WARPS, KNN_MMA_WARP = KNN_EPI_WARPS + 1;
-constexpr int KNN_THREADS = 32 * (KNN_EPI_WARPS + 2);
-constexpr uint32_t KNN_TMEM_COLS = KNN_BN * KNN_STAGES;    // 256
+constexpr int KNN_BM = 128, KNN_BN = 256, KNN_STAGES = 4, KNN_ACC = 2;
+constexpr uint32_t KNN_A_KB = KNN_BM * 128u, KNN_B_KB = KNN_BN * 128u;   // bytes per 64-element K block
+constexpr uint32_t KNN_TMEM_COLS = KNN_BN * KNN_ACC;                     // 512: all of tensor memory
 constexpr uint32_t KNN_WAIT_LIMIT = 1u << 22;    // mbarrier polls (32 ns sleeps) before giving up
 enum : uint32_t { KNN_ERR_TIMEOUT = 1u };
+
+// Epilogue shape per list length: 16 warps (4 column slices of 64) for
+// KMAX 16, 8 warps (2 slices of 128) for KMAX 32, within the register file.
+template <int KMAX>
+struct KnnRoles {
+    static constexpr int EPI = KMAX <= 16 ? 16 : 8;
+    static constexpr int SLICES = EPI / 4, CW = KNN_BN / SLICES, BLOCKS = CW / 32;
+    static constexpr int COPY = EPI, MMA = EPI + 1, THREADS = 32 * (EPI + 2);
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -205,28 +214,26 @@ __device__ __forceinline__ void bulk_load(unsigned char* dst, const unsigned cha
                      : "memory");
 }
 
-// The MMAs of one tile into the accumulator at tmem_d, committed to mbar.
-// Every lane of the (converged) MMA warp runs the loop; the instructions are
-// predicated on `leader`, so one thread issues them and the commit.  ad / bd:
-// descriptors of K block 0; a K block is 16 KB of A (128 rows) and 8 KB of B
-// (64 rows); a K step of 16 elements moves the start address by 32 B.
-__device__ __forceinline__ void issue_tile_mma(uint64_t ad, uint64_t bd, uint32_t nkb, uint32_t tmem_d,
-                                               uint64_t* mbar, uint32_t leader) {
+// The 4 MMAs of one K block (K = 64) into the accumulator at tmem_d.  Every
+// lane of the (converged) MMA warp runs this; the instructions are predicated
+// on `leader`, so one thread issues them.  ad / bd: descriptors of the
+// block; a K step of 16 elements moves the start address by 32 B.
+__device__ __forceinline__ void issue_kblock_mma(uint64_t ad, uint64_t bd, uint32_t tmem_d, bool first,
+                                                 uint32_t leader) {
     constexpr uint32_t idesc = umma_idesc(KNN_BM, KNN_BN);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    for (uint32_t kb = 0; kb < nkb; ++kb) {
 #pragma unroll
-        for (uint32_t s = 0; s < 4; ++s) {
-            const uint64_t a = ad + kb * ((KNN_BM * 128u) >> 4) + s * 2u;
-            const uint64_t b = bd + kb * ((KNN_BN * 128u) >> 4) + s * 2u;
-            const uint32_t acc = (kb | s) ? 1u : 0u;
-            asm volatile(
-                "{\n .reg .pred p, l;\n setp.ne.b32 p, %4, 0;\n setp.ne.b32 l, %5, 0;\n"
-                " @l tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
-                "l"(a), "l"(b), "r"(idesc), "r"(acc), "r"(leader)
-                : "memory");
-        }
+    for (uint32_t s = 0; s < 4; ++s) {
+        const uint32_t acc = (!first || s) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p, l;\n setp.ne.b32 p, %4, 0;\n setp.ne.b32 l, %5, 0;\n"
+            " @l tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
+            "l"(ad + s * 2u), "l"(bd + s * 2u), "r"(idesc), "r"(acc), "r"(leader)
+            : "memory");
     }
+}
+
+// Arrives on mbar once every MMA this thread issued so far has completed.
+__device__ __forceinline__ void mma_commit(uint64_t* mbar, uint32_t leader) {
     asm volatile(
         "{\n .reg .pred l;\n setp.ne.b32 l, %1, 0;\n"
         " @l tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}" ::"r"(smem_u32(mbar)),
@@ -263,22 +270,24 @@ __device__ __forceinline__ float kth_value(const float (&vals)[KMAX], uint32_t k
 }
 
 template <int KMAX>
-__global__ void __launch_bounds__(KNN_THREADS, 1)
+__global__ void __launch_bounds__(KnnRoles<KMAX>::THREADS, 1)
     k_cos_topk(const unsigned char* __restrict__ Q, uint64_t nq, const unsigned char* __restrict__ D, uint64_t ndb,
                uint32_t dpad, const uint64_t* __restrict__ qself, uint32_t k, uint32_t* __restrict__ idx_out,
                float* __restrict__ sim_out, uint32_t* __restrict__ err) {
+    using R = KnnRoles<KMAX>;
     extern __shared__ unsigned char knn_smem_raw[];
-    __shared__ uint64_t bar_a, bar_full[KNN_STAGES], bar_mma[KNN_STAGES], bar_free[KNN_STAGES];
-    __shared__ uint64_t s_loaded, s_landed, s_issued;    // tiles copied / seen landed / MMAs issued
+    __shared__ uint64_t bar_a, bar_full[KNN_STAGES], bar_empty[KNN_STAGES], bar_acc_full[KNN_ACC],
+        bar_acc_free[KNN_ACC];
+    __shared__ uint64_t s_loaded, s_landed, s_issued;    // stages copied / seen landed / stages whose MMAs issued
     __shared__ uint32_t tmem_slot, s_a_landed;
     __shared__ volatile uint32_t abort_flag;
     unsigned char* smem = (unsigned char*)(((uintptr_t)knn_smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t nkb = dpad / 64;
-    const uint32_t a_bytes = nkb * (KNN_BM * 128u), b_bytes = nkb * (KNN_BN * 128u);
+    const uint32_t a_bytes = nkb * KNN_A_KB;
     unsigned char* sA = smem;
-    auto sB = [&](uint32_t st) { return smem + a_bytes + st * b_bytes; };
+    auto sB = [&](uint32_t st) { return smem + a_bytes + st * KNN_B_KB; };
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint64_t ntiles = (ndb + KNN_BN - 1) / KNN_BN;
+    const uint64_t ntiles = (ndb + KNN_BN - 1) / KNN_BN, nstages = ntiles * nkb;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -293,8 +302,11 @@ __global__ void __launch_bounds__(KNN_THREADS, 1)
         mbar_init(&bar_a, 1);
         for (int i = 0; i < KNN_STAGES; ++i) {
             mbar_init(&bar_full[i], 1);
-            mbar_init(&bar_mma[i], 1);
-            mbar_init(&bar_free[i], KNN_EPI_WARPS);
+            mbar_init(&bar_empty[i], 1);
+        }
+        for (int i = 0; i < KNN_ACC; ++i) {
+            mbar_init(&bar_acc_full[i], 1);
+            mbar_init(&bar_acc_free[i], R::EPI);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -308,52 +320,60 @@ __global__ void __launch_bounds__(KNN_THREADS, 1)
     uint32_t ids[KMAX];
 #pragma unroll
     for (int i = 0; i < KMAX; ++i) { vals[i] = -INFINITY; ids[i] = 0xffffffffu; }
-    const int quarter = warp & 3, half = (warp >> 2) & 1;
+    const int quarter = warp & 3, slice = warp >> 2;
     const uint32_t qrow = 32u * quarter + lane;                 // TMEM lane = accumulator row = query
     const uint64_t myq = (uint64_t)blockIdx.x * KNN_BM + qrow;
-    const uint64_t self = (warp < KNN_EPI_WARPS && qself && myq < nq) ? qself[myq] : ~0ull;
+    const uint64_t self = (warp < R::EPI && qself && myq < nq) ? qself[myq] : ~0ull;
 
-    if (warp == KNN_COPY_WARP) {
+    if (warp == R::COPY) {
         // ---- copies ----
         uint64_t loaded = 0;
         if (ntiles) {
-            if (lane == 0) bulk_load(sA, Q + (uint64_t)blockIdx.x * a_bytes, nkb, KNN_BM * 128u, KNN_BM * 128u, &bar_a);
-            for (uint64_t j = 0; j < ntiles; ++j) {
-                const uint32_t st = (uint32_t)(j % KNN_STAGES), use = (uint32_t)(j / KNN_STAGES);
-                // the buffer is free once the MMAs of its previous tile completed
-                if (j >= (uint64_t)KNN_STAGES &&
-                    !__all_sync(0xffffffffu, mbar_wait(&bar_mma[st], (use - 1u) & 1u, &abort_flag))) {
+            if (lane == 0) bulk_load(sA, Q + (uint64_t)blockIdx.x * a_bytes, nkb, KNN_A_KB, KNN_A_KB, &bar_a);
+            for (uint64_t sg = 0; sg < nstages; ++sg) {
+                const uint32_t st = (uint32_t)(sg % KNN_STAGES), use = (uint32_t)(sg / KNN_STAGES);
+                // the stage is free once the MMAs of its previous K block completed
+                if (sg >= (uint64_t)KNN_STAGES &&
+                    !__all_sync(0xffffffffu, mbar_wait(&bar_empty[st], (use - 1u) & 1u, &abort_flag))) {
                     abort_flag = 1;
                     break;
                 }
-                if (lane == 0)
-                    bulk_load(sB(st), D + j * b_bytes, nkb, KNN_BN * 128u, KNN_BN * 128u, &bar_full[st]);
-                loaded = j + 1;
+                if (lane == 0) bulk_load(sB(st), D + sg * KNN_B_KB, 2, KNN_B_KB / 2, KNN_B_KB / 2, &bar_full[st]);
+                loaded = sg + 1;
             }
         }
         if (lane == 0) s_loaded = loaded;
-    } else if (warp == KNN_MMA_WARP) {
+    } else if (warp == R::MMA) {
         // ---- MMA issue ----
         uint64_t landed = 0, issued = 0;
         uint32_t a_ok = 0;
         if (ntiles) {
-            const uint64_t ad = umma_desc(smem_u32(sA)), bd0 = umma_desc(smem_u32(sB(0)));
+            const uint64_t ad0 = umma_desc(smem_u32(sA)), bd0 = umma_desc(smem_u32(sB(0)));
             bool ok = a_ok = __all_sync(0xffffffffu, mbar_wait(&bar_a, 0, &abort_flag));
+            uint64_t sg = 0;
             for (uint64_t j = 0; ok && j < ntiles; ++j) {
-                const uint32_t st = (uint32_t)(j % KNN_STAGES), use = (uint32_t)(j / KNN_STAGES);
-                if (!__all_sync(0xffffffffu, mbar_wait(&bar_full[st], use & 1u, &abort_flag))) {
+                const uint32_t acc = (uint32_t)(j % KNN_ACC), ause = (uint32_t)(j / KNN_ACC);
+                if (j >= (uint64_t)KNN_ACC &&
+                    !__all_sync(0xffffffffu, mbar_wait(&bar_acc_free[acc], (ause - 1u) & 1u, &abort_flag))) {
                     ok = false;
                     break;
                 }
-                landed = j + 1;
-                if (j >= (uint64_t)KNN_STAGES &&
-                    !__all_sync(0xffffffffu, mbar_wait(&bar_free[st], (use - 1u) & 1u, &abort_flag))) {
-                    ok = false;
-                    break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                for (uint32_t kb = 0; kb < nkb; ++kb, ++sg) {
+                    const uint32_t st = (uint32_t)(sg % KNN_STAGES), use = (uint32_t)(sg / KNN_STAGES);
+                    if (!__all_sync(0xffffffffu, mbar_wait(&bar_full[st], use & 1u, &abort_flag))) {
+                        ok = false;
+                        break;
+                    }
+                    landed = sg + 1;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    issue_kblock_mma(ad0 + kb * (KNN_A_KB >> 4), bd0 + st * (KNN_B_KB >> 4), tmem + acc * KNN_BN,
+                                     kb == 0, lane == 0);
+                    mma_commit(&bar_empty[st], lane == 0);
+                    issued = sg + 1;
                 }
-                issue_tile_mma(ad, bd0 + st * (b_bytes >> 4), nkb, tmem + st * (uint32_t)KNN_BN, &bar_mma[st],
-                               lane == 0);
-                issued = j + 1;
+                if (!ok) break;
+                mma_commit(&bar_acc_full[acc], lane == 0);
             }
             if (!ok) abort_flag = 1;
         }
@@ -366,55 +386,61 @@ __global__ void __launch_bounds__(KNN_THREADS, 1)
         // ---- epilogue ----
         float thr = -INFINITY;                     // k-th best so far
         for (uint64_t j = 0; j < ntiles; ++j) {
-            const uint32_t st = (uint32_t)(j % KNN_STAGES), use = (uint32_t)(j / KNN_STAGES);
+            const uint32_t acc = (uint32_t)(j % KNN_ACC), ause = (uint32_t)(j / KNN_ACC);
             // warp-uniform decision: the loads below are .sync.aligned
-            if (!__all_sync(0xffffffffu, mbar_wait(&bar_mma[st], use & 1u, &abort_flag))) {
+            if (!__all_sync(0xffffffffu, mbar_wait(&bar_acc_full[acc], ause & 1u, &abort_flag))) {
                 abort_flag = 1;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            __syncwarp();
-            uint32_t r[32];
-            const uint32_t taddr = tmem + st * (uint32_t)KNN_BN + (uint32_t)half * 32u + ((uint32_t)(32 * quarter) << 16);
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                  "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-                  "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-                  "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                : "r"(taddr)
-                : "memory");
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            // release the accumulator: the values are in registers now
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&bar_free[st]);
-            // the block's largest similarity first: most blocks cannot enter
-            float mx[16];
+#pragma unroll 1
+            for (int bl = 0; bl < R::BLOCKS; ++bl) {
+                __syncwarp();
+                uint32_t r[32];
+                const uint32_t cofs = (uint32_t)(slice * R::CW + bl * 32);
+                const uint32_t taddr = tmem + acc * KNN_BN + cofs + ((uint32_t)(32 * quarter) << 16);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                      "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                      "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+                      "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+                      "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                    : "r"(taddr)
+                    : "memory");
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (bl == R::BLOCKS - 1) {
+                    // release the accumulator: this warp's values are all in registers
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&bar_acc_free[acc]);
+                }
+                // the block's largest similarity first: most blocks cannot enter
+                float mx[16];
 #pragma unroll
-            for (int t = 0; t < 16; ++t) mx[t] = fmaxf(__uint_as_float(r[2 * t]), __uint_as_float(r[2 * t + 1]));
+                for (int t = 0; t < 16; ++t) mx[t] = fmaxf(__uint_as_float(r[2 * t]), __uint_as_float(r[2 * t + 1]));
 #pragma unroll
-            for (int w2 = 8; w2 >= 1; w2 >>= 1) {
+                for (int w2 = 8; w2 >= 1; w2 >>= 1) {
 #pragma unroll
-                for (int t = 0; t < w2; ++t) mx[t] = fmaxf(mx[t], mx[t + w2]);
-            }
-            if (mx[0] > thr) {
-                unsigned cand = 0;
+                    for (int t = 0; t < w2; ++t) mx[t] = fmaxf(mx[t], mx[t + w2]);
+                }
+                if (mx[0] > thr) {
+                    unsigned cand = 0;
 #pragma unroll
-                for (int t = 0; t < 32; ++t) cand |= (__uint_as_float(r[t]) > thr ? 1u : 0u) << t;
-                const uint64_t col0 = j * KNN_BN + (uint32_t)half * 32u;
-                while (cand) {
-                    const int t = __ffs(cand) - 1;
-                    cand &= cand - 1;
-                    float v = __uint_as_float(r[0]);
+                    for (int t = 0; t < 32; ++t) cand |= (__uint_as_float(r[t]) > thr ? 1u : 0u) << t;
+                    const uint64_t col0 = j * KNN_BN + cofs;
+                    while (cand) {
+                        const int t = __ffs(cand) - 1;
+                        cand &= cand - 1;
+                        float v = __uint_as_float(r[0]);
 #pragma unroll
-                    for (int u = 1; u < 32; ++u) v = t == u ? __uint_as_float(r[u]) : v;
-                    const uint64_t col = col0 + (uint32_t)t;
-                    if (v > thr && col < ndb && col != self) {
-                        topk_push<KMAX>(vals, ids, v, (uint32_t)col);
-                        thr = kth_value<KMAX>(vals, k);
+                        for (int u = 1; u < 32; ++u) v = t == u ? __uint_as_float(r[u]) : v;
+                        const uint64_t col = col0 + (uint32_t)t;
+                        if (v > thr && col < ndb && col != self) {
+                            topk_push<KMAX>(vals, ids, v, (uint32_t)col);
+                            thr = kth_value<KMAX>(vals, k);
+                        }
                     }
                 }
             }
@@ -424,33 +450,37 @@ __global__ void __launch_bounds__(KNN_THREADS, 1)
     const bool aborted = abort_flag != 0;
     if (aborted) {
         if (threadIdx.x == 0) atomicOr(err, KNN_ERR_TIMEOUT);
-        if (warp == KNN_MMA_WARP && lane == 0 && ntiles) {
+        if (warp == R::MMA && lane == 0 && ntiles) {
             // last bounded waits for the copies and MMAs that may still be in flight
             volatile uint32_t never = 0;
             if (!s_a_landed) mbar_wait(&bar_a, 0, &never);
-            for (uint64_t j = s_landed; j < s_loaded; ++j)
-                mbar_wait(&bar_full[j % KNN_STAGES], (uint32_t)((j / KNN_STAGES) & 1), &never);
-            for (uint64_t j = s_issued > KNN_STAGES ? s_issued - KNN_STAGES : 0; j < s_issued; ++j)
-                mbar_wait(&bar_mma[j % KNN_STAGES], (uint32_t)((j / KNN_STAGES) & 1), &never);
+            for (uint64_t sg = s_landed; sg < s_loaded; ++sg)
+                mbar_wait(&bar_full[sg % KNN_STAGES], (uint32_t)((sg / KNN_STAGES) & 1), &never);
+            if (s_issued) {     // a commit covers every earlier MMA
+                const uint64_t sg = s_issued - 1;
+                mbar_wait(&bar_empty[sg % KNN_STAGES], (uint32_t)((sg / KNN_STAGES) & 1), &never);
+            }
         }
     } else {
-        // merge the two halves' sorted lists per query (tile buffers are free now)
-        float* pv = reinterpret_cast<float*>(smem);                         // [2][128][KMAX]
-        uint32_t* pi = reinterpret_cast<uint32_t*>(smem + (size_t)2 * KNN_BM * KMAX * 4);
-        if (warp < KNN_EPI_WARPS) {
-            const size_t base = ((size_t)half * KNN_BM + qrow) * KMAX;
+        // merge the slices' sorted lists per query (the stages are free now)
+        float* pv = reinterpret_cast<float*>(smem);                         // [SLICES][128][KMAX]
+        uint32_t* pi = reinterpret_cast<uint32_t*>(smem + (size_t)R::SLICES * KNN_BM * KMAX * 4);
+        if (warp < R::EPI) {
+            const size_t base = ((size_t)slice * KNN_BM + qrow) * KMAX;
 #pragma unroll
             for (int i = 0; i < KMAX; ++i) { pv[base + i] = vals[i]; pi[base + i] = ids[i]; }
         }
         __syncthreads();
         if (warp < 4 && myq < nq) {
-            const size_t b2 = ((size_t)KNN_BM + qrow) * KMAX;
             float thr = kth_value<KMAX>(vals, k);
-            for (uint32_t i = 0; i < k; ++i) {
-                const float v = pv[b2 + i];
-                if (!(v > thr)) break;     // sorted: the rest cannot enter
-                topk_push<KMAX>(vals, ids, v, pi[b2 + i]);
-                thr = kth_value<KMAX>(vals, k);
+            for (int sl = 1; sl < R::SLICES; ++sl) {
+                const size_t b2 = ((size_t)sl * KNN_BM + qrow) * KMAX;
+                for (uint32_t i = 0; i < k; ++i) {
+                    const float v = pv[b2 + i];
+                    if (!(v > thr)) break;     // sorted: the rest cannot enter
+                    topk_push<KMAX>(vals, ids, v, pi[b2 + i]);
+                    thr = kth_value<KMAX>(vals, k);
+                }
             }
 #pragma unroll
             for (int i = 0; i < KMAX; ++i) {
@@ -475,9 +505,9 @@ __global__ void __launch_bounds__(KNN_THREADS, 1)
 template <int KMAX>
 int knn_run(const unsigned char* Q, uint64_t nq, const unsigned char* D, uint64_t ndb, uint32_t dpad,
             const uint64_t* qself, uint32_t k, uint32_t* idx, float* sim, uint32_t* err, cudaStream_t s) {
-    // query tile + KNN_STAGES database tiles (reused at the end for the two halves' lists)
-    const size_t tiles = (size_t)(dpad / 64) * 128 * (KNN_BM + KNN_STAGES * KNN_BN);
-    const size_t lists = (size_t)2 * KNN_BM * KMAX * 8;
+    // query tile + KNN_STAGES K-block stages (reused at the end for the slices' lists)
+    const size_t tiles = (size_t)(dpad / 64) * KNN_A_KB + (size_t)KNN_STAGES * KNN_B_KB;
+    const size_t lists = (size_t)KnnRoles<KMAX>::SLICES * KNN_BM * KMAX * 8;
     const size_t smem = std::max(tiles, lists) + 1024;
     KCK(cudaFuncSetAttribute(k_cos_topk<KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
         "knn shared memory");
@@ -486,7 +516,7 @@ int knn_run(const unsigned char* Q, uint64_t nq, const unsigned char* D, uint64_
     KCK(cudaEventCreate(&e0), "events");
     KCK(cudaEventCreate(&e1), "events");
     cudaEventRecord(e0, s);
-    k_cos_topk<KMAX><<<grid, KNN_THREADS, smem, s>>>(Q, nq, D, ndb, dpad, qself, k, idx, sim, err);
+    k_cos_topk<KMAX><<<grid, KnnRoles<KMAX>::THREADS, smem, s>>>(Q, nq, D, ndb, dpad, qself, k, idx, sim, err);
     cudaEventRecord(e1, s);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
@@ -570,7 +600,7 @@ extern "C" int ep_knn_cosine(int device, uint64_t n_db, uint32_t dims, const flo
     if (n_db) {
         KCK(cudaMemcpyAsync(draw.p, db, n_db * dims * 4, cudaMemcpyHostToDevice, s), "upload");
         k_norm_swz<<<(unsigned)((db_tiles * KNN_BN * 32 + 255) / 256), 256, 0, s>>>(
-            n_db, db_tiles * KNN_BN, dims, dpad, 6, (const float*)draw.p, (unsigned char*)dD.p);
+            n_db, db_tiles * KNN_BN, dims, dpad, 8, (const float*)draw.p, (unsigned char*)dD.p);
         KCK(cudaGetLastError(), "normalise");
     }
     KCK(cudaMemcpyAsync(draw.p, q, n_q * dims * 4, cudaMemcpyHostToDevice, s), "upload");
