@@ -136,8 +136,8 @@ __global__ void __launch_bounds__(256) k_norm_swz(uint64_t n, uint64_t n_tiled, 
 // and the column slice w / 4 of each tile, 32 columns per load, then
 // releases the accumulator.  Each thread keeps a sorted top-KMAX of its
 // columns in registers and admits a value only above its k-th best so far,
-// skipping 32-value blocks whose maximum cannot enter; the slices' lists are
-// merged per query at the end.  Operands sit in shared memory as K-major,
+// skipping blocks of 16 or 32 values whose maximum cannot enter; the slices'
+// lists are merged per query at the end.  Operands sit in shared memory as K-major,
 // 128-byte-swizzled tiles.
 // All waits are bounded; a timeout sets an abort flag that ends every role's
 // loop, the copies and MMAs still in flight are waited for, and the error
@@ -149,12 +149,37 @@ constexpr uint32_t KNN_TMEM_COLS = KNN_BN * KNN_ACC;                     // 512:
 constexpr uint32_t KNN_WAIT_LIMIT = 1u << 22;    // mbarrier polls (32 ns sleeps) before giving up
 enum : uint32_t { KNN_ERR_TIMEOUT = 1u };
 
-// Epilogue shape per list length: 16 warps (4 column slices of 64) for
-// KMAX 16, 8 warps (2 slices of 128) for KMAX 32, within the register file.
+// This warp's TMEM lane quarter, columns taddr .. taddr + N - 1 (one 32-bit
+// value per column) into r; waits for the load.
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+          "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+          "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+}
+
+// Epilogue shape per list length, within the register file: 16 warps (4
+// column slices of 64, loaded 16 columns at a time) for KMAX 16; 8 warps
+// (2 slices of 128, 32 at a time) for KMAX 32.
 template <int KMAX>
 struct KnnRoles {
     static constexpr int EPI = KMAX <= 16 ? 16 : 8;
-    static constexpr int SLICES = EPI / 4, CW = KNN_BN / SLICES, BLOCKS = CW / 32;
+    static constexpr int BW = KMAX <= 16 ? 16 : 32;    // columns per TMEM load and per skip test
+    static constexpr int SLICES = EPI / 4, CW = KNN_BN / SLICES, BLOCKS = CW / BW;
     static constexpr int COPY = EPI, MMA = EPI + 1, THREADS = 32 * (EPI + 2);
 };
 
@@ -323,7 +348,9 @@ __global__ void __launch_bounds__(KnnRoles<KMAX>::THREADS, 1)
     const int quarter = warp & 3, slice = warp >> 2;
     const uint32_t qrow = 32u * quarter + lane;                 // TMEM lane = accumulator row = query
     const uint64_t myq = (uint64_t)blockIdx.x * KNN_BM + qrow;
-    const uint64_t self = (warp < R::EPI && qself && myq < nq) ? qself[myq] : ~0ull;
+    // column ids fit 32 bits (the host keeps n_db below 2^32 - 1); ~0 = no row to skip
+    const uint32_t self = (warp < R::EPI && qself && myq < nq && qself[myq] < ndb) ? (uint32_t)qself[myq] : ~0u;
+    const uint32_t ndb32 = (uint32_t)ndb;
 
     if (warp == R::COPY) {
         // ---- copies ----
@@ -396,19 +423,9 @@ __global__ void __launch_bounds__(KnnRoles<KMAX>::THREADS, 1)
 #pragma unroll 1
             for (int bl = 0; bl < R::BLOCKS; ++bl) {
                 __syncwarp();
-                uint32_t r[32];
-                const uint32_t cofs = (uint32_t)(slice * R::CW + bl * 32);
-                const uint32_t taddr = tmem + acc * KNN_BN + cofs + ((uint32_t)(32 * quarter) << 16);
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                      "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                      "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
-                      "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
-                      "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                    : "r"(taddr)
-                    : "memory");
+                uint32_t r[R::BW];
+                const uint32_t cofs = (uint32_t)(slice * R::CW + bl * R::BW);
+                tmem_ld(tmem + acc * KNN_BN + cofs + ((uint32_t)(32 * quarter) << 16), r);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 if (bl == R::BLOCKS - 1) {
                     // release the accumulator: this warp's values are all in registers
@@ -417,28 +434,27 @@ __global__ void __launch_bounds__(KnnRoles<KMAX>::THREADS, 1)
                     if (lane == 0) mbar_arrive(&bar_acc_free[acc]);
                 }
                 // the block's largest similarity first: most blocks cannot enter
-                float mx[16];
+                // (four interleaved chains: few registers, short dependency chains)
+                float mx[4];
 #pragma unroll
-                for (int t = 0; t < 16; ++t) mx[t] = fmaxf(__uint_as_float(r[2 * t]), __uint_as_float(r[2 * t + 1]));
+                for (int t = 0; t < 4; ++t) mx[t] = __uint_as_float(r[t]);
 #pragma unroll
-                for (int w2 = 8; w2 >= 1; w2 >>= 1) {
-#pragma unroll
-                    for (int t = 0; t < w2; ++t) mx[t] = fmaxf(mx[t], mx[t + w2]);
-                }
+                for (int t = 4; t < R::BW; ++t) mx[t & 3] = fmaxf(mx[t & 3], __uint_as_float(r[t]));
+                mx[0] = fmaxf(fmaxf(mx[0], mx[1]), fmaxf(mx[2], mx[3]));
                 if (mx[0] > thr) {
                     unsigned cand = 0;
 #pragma unroll
-                    for (int t = 0; t < 32; ++t) cand |= (__uint_as_float(r[t]) > thr ? 1u : 0u) << t;
-                    const uint64_t col0 = j * KNN_BN + cofs;
+                    for (int t = 0; t < R::BW; ++t) cand |= (__uint_as_float(r[t]) > thr ? 1u : 0u) << t;
+                    const uint32_t col0 = (uint32_t)j * KNN_BN + cofs;
                     while (cand) {
                         const int t = __ffs(cand) - 1;
                         cand &= cand - 1;
                         float v = __uint_as_float(r[0]);
 #pragma unroll
-                        for (int u = 1; u < 32; ++u) v = t == u ? __uint_as_float(r[u]) : v;
-                        const uint64_t col = col0 + (uint32_t)t;
-                        if (v > thr && col < ndb && col != self) {
-                            topk_push<KMAX>(vals, ids, v, (uint32_t)col);
+                        for (int u = 1; u < R::BW; ++u) v = t == u ? __uint_as_float(r[u]) : v;
+                        const uint32_t col = col0 + (uint32_t)t;
+                        if (v > thr && col < ndb32 && col != self) {
+                            topk_push<KMAX>(vals, ids, v, col);
                             thr = kth_value<KMAX>(vals, k);
                         }
                     }
@@ -571,6 +587,7 @@ extern "C" int ep_knn_cosine(int device, uint64_t n_db, uint32_t dims, const flo
                              const float* q, const uint64_t* q_self, uint32_t k, uint32_t* idx_out, float* sim_out) {
     if (dims == 0 || dims > 256) return knn_fail(EP_ERR_INVALID_ARG, "dims must be in [1, 256]");
     if (k == 0 || k > 32) return knn_fail(EP_ERR_INVALID_ARG, "k must be in [1, 32]");
+    if (n_db >= 0xffffffffull) return knn_fail(EP_ERR_INVALID_ARG, "n_db must be below 2^32 - 1");
     if ((n_db && !db) || (n_q && (!q || !idx_out || !sim_out)))
         return knn_fail(EP_ERR_INVALID_ARG, "null array");
     if (q_self)

@@ -269,7 +269,9 @@ int ep_embed_features(int device, uint64_t n_nodes, const uint64_t* fptr, const 
  * BF16; similarities accumulate in FP32 on the tensor cores.  idx_out /
  * sim_out (n_q x k) get the k most similar database rows per query in
  * decreasing similarity; q_self (optional) names a database row to skip per
- * query (~0 = none).  dims <= 256, k <= 32.  Host buffers. */
+ * query (~0 = none).  When fewer than k rows qualify, the remaining slots
+ * hold id 0xFFFFFFFF and similarity -inf.  dims <= 256, k <= 32.  Host
+ * buffers. */
 int ep_knn_cosine(int device, uint64_t n_db, uint32_t dims, const float* db, uint64_t n_q, const float* q,
                   const uint64_t* q_self, uint32_t k, uint32_t* idx_out, float* sim_out);
 

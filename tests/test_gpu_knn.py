@@ -94,3 +94,42 @@ def test_knn_cosine_separated_clusters_exact():
     idx, _ = _native.knn_cosine(db, db, 24, q_self=np.arange(1000))
     want = np.arange(1000) // 25
     assert (idx.astype(np.int64) // 25 == want[:, None]).all()
+
+
+@pytest.mark.parametrize("k", [5, 20])
+def test_knn_cosine_many_tiles_ragged(k):
+    # 20000 rows = 78 full 256-row tiles + 32; 700 queries = 5 full query
+    # tiles + 60; 192 dims = 3 K blocks, so copy stages wrap inside a tile
+    rng = np.random.default_rng(31 + k)
+    n_db, n_q, dims = 20000, 700, 192
+    db = rng.standard_normal((n_db, dims)).astype(np.float32)
+    q = rng.standard_normal((n_q, dims)).astype(np.float32)
+    q[:50] = db[19950:20000]                 # some queries sit in the ragged last tile
+    selfs = np.full(n_q, np.iinfo(np.uint64).max, np.uint64)
+    selfs[:50] = np.arange(19950, 20000)
+    idx, sim = _native.knn_cosine(db, q, k, q_self=selfs)
+    S = _exact(db, q)
+    S[np.arange(50), np.arange(19950, 20000)] = -np.inf
+    kth = -np.sort(-S, axis=1)[:, k - 1]
+    assert (idx < n_db).all()
+    assert all(len(set(r)) == k for r in idx.tolist())
+    assert (np.diff(sim, axis=1) <= 0).all()
+    ex = S[np.arange(n_q)[:, None], idx.astype(np.int64)]
+    assert np.isfinite(ex).all()             # the skipped row never comes back
+    assert (ex >= kth[:, None] - TOL_BF16).all()
+    assert np.abs(ex - sim).max() < TOL_BF16
+
+
+def test_knn_cosine_fewer_rows_than_k():
+    rng = np.random.default_rng(3)
+    db = rng.standard_normal((5, 48)).astype(np.float32)
+    q = rng.standard_normal((3, 48)).astype(np.float32)
+    idx, sim = _native.knn_cosine(db, q, 8, q_self=np.array([0, 2**64 - 1, 4], np.uint64))
+    S = _exact(db, q)
+    for i, skip in enumerate([0, None, 4]):
+        n_ok = 4 if skip is not None else 5
+        assert sorted(idx[i, :n_ok].tolist()) == [j for j in range(5) if j != skip]
+        assert (np.diff(sim[i, :n_ok]) <= 0).all()
+        assert (idx[i, n_ok:] == 0xFFFFFFFF).all() and np.isneginf(sim[i, n_ok:]).all()
+    e_idx, e_sim = _native.knn_cosine(np.zeros((0, 48), np.float32), q, 4)
+    assert (e_idx == 0xFFFFFFFF).all() and np.isneginf(e_sim).all()
