@@ -173,7 +173,7 @@ __device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[16]) {
 }
 
 // Epilogue shape per list length, within the register file: 16 warps (4
-// column slices of 64, loaded 16 columns at a time) for KMAX 16; 8 warps
+// column slices of 64, loaded 16 columns at a time) for KMAX <= 16; 8 warps
 // (2 slices of 128, 32 at a time) for KMAX 32.
 template <int KMAX>
 struct KnnRoles {
@@ -281,6 +281,32 @@ __device__ __forceinline__ void topk_push(float (&vals)[KMAX], uint32_t (&ids)[K
             ids[i - 1] = ti;
         }
     }
+}
+
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Largest of N floats held as bits in registers (N a multiple of 8): four
+// interleaved chains of three-input maxima, 8 instructions for 16 values and
+// 16 for 32, with few extra registers and short dependency chains.
+template <int N>
+__device__ __forceinline__ float max_of(const uint32_t (&r)[N]) {
+    static_assert(N >= 8 && N % 8 == 0, "N a multiple of 8");
+    auto x = [&](int t) { return __uint_as_float(r[t]); };
+    float m[4] = {x(0), x(1), x(2), x(3)};
+    int i = 4;
+#pragma unroll
+    for (; i + 7 < N; i += 8) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) m[j] = fmax3(m[j], x(i + 2 * j), x(i + 2 * j + 1));
+    }
+    // the last 4 values
+    m[0] = fmax3(m[0], x(i), x(i + 1));
+    m[1] = fmax3(m[1], x(i + 2), x(i + 3));
+    return fmaxf(fmax3(m[0], m[1], m[2]), m[3]);
 }
 
 // k-th largest of a list sorted in descending order (k in [1, KMAX]): the
@@ -434,14 +460,7 @@ __global__ void __launch_bounds__(KnnRoles<KMAX>::THREADS, 1)
                     if (lane == 0) mbar_arrive(&bar_acc_free[acc]);
                 }
                 // the block's largest similarity first: most blocks cannot enter
-                // (four interleaved chains: few registers, short dependency chains)
-                float mx[4];
-#pragma unroll
-                for (int t = 0; t < 4; ++t) mx[t] = __uint_as_float(r[t]);
-#pragma unroll
-                for (int t = 4; t < R::BW; ++t) mx[t & 3] = fmaxf(mx[t & 3], __uint_as_float(r[t]));
-                mx[0] = fmaxf(fmaxf(mx[0], mx[1]), fmaxf(mx[2], mx[3]));
-                if (mx[0] > thr) {
+                if (max_of<R::BW>(r) > thr) {
                     unsigned cand = 0;
 #pragma unroll
                     for (int t = 0; t < R::BW; ++t) cand |= (__uint_as_float(r[t]) > thr ? 1u : 0u) << t;
@@ -626,10 +645,14 @@ extern "C" int ep_knn_cosine(int device, uint64_t n_db, uint32_t dims, const flo
                                                                               (unsigned char*)dQ.p);
     KCK(cudaGetLastError(), "normalise");
     const uint64_t* qs = q_self ? (const uint64_t*)dself.p : nullptr;
-    int rc = k <= 16 ? knn_run<16>((const unsigned char*)dQ.p, n_q, (const unsigned char*)dD.p, n_db, dpad, qs, k,
-                                   (uint32_t*)didx.p, (float*)dsim.p, (uint32_t*)derr.p, s)
-                     : knn_run<32>((const unsigned char*)dQ.p, n_q, (const unsigned char*)dD.p, n_db, dpad, qs, k,
-                                   (uint32_t*)didx.p, (float*)dsim.p, (uint32_t*)derr.p, s);
+    // the shortest list that holds k: insertion and the k-th-value scan cost O(KMAX)
+    const unsigned char *Qp = (const unsigned char*)dQ.p, *Dp = (const unsigned char*)dD.p;
+    uint32_t *ip = (uint32_t*)didx.p, *ep = (uint32_t*)derr.p;
+    float* sp = (float*)dsim.p;
+    int rc = k <= 8    ? knn_run<8>(Qp, n_q, Dp, n_db, dpad, qs, k, ip, sp, ep, s)
+             : k <= 12 ? knn_run<12>(Qp, n_q, Dp, n_db, dpad, qs, k, ip, sp, ep, s)
+             : k <= 16 ? knn_run<16>(Qp, n_q, Dp, n_db, dpad, qs, k, ip, sp, ep, s)
+                       : knn_run<32>(Qp, n_q, Dp, n_db, dpad, qs, k, ip, sp, ep, s);
     if (rc) return rc;
     uint32_t herr = 0;
     KCK(cudaMemcpyAsync(idx_out, didx.p, n_q * k * 4, cudaMemcpyDeviceToHost, s), "download");
