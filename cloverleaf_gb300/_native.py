@@ -14,14 +14,14 @@ import numpy as np
 
 from . import _build
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 EP_OK = 0
 _STATUS = {
     -1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "bad call order",
     -5: "device error flag", -6: "unsupported option", -7: "no CUDA device",
 }
-LOSS_MARGIN, LOSS_STARSPACE, LOSS_CONTRASTIVE = 0, 1, 2
+LOSS_MARGIN, LOSS_STARSPACE, LOSS_CONTRASTIVE, LOSS_RANK, LOSS_RANKSPACE, LOSS_PPR = 0, 1, 2, 3, 4, 5
 SAMPLE_ALL, SAMPLE_FIXED, SAMPLE_PROB = 0, 1, 2
 LW_NONE, LW_LOG, LW_EXP = 0, 1, 2
 FORM_PLAIN_FP32, FORM_FUSED_BF16 = 0, 1
@@ -68,6 +68,7 @@ class EpConfig(ctypes.Structure):
         ("device", ctypes.c_int32),
         ("use_graphs", ctypes.c_int32),
         ("autotune", ctypes.c_int32),
+        ("ppr_restart_p", ctypes.c_float),
     ]
 
 

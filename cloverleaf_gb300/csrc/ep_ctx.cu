@@ -163,6 +163,7 @@ extern "C" void ep_config_default(ep_config* cfg) {
     cfg->form = EP_FORM_PLAIN_FP32;
     cfg->grad_mode = EP_GRAD_REFERENCE;
     cfg->use_graphs = 1;
+    cfg->ppr_restart_p = 0.5f;
 }
 
 extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
@@ -172,7 +173,11 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     if (cfg->dims == 0 || cfg->dims > 512) { g_create_err = "dims must be in [1, 512]"; return EP_ERR_INVALID_ARG; }
     if (cfg->batch_size == 0) { g_create_err = "batch_size must be > 0"; return EP_ERR_INVALID_ARG; }
     if (cfg->negatives == 0 || cfg->negatives > 1024) { g_create_err = "negatives must be in [1, 1024]"; return EP_ERR_INVALID_ARG; }
-    if (cfg->loss < EP_LOSS_MARGIN || cfg->loss > EP_LOSS_CONTRASTIVE) { g_create_err = "unknown loss"; return EP_ERR_INVALID_ARG; }
+    if (cfg->loss < EP_LOSS_MARGIN || cfg->loss > EP_LOSS_PPR) { g_create_err = "unknown loss"; return EP_ERR_INVALID_ARG; }
+    if (cfg->loss == EP_LOSS_PPR && !(cfg->ppr_restart_p >= 0.f && cfg->ppr_restart_p <= 1.f)) {
+        g_create_err = "PPR restart probability must be in [0, 1]";
+        return EP_ERR_INVALID_ARG;
+    }
     if (cfg->max_nodes < 0.f || cfg->max_features < 0.f) {
         g_create_err = "max_nodes / max_features must be either None, or (0, N)";
         return EP_ERR_INVALID_ARG;
@@ -186,7 +191,7 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
         g_create_err = "probability max_features must be in (0, 1)";
         return EP_ERR_INVALID_ARG;
     }
-    if (cfg->weighted_neighbor_sampling && cfg->weighted_neighbor_averaging &&
+    if (cfg->loss != EP_LOSS_PPR && cfg->weighted_neighbor_sampling && cfg->weighted_neighbor_averaging &&
         (cfg->max_nodes_kind == EP_SAMPLE_PROB || (cfg->max_nodes_kind == EP_SAMPLE_FIXED && cfg->max_nodes > 32.f))) {
         g_create_err = "weighted neighbour sampling with weighted averaging is implemented for max_nodes <= 32 (Fixed) or all";
         return EP_ERR_UNSUPPORTED;
@@ -437,10 +442,12 @@ static int prepare_train(ep_ctx* c) {
     c->warmup = (uint64_t)((float)c->total_steps / 5.f);                        // mod.rs:134
     uint32_t K = c->max_deg;
     if (c->cfg.max_nodes_kind == EP_SAMPLE_FIXED) K = std::min<uint32_t>((uint32_t)c->cfg.max_nodes, c->max_deg);
+    if (c->cfg.loss == EP_LOSS_PPR) K = c->R;     // one slot per walk
     // item bound: sum of the B largest per-anchor bounds
     if (!c->bound.ensure((size_t)n * 4)) return c->fail(EP_ERR_OOM, "bound allocation failed");
     launch_node_bound(c->row.as<uint64_t>(), c->cols.as<uint32_t>(), c->fptr.as<uint64_t>(), n, c->cfg.max_nodes_kind,
-                      (uint32_t)c->cfg.max_nodes, c->R, c->max_feat, c->bound.as<uint32_t>(), c->stream);
+                      (uint32_t)c->cfg.max_nodes, c->R, c->max_feat, c->cfg.loss == EP_LOSS_PPR,
+                      c->bound.as<uint32_t>(), c->stream);
     std::vector<uint32_t> hb(n);
     CK(cudaMemcpyAsync(hb.data(), c->bound.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream), "bounds");
     CK(cudaStreamSynchronize(c->stream), "bounds");
@@ -495,6 +502,8 @@ static SampleParams sample_params(ep_ctx* c, BatchState* st, bool eval, int inje
     sp.cfg.weighted_sampling = c->cfg.weighted_neighbor_sampling;
     sp.cfg.fd = feat_drop(c);
     sp.cfg.hard = c->cfg.hard_negatives;
+    sp.cfg.ppr = c->cfg.loss == EP_LOSS_PPR;
+    sp.cfg.ppr_restart = c->cfg.ppr_restart_p;
     sp.cfg.seed = c->cfg.seed;
     sp.row_ptr = c->row.as<uint64_t>();
     sp.cols = c->cols.as<uint32_t>();
@@ -520,7 +529,7 @@ static SampleParams sample_params(ep_ctx* c, BatchState* st, bool eval, int inje
 static ForwardParams forward_params(ep_ctx* c, BatchState* st, const void* table, bool emit, bool eval) {
     ForwardParams fp{};
     fp.st = st;
-    fp.loss = c->cfg.loss;
+    fp.loss = c->cfg.loss == EP_LOSS_PPR ? EP_LOSS_MARGIN : c->cfg.loss;   // PPR: margin on walk positives
     fp.gamma = c->cfg.gamma;
     fp.neg_margin = c->cfg.neg_margin;
     fp.loss_weighting = eval ? EP_LW_NONE : c->cfg.loss_weighting;   // validation reports the raw loss

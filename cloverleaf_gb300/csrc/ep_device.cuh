@@ -45,7 +45,7 @@ __host__ __device__ __forceinline__ u32x4 philox(u32x4 c, uint64_t key) {
 }
 
 // Stream ids (third counter word, top byte).
-enum : uint32_t { ST_NBR = 1u, ST_NEG = 2u, ST_NSEL = 3u, ST_ROUND = 4u, ST_INIT = 5u, ST_NOISE = 6u, ST_FSEL = 7u, ST_HARD = 8u, ST_WRES = 9u };
+enum : uint32_t { ST_NBR = 1u, ST_NEG = 2u, ST_NSEL = 3u, ST_ROUND = 4u, ST_INIT = 5u, ST_NOISE = 6u, ST_FSEL = 7u, ST_HARD = 8u, ST_WRES = 9u, ST_PPR = 10u };
 
 __host__ __device__ __forceinline__ uint32_t rand_u32(uint64_t seed, uint32_t a, uint32_t b,
                                                       uint32_t stream, uint32_t i) {

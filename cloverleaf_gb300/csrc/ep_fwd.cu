@@ -20,7 +20,7 @@
 
 namespace ep {
 
-enum { LOSS_MARGIN = 0, LOSS_STARSPACE = 1, LOSS_CONTRASTIVE = 2 };
+enum { LOSS_MARGIN = 0, LOSS_STARSPACE = 1, LOSS_CONTRASTIVE = 2, LOSS_RANK = 3, LOSS_RANKSPACE = 4 };
 enum { S_ALL = 0, S_FIXED = 1, S_PROB = 2 };
 enum { LW_NONE = 0, LW_LOG = 1, LW_EXP = 2 };
 
@@ -218,7 +218,47 @@ __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
         uint32_t cnt = 0;
         float sw = 1.f;
         int take_all = 0;
-        if (c.nodes_kind == S_ALL) {
+        if (c.ppr) {
+            // PPR positives (loss.rs:166-187): the end nodes of R random
+            // walks from v (random_walk, loss.rs:190-222), weight 1 each, in
+            // walk order; v itself when no walk yields one.  A walk makes at
+            // most 10 moves and, from the second move on, stops with
+            // probability restart_p unless it stands on v; ending on v
+            // yields a uniform neighbour of v instead (none when deg = 0).
+            uint32_t got = 0;
+            for (uint32_t w0 = 0; w0 < c.R; w0 += 32) {
+                const uint32_t t = w0 + lane;
+                uint32_t node = v;
+                bool some = false;
+                if (t < c.R) {
+                    for (uint32_t i = 1; i <= 10; ++i) {
+                        const uint64_t ns = p.row_ptr[node];
+                        const uint32_t nd = (uint32_t)(p.row_ptr[node + 1] - ns);
+                        if (nd == 0) break;
+                        node = p.cols[ns + below(rand_u32(c.seed, v, salt, ST_PPR, t * 32 + 2 * i), nd)];
+                        if (i > 1 && node != v &&
+                            unit_f32(rand_u32(c.seed, v, salt, ST_PPR, t * 32 + 2 * i + 1)) < c.ppr_restart)
+                            break;
+                    }
+                    if (node != v) {
+                        some = true;
+                    } else if (deg > 0) {
+                        node = p.cols[rs + below(rand_u32(c.seed, v, salt, ST_PPR, t * 32 + 31), deg)];
+                        some = true;
+                    }
+                }
+                const unsigned m = __ballot_sync(FULL, some);
+                const uint32_t rank = __popc(m & ((1u << lane) - 1u));
+                if (some) { out[got + rank] = node; outw[got + rank] = 1.f; }
+                got += (uint32_t)__popc(m);
+            }
+            if (got == 0) {
+                if (lane == 0) { out[0] = v; outw[0] = 1.f; }
+                got = 1;
+            }
+            cnt = got;
+            __syncwarp();
+        } else if (c.nodes_kind == S_ALL) {
             take_all = 1;
         } else if (c.nodes_kind == S_FIXED) {
             const uint32_t r = min(c.K, deg);
@@ -349,7 +389,7 @@ __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
         __syncwarp();
         // weights: scale_weight, or scale * p_j * deg when averaging by edge
         // weight (CDFtoP, graph.rs:630-661)
-        for (uint32_t q = lane; q < cnt; q += 32) {
+        for (uint32_t q = lane; q < cnt && !c.ppr; q += 32) {
             float w = sw;
             if (c.weighted_avg && p.wcdf) {
                 const uint32_t pos2 = __float_as_uint(outw[q]);
@@ -972,6 +1012,132 @@ __global__ void __launch_bounds__(128) k_fwd_loss(ForwardParams p) {
         const A deg = (A)(p.row_ptr[v + 1] - p.row_ptr[v]);
         wdiv = p.loss_weighting == LW_LOG ? (A)log((double)(1 + deg)) : (A)pow((double)deg, (double)p.lw_exp);
     }
+    A up = 1;
+    if (p.dloss) up = p.dloss_f64 ? (A)((const double*)p.dloss)[a] : (A)p.dloss[a];
+
+    if (p.loss == LOSS_RANK || p.loss == LOSS_RANKSPACE) {
+        // RankLoss (loss.rs:130-155): logits u_i.h and h.t, p = softmax(.)[h.t];
+        // p < tau gives -ln p.  RankSpace (loss.rs:75-79) adds StarSpace with
+        // gamma = tau.  Exact exponentials throughout (the reference's
+        // approximate exp is its own fallback-checked shortcut).
+        // d(-ln p)/d logit_j = softmax_j - [j is h.t]: dL/du_i = s_i h,
+        // dL/dt = (p - 1) h, dL/dh = sum_i s_i u_i + (p - 1) t.
+        const bool ss = p.loss == LOSS_RANKSPACE;
+        const A tau = (A)p.gamma;
+        A xa[VPL], xh[VPL];            // StarSpace: normalised t and h
+        A nt = 1, nh = 1, rd = 0;
+        if (ss) {
+            A tt_, hh_;
+            warp_dot2<A, VPL>(tv, tv, hv, hv, tt_, hh_);
+            nt = sqrt(tt_);
+            nh = sqrt(hh_);
+            const A rnt = (A)1 / nt, rnh = (A)1 / nh;
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) { xa[k] = tv[k] * rnt; xh[k] = hv[k] * rnh; }
+            rd = warp_dot<A, VPL>(xa, xh);
+        }
+        const A lpos = warp_dot<A, VPL>(hv, tv);
+        // pass 1: running max / sum of the exponentials, StarSpace margins
+        A M = lpos, Z = 1, lsum = 0;
+        uint32_t P = 0;
+        auto logits = [&](const A (&uu_)[VPL], A& lg, A& cs, A& nu) {
+            A uu = 0, hx = 0;
+            if (ss) warp_dot2<A, VPL>(uu_, uu_, xh, uu_, uu, hx);
+            lg = warp_dot<A, VPL>(uu_, hv);
+            nu = sqrt(uu);
+            cs = hx / nu;
+        };
+        for (uint32_t i = 0; i < R; ++i) {
+            load_mean(sbase + 2 + i, u);
+            A lg, cs, nu;
+            logits(u, lg, cs, nu);
+            if (lg > M) { Z = Z * exp(M - lg) + (A)1; M = lg; }
+            else Z += exp(lg - M);
+            if (ss) {
+                const A li = tau - (rd - cs);
+                if (li > 0) { ++P; lsum += li; }
+            }
+        }
+        const A pp = exp(lpos - M) / Z;
+        const bool rk = pp < tau;                 // rank term present
+        const bool under = rk && !(pp > 0);       // -ln 0: simple_grad's gradients are NaN
+        A L = (P ? lsum / (A)P : (A)0) + (rk ? -log(pp) : (A)0);
+        L = L / wdiv;
+        const bool is_nan = L != L;
+        const bool ok = !is_nan && L > 0;
+        const A inv = P ? (A)1 / (A)P : (A)0;
+        // pass 2: every negative's gradient; sums for h
+        A gs[VPL], gr[VPL];            // sum of kept normalised u (StarSpace), sum s_i u_i (rank)
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) { gs[k] = 0; gr[k] = 0; }
+        for (uint32_t i = 0; i < R; ++i) {
+            const uint64_t src = sbase + 2 + i;
+            load_mean(src, u);
+            A lg, cs, nu;
+            logits(u, lg, cs, nu);
+            const A si = exp(lg - M) / Z;
+            const bool kept = ss && tau - (rd - cs) > 0;
+            const A rnu = (A)1 / nu;
+            A d[VPL];
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) {
+                d[k] = rk ? si * hv[k] : (A)0;
+                if (rk) gr[k] += si * u[k];
+                if (kept) {
+                    const A un_k = u[k] * rnu;
+                    gs[k] += un_k;
+                    d[k] += (xh[k] - un_k * cs) * rnu * inv;
+                }
+            }
+            const bool fin = warp_all_finite<A, VPL>(d);
+            const bool em = ok && (rk || kept) && fin && !under;
+            if (em && lane_on) store_row<D, VPL, A>(dout + src * dpad, lane, d);
+            __syncwarp();
+            if (lane == 0) {
+                const A n_u = scale[src];
+                p.valid[src] = (uint8_t)em;
+                scale[src] = em ? up / (n_u * wdiv) : (A)0;
+            }
+        }
+        A dh[VPL], dt[VPL];
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+            dh[k] = rk ? gr[k] + (pp - (A)1) * tv[k] : (A)0;
+            dt[k] = rk ? (pp - (A)1) * hv[k] : (A)0;
+        }
+        if (P) {
+            A gtn[VPL], ghn[VPL];
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) {
+                gtn[k] = -xh[k];                       // P terms, each -h^, times 1/P
+                ghn[k] = (gs[k] - xa[k] * (A)P) * inv;
+            }
+            A st_, sh_;
+            warp_dot2<A, VPL>(xa, gtn, xh, ghn, st_, sh_);
+            const A rnt = (A)1 / nt, rnh = (A)1 / nh;
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) {
+                dt[k] += (gtn[k] - xa[k] * st_) * rnt;
+                dh[k] += (ghn[k] - xh[k] * sh_) * rnh;
+            }
+        }
+        const bool reach = rk || P;
+        const bool fin_h = warp_all_finite<A, VPL>(dh);
+        const bool fin_t = warp_all_finite<A, VPL>(dt);
+        if (lane_on) {
+            store_row<D, VPL, A>(dout + sbase * dpad, lane, dh);
+            store_row<D, VPL, A>(dout + (sbase + 1) * dpad, lane, dt);
+        }
+        if (lane == 0) {
+            p.valid[sbase] = (uint8_t)(ok && reach && fin_h && !under);
+            p.valid[sbase + 1] = (uint8_t)(ok && reach && fin_t && !under);
+            scale[sbase] = up / (n_h * wdiv);
+            scale[sbase + 1] = up / (n_t * wdiv);
+            if (p.loss_out) ((A*)p.loss_out)[a] = L;
+            p.status[a] = is_nan ? 2 : (ok ? 0 : 1);
+        }
+        return;
+    }
 
     A gsum[VPL];
 #pragma unroll
@@ -1057,8 +1223,6 @@ __global__ void __launch_bounds__(128) k_fwd_loss(ForwardParams p) {
     L = L / wdiv;
     const bool is_nan = L != L;
     const bool ok = !is_nan && L > 0;
-    A up = 1;
-    if (p.dloss) up = p.dloss_f64 ? (A)((const double*)p.dloss)[a] : (A)p.dloss[a];
     const A inv = n_terms ? (A)1 / (A)n_terms : (A)0;
 
     A dh[VPL], dt[VPL];
@@ -1228,20 +1392,22 @@ __global__ void k_convert(T* dev, float* host_layout, uint64_t n_feat, uint32_t 
 // ---------------------------------------------------------------------------
 // Set-up kernels.
 // k_node_bound: an upper bound on the items one anchor can emit:
-//   F(v) + R * maxF + (neighbour part): the exact sum of the neighbours'
+//   F(v) + R * maxF + (positive part): the exact sum of the neighbours'
 //   feature counts when all of them can be taken (All / Prob), else
-//   min(K, deg) * (largest neighbour feature count).
+//   min(K, deg) * (largest neighbour feature count); R * maxF for PPR walks.
 // k_split: train / validation ids as the first n_train / remaining positions
 //   of a seeded permutation of all nodes (mod.rs:118-122).
 // ---------------------------------------------------------------------------
 __global__ void k_node_bound(const uint64_t* row_ptr, const uint32_t* cols, const uint64_t* fptr, uint32_t n,
-                             int nodes_kind, uint32_t K, uint32_t R, uint32_t max_feat, uint32_t* bound) {
+                             int nodes_kind, uint32_t K, uint32_t R, uint32_t max_feat, int ppr, uint32_t* bound) {
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
     const uint64_t rs = row_ptr[v], re = row_ptr[v + 1];
     const uint64_t deg = re - rs;
     uint64_t nb = 0;
-    if (nodes_kind == S_FIXED && deg > K) {
+    if (ppr) {
+        nb = (uint64_t)R * max_feat;          // R walk end nodes
+    } else if (nodes_kind == S_FIXED && deg > K) {
         uint64_t mx = 0;
         for (uint64_t j = rs; j < re; ++j) { const uint32_t u = cols[j]; mx = max(mx, fptr[u + 1] - fptr[u]); }
         nb = (uint64_t)K * mx;
@@ -1265,8 +1431,9 @@ __global__ void k_split(uint32_t* train, uint32_t n_train, uint32_t* valid, uint
 }
 
 void launch_node_bound(const uint64_t* row_ptr, const uint32_t* cols, const uint64_t* fptr, uint32_t n,
-                       int nodes_kind, uint32_t K, uint32_t R, uint32_t max_feat, uint32_t* bound, cudaStream_t s) {
-    k_node_bound<<<(n + 255) / 256, 256, 0, s>>>(row_ptr, cols, fptr, n, nodes_kind, K, R, max_feat, bound);
+                       int nodes_kind, uint32_t K, uint32_t R, uint32_t max_feat, int ppr, uint32_t* bound,
+                       cudaStream_t s) {
+    k_node_bound<<<(n + 255) / 256, 256, 0, s>>>(row_ptr, cols, fptr, n, nodes_kind, K, R, max_feat, ppr, bound);
 }
 
 void launch_split(uint32_t* train, uint32_t n_train, uint32_t* valid, uint32_t n, uint64_t seed, uint32_t half,

@@ -79,6 +79,8 @@ struct SampleCfg {
     int weighted_sampling;  // weighted_neighbor_sampling (with weighted averaging: A-Res)
     FeatDrop fd;            // feature dropout of every role node
     uint32_t hard;          // hard negatives from random walks (0 = off)
+    int ppr;                // PPR loss: positives are R random-walk end nodes
+    float ppr_restart;      // its restart probability
     uint64_t seed;
 };
 
@@ -196,7 +198,7 @@ void launch_init_table(int tt, void* table, uint64_t n_feat, uint32_t dims, uint
 void launch_convert_table(int tt_dst, void* dst, const float* src, uint64_t n_feat,
                           uint32_t dims, uint32_t dpad, int to_device_layout, cudaStream_t s);
 void launch_node_bound(const uint64_t* row_ptr, const uint32_t* cols, const uint64_t* fptr, uint32_t n,
-                       int nodes_kind, uint32_t K, uint32_t R, uint32_t max_feat, uint32_t* bound,
+                       int nodes_kind, uint32_t K, uint32_t R, uint32_t max_feat, int ppr, uint32_t* bound,
                        cudaStream_t s);
 void launch_split(uint32_t* train, uint32_t n_train, uint32_t* valid, uint32_t n, uint64_t seed,
                   uint32_t half, uint32_t* err, cudaStream_t s);

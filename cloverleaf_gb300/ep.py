@@ -23,8 +23,10 @@ SEED = 20222022   # lib.rs:90
 
 
 class EPLoss:
-    """Loss choice (loss.rs:15-38).  On the GPU path: margin (Euclidean),
-    starspace (cosine margin) and contrastive."""
+    """Loss choice (loss.rs:15-38): margin (Euclidean), starspace (cosine
+    margin), contrastive, rank (softmax NLL of the positive with margin tau),
+    rankspace (starspace + rank) and ppr (margin with random-walk
+    positives)."""
 
     def __init__(self, kind: str, gamma: float, negatives: int, neg_margin: float = 0.0,
                  restart_p: Optional[float] = None):
@@ -56,11 +58,9 @@ class EPLoss:
         return EPLoss("ppr", gamma, max(1, negatives), restart_p=restart_p)
 
     def code(self) -> int:
-        codes = {"margin": _native.LOSS_MARGIN, "starspace": _native.LOSS_STARSPACE,
-                 "contrastive": _native.LOSS_CONTRASTIVE}
-        if self.kind not in codes:
-            raise _native.UnsupportedOption(-6, f"EPLoss.{self.kind} is not implemented on the GPU path")
-        return codes[self.kind]
+        return {"margin": _native.LOSS_MARGIN, "starspace": _native.LOSS_STARSPACE,
+                "contrastive": _native.LOSS_CONTRASTIVE, "rank": _native.LOSS_RANK,
+                "rankspace": _native.LOSS_RANKSPACE, "ppr": _native.LOSS_PPR}[self.kind]
 
     def __repr__(self) -> str:
         return f"EPLoss<{self.kind}({self.gamma}, {self.negatives})>"
@@ -144,6 +144,8 @@ class EmbeddingPropagator:
         cfg.loss = self.loss.code()
         cfg.gamma = self.loss.gamma
         cfg.neg_margin = self.loss.neg_margin
+        if self.loss.restart_p is not None:
+            cfg.ppr_restart_p = float(self.loss.restart_p)
         cfg.negatives = self.loss.negatives
         cfg.batch_size = self.batch_size
         cfg.dims = self.dims

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define EP_ABI_VERSION 1u
+#define EP_ABI_VERSION 2u
 
 typedef struct ep_ctx ep_ctx;
 
@@ -41,8 +41,17 @@ typedef enum ep_status {
     EP_ERR_NO_DEVICE = -7      /* no usable CUDA device */
 } ep_status;
 
-/* Loss (src/algos/ep/loss.rs:15-38, constructors src/lib.rs:988-1103). */
-enum { EP_LOSS_MARGIN = 0, EP_LOSS_STARSPACE = 1, EP_LOSS_CONTRASTIVE = 2 };
+/* Loss (src/algos/ep/loss.rs:15-38, constructors src/lib.rs:988-1103).
+ * RANK and RANKSPACE take tau in `gamma`; PPR is the margin loss with
+ * random-walk positives (`negatives` walks, restart `ppr_restart_p`). */
+enum {
+    EP_LOSS_MARGIN = 0,
+    EP_LOSS_STARSPACE = 1,
+    EP_LOSS_CONTRASTIVE = 2,
+    EP_LOSS_RANK = 3,
+    EP_LOSS_RANKSPACE = 4,
+    EP_LOSS_PPR = 5
+};
 /* Sample kind for max_nodes / max_features (src/algos/utils.rs:165-184). */
 enum { EP_SAMPLE_ALL = 0, EP_SAMPLE_FIXED = 1, EP_SAMPLE_PROB = 2 };
 /* Loss weighting (src/algos/ep/mod.rs:31-36, src/lib.rs:941-960). */
@@ -62,7 +71,7 @@ typedef struct ep_config {
     uint32_t abi_version;        /* must be EP_ABI_VERSION */
     float alpha;                 /* peak learning rate (lib.rs:1263, default 0.9) */
     int32_t loss;                /* EP_LOSS_* (default margin) */
-    float gamma;                 /* margin / positive margin (default 1) */
+    float gamma;                 /* margin / positive margin / tau (default 1) */
     float neg_margin;            /* contrastive negative margin */
     uint32_t negatives;          /* negatives per anchor (default 1) */
     uint32_t batch_size;         /* default 50 */
@@ -87,6 +96,7 @@ typedef struct ep_config {
     int32_t autotune;            /* pick launch shapes by timing candidates on the
                                     first training batches (see ep_get_tuning);
                                     results then depend on timing: default 0 */
+    float ppr_restart_p;         /* EP_LOSS_PPR walk restart probability in [0, 1] */
 } ep_config;
 
 typedef struct ep_pass_stats {

@@ -384,6 +384,27 @@ static int random_walk(uint32_t anchor, const uint64_t* rows, const uint32_t* co
     return 1;
 }
 
+/* random_walk of the PPR loss (loss.rs:190-222): at most max_steps uniform
+ * moves from the anchor; from the second move on the walk stops with
+ * probability p unless it stands on the anchor.  Yields the end node, or when
+ * that is the anchor a uniform neighbour of it; nothing when the anchor has
+ * no edges. */
+static int ppr_walk(uint32_t anchor, const uint64_t* rows, const uint32_t* cols, rng_t* r, float p,
+                    uint32_t max_steps, uint32_t* out) {
+    uint32_t node = anchor;
+    for (uint32_t i = 1;; ++i) {
+        const uint64_t s = rows[node], n = rows[(uint64_t)node + 1] - s;
+        if (n == 0 || i > max_steps) break;
+        node = cols[s + rng_below(r, n)];
+        if (i > 1 && rng_f32(r) < p && node != anchor) break;
+    }
+    if (node != anchor) { *out = node; return 1; }
+    const uint64_t as = rows[anchor], an = rows[(uint64_t)anchor + 1] - as;
+    if (an == 0) return 0;
+    *out = cols[as + rng_below(r, an)];
+    return 1;
+}
+
 /* run_forward_pass (mod.rs:289-327) building the role maps for anchor v. */
 static void build_roles(uint32_t v, const uint64_t* rows, const uint32_t* cols,
                         const uint64_t* fptr, const uint32_t* fids,
@@ -393,12 +414,30 @@ static void build_roles(uint32_t v, const uint64_t* rows, const uint32_t* cols,
     for (uint32_t q = 0; q < R + 2; ++q) fmap_clear(&s->maps[q]);
     /* h(v) */
     collect_node(&s->maps[0], fptr, fids, v, 1.f, cfg, r, s);
-    /* ~h(v): reconstruct_node_embedding (model.rs:342-386) */
+    /* ~h(v): reconstruct_node_embedding (model.rs:342-386), or for PPR the
+     * end nodes of R walks with weight 1 each, v itself when there are none
+     * (construct_positive, loss.rs:166-187) */
     uint64_t es = rows[v], deg = rows[(uint64_t)v + 1] - es;
     uint64_t ns;
     float sw;
-    sample_count(cfg->max_nodes_kind, cfg->max_nodes, deg, r, &ns, &sw);
-    if (deg == ns) {
+    if (cfg->loss.loss == ORC_LOSS_PPR) {
+        uint32_t got = 0;
+        for (uint32_t t = 0; t < R; ++t) {
+            uint32_t u;
+            if (ppr_walk(v, rows, cols, r, cfg->ppr_restart_p, 10, &u)) {
+                collect_node(&s->maps[1], fptr, fids, u, 1.f, cfg, r, s);
+                ++got;
+            }
+        }
+        if (!got) collect_node(&s->maps[1], fptr, fids, v, 1.f, cfg, r, s);
+        ns = deg = 0;
+        sw = 1.f;
+    } else {
+        sample_count(cfg->max_nodes_kind, cfg->max_nodes, deg, r, &ns, &sw);
+    }
+    if (cfg->loss.loss == ORC_LOSS_PPR) {
+        /* done above */
+    } else if (deg == ns) {
         for (uint64_t j = 0; j < deg; ++j) collect_node(&s->maps[1], fptr, fids, cols[es + j], sw, cfg, r, s);
     } else {
         /* reservoir_sample (utils.rs:128-145), including its Uniform(0, i) draw */

@@ -27,8 +27,18 @@
 extern "C" {
 #endif
 
-/* Loss kinds (src/algos/ep/loss.rs:15-38). */
-enum { ORC_LOSS_MARGIN = 0, ORC_LOSS_STARSPACE = 1, ORC_LOSS_CONTRASTIVE = 2 };
+/* Loss kinds (src/algos/ep/loss.rs:15-38).  RANK / RANKSPACE take tau in
+ * gamma; PPR is the margin loss whose positive role is built from random-walk
+ * end nodes (orc_train_cfg.ppr_restart_p; explicit samples give them as the
+ * neighbour list with weight 1). */
+enum {
+    ORC_LOSS_MARGIN = 0,
+    ORC_LOSS_STARSPACE = 1,
+    ORC_LOSS_CONTRASTIVE = 2,
+    ORC_LOSS_RANK = 3,
+    ORC_LOSS_RANKSPACE = 4,
+    ORC_LOSS_PPR = 5
+};
 /* Loss weighting (src/algos/ep/mod.rs:31-36). */
 enum { ORC_LW_NONE = 0, ORC_LW_LOG = 1, ORC_LW_EXP = 2 };
 /* Gradient extraction: reference = first finite occurrence of a feature
@@ -106,6 +116,7 @@ typedef struct orc_train_cfg {
     int32_t threads;        /* OpenMP threads, <= 0 means all */
     uint64_t max_batches;   /* stop after this many batches in total (0 = all) */
     uint32_t hard_negatives; /* random-walk negatives per anchor (node_sampler.rs:83-145) */
+    float ppr_restart_p;    /* ORC_LOSS_PPR walk restart probability (loss.rs:166-187) */
 } orc_train_cfg;
 
 typedef struct orc_train_stats {

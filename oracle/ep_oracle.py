@@ -36,7 +36,7 @@ _SOURCES = ("ep_oracle.c", "ep_oracle_batch.inc", "ep_oracle.h", "Makefile")
 _lock = threading.Lock()
 _lib = None
 
-LOSS_MARGIN, LOSS_STARSPACE, LOSS_CONTRASTIVE = 0, 1, 2
+LOSS_MARGIN, LOSS_STARSPACE, LOSS_CONTRASTIVE, LOSS_RANK, LOSS_RANKSPACE, LOSS_PPR = 0, 1, 2, 3, 4, 5
 LW_NONE, LW_LOG, LW_EXP = 0, 1, 2
 GRAD_REFERENCE, GRAD_TRUE = 0, 1
 SAMPLE_ALL, SAMPLE_FIXED, SAMPLE_PROB = 0, 1, 2
@@ -79,6 +79,7 @@ class TrainCfg(ctypes.Structure):
         ("threads", ctypes.c_int32),
         ("max_batches", ctypes.c_uint64),
         ("hard_negatives", ctypes.c_uint32),
+        ("ppr_restart_p", ctypes.c_float),
     ]
 
 
@@ -205,7 +206,8 @@ def adam(table, m, v, grad, touched, lr, pass_idx):
 def train(rows, cols, wcdf, fptr, fids, n_feat, *, dims, alpha, loss=LOSS_STARSPACE, gamma=0.5,
           neg_margin=0.0, negatives=5, batch_size=256, passes=5, seed=20222022,
           max_nodes=(SAMPLE_ALL, 0.0), max_features=(SAMPLE_ALL, 0.0), valid_pct=0.0,
-          loss_weighting=LW_NONE, lw_exp=1.0, threads=0, max_batches=0, init_table=None, hard_negatives=0):
+          loss_weighting=LW_NONE, lw_exp=1.0, threads=0, max_batches=0, init_table=None, hard_negatives=0,
+          ppr_restart_p=0.5):
     """The whole reference training loop (mod.rs:92-287) on host cores.
     Returns (table[n_feat, dims], TrainStats)."""
     rows = _c(rows, np.uint64)
@@ -227,6 +229,7 @@ def train(rows, cols, wcdf, fptr, fids, n_feat, *, dims, alpha, loss=LOSS_STARSP
     cfg.threads = threads
     cfg.max_batches = max_batches
     cfg.hard_negatives = hard_negatives
+    cfg.ppr_restart_p = ppr_restart_p
     if init_table is not None:
         table = _c(init_table, np.float32).copy()
         given = 1
@@ -299,15 +302,17 @@ def batch_autograd(fptr, fids, n_feat, table, graph_rows, anchors, nbr_ptr, nbr,
         maps += [role([(int(neg[a, i]), 1.0)]) for i in range(R)]
         hv, thv = mean(maps[0]), mean(maps[1])
         hus = [mean(m) for m in maps[2:]]
-        if loss == LOSS_MARGIN:
+        if loss in (LOSS_MARGIN, LOSS_PPR):
             d1 = gamma + l2(thv - hv)
             terms = [d1 - l2(thv - hu) for hu in hus]
             terms = [t for t in terms if t.item() > 0]
-        elif loss == LOSS_STARSPACE:
+        elif loss in (LOSS_STARSPACE, LOSS_RANKSPACE):
             tn, hn = thv / l2(thv), hv / l2(hv)
             rd = tn.dot(hn)
             terms = [torch.clamp(gamma - (rd - hn.dot(hu / l2(hu))), min=0.0) for hu in hus]
             terms = [t for t in terms if t.item() > 0]
+        elif loss == LOSS_RANK:
+            terms = []
         else:
             tn, hn = thv / l2(thv), hv / l2(hv)
             pos = torch.clamp(gamma - tn.dot(hn), min=0.0)
@@ -316,6 +321,14 @@ def batch_autograd(fptr, fids, n_feat, table, graph_rows, anchors, nbr_ptr, nbr,
             if pos.item() > 0:
                 terms.append(pos)
         L = torch.stack(terms).sum() / len(terms) if terms else torch.zeros((), dtype=dtype)
+        if loss in (LOSS_RANK, LOSS_RANKSPACE):
+            # RankLoss (loss.rs:130-155) with the exact softmax; the max is a
+            # constant outside the graph, as in attention.rs:283-296
+            ds = torch.stack([hu.dot(hv) for hu in hus] + [hv.dot(thv)])
+            n = torch.exp(ds - ds.max().detach())
+            pr = (n / n.sum())[-1]
+            if pr.item() < gamma:
+                L = L - torch.log(pr)
         if loss_weighting != LW_NONE:
             deg = float(graph_rows[v + 1] - graph_rows[v])
             L = L / (np.log(1.0 + deg) if loss_weighting == LW_LOG else deg ** lw_exp)

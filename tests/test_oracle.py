@@ -97,13 +97,13 @@ def test_l2norm_known_answer(oracle):
     np.testing.assert_allclose(grad[2], gu, atol=1e-7)
 
 
-@pytest.mark.parametrize("loss", [0, 1, 2])
+@pytest.mark.parametrize("loss", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("grad_mode", [0, 1])
 @pytest.mark.parametrize("weighting", [0, 1, 2])
 def test_c_oracle_matches_autograd(oracle, loss, grad_mode, weighting):
     prob = random_problem(7 + loss, n=80, n_feat=50, dims=8)
     smp = sample_batch(11 + grad_mode, prob, B=24, K=3, R=4, weighted=weighting == 2)
-    gamma = 1.0 if loss == 0 else 0.5
+    gamma = {0: 1.0, 3: 0.3, 4: 0.3, 5: 1.0}.get(loss, 0.5)      # rank losses: tau
     cfg = oracle.loss_cfg(loss=loss, gamma=gamma, neg_margin=0.1, grad_mode=grad_mode, loss_weighting=weighting,
                           lw_exp=0.5)
     args = (prob["fptr"], prob["fids"], prob["n_feat"], prob["table"], prob["rows"], smp["anchors"], smp["nbr_ptr"],
@@ -117,6 +117,26 @@ def test_c_oracle_matches_autograd(oracle, loss, grad_mode, weighting):
     l32, s32, g32, t32 = oracle.batch(*args, cfg, "f32")
     assert (s32 == sa).all()
     assert rel_err(g32, ga) < 1e-5
+
+
+def test_rank_loss_known_answer(oracle):
+    # h = [1, 0], t = [.5, .5], u = [0, 1]: logits u.h = 0 and h.t = .5, so
+    # p = e^.5 / (1 + e^.5); L = -ln p (p < tau = .9); dL/du = (1 - p) h,
+    # dL/dt = (p - 1) h, dL/dh = (1 - p) u + (p - 1) t (loss.rs:130-155)
+    table = np.array([[1.0, 0.0], [0.5, 0.5], [0.0, 1.0]], np.float32)
+    fptr = np.array([0, 1, 2, 3], np.uint64)
+    fids = np.array([0, 1, 2], np.uint32)
+    rows = np.array([0, 1, 2, 3], np.uint64)
+    args = (fptr, fids, 3, table, rows, [0], [0, 1], [1], [1.0], [[2]])
+    loss, st, g, t = oracle.batch(*args, oracle.loss_cfg(loss=oracle.LOSS_RANK, gamma=0.9), "f64")
+    p = math.exp(0.5) / (1 + math.exp(0.5))
+    assert st.tolist() == [0] and abs(loss[0] + math.log(p)) < 1e-7
+    np.testing.assert_allclose(g[2], [1 - p, 0], atol=1e-7)
+    np.testing.assert_allclose(g[1], [p - 1, 0], atol=1e-7)
+    np.testing.assert_allclose(g[0], [(p - 1) * 0.5, (1 - p) + (p - 1) * 0.5], atol=1e-7)
+    # p >= tau: no loss, no gradient
+    loss, st, g, t = oracle.batch(*args, oracle.loss_cfg(loss=oracle.LOSS_RANK, gamma=0.5), "f64")
+    assert st.tolist() == [1] and not t.any()
 
 
 def test_first_occurrence_rule(oracle):
