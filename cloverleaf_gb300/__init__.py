@@ -5,6 +5,7 @@ same Python classes and keyword arguments, with training executed by
 hand-written CUDA kernels behind the C ABI in ``include/ep_gb300.h``.
 """
 from ._native import NativeError, UnsupportedOption
+from .alignment import NeighborhoodAligner
 from .embeddings import Distance, FeatureAggregator, NodeEmbedder, NodeEmbeddings
 from .ep import EmbeddingPropagator, EPLoss, LossWeighting
 from .features import FeatureNamespace, FeatureSet
@@ -12,7 +13,8 @@ from .graph import EdgeType, Graph, GraphBuilder, Vocab
 
 __all__ = [
     "Distance", "EdgeType", "EmbeddingPropagator", "EPLoss", "FeatureAggregator", "FeatureNamespace", "FeatureSet",
-    "Graph", "GraphBuilder", "LossWeighting", "NativeError", "NodeEmbedder", "NodeEmbeddings", "UnsupportedOption",
+    "Graph", "GraphBuilder", "LossWeighting", "NativeError", "NeighborhoodAligner", "NodeEmbedder", "NodeEmbeddings",
+    "UnsupportedOption",
     "Vocab", "build",
 ]
 

@@ -143,6 +143,7 @@ SIGNATURES = {
     "ep_sample": (ctypes.c_int, [_P, _P, _U32, _U32, _U32, _P, _P, _P, _P]),
     "ep_embed_features": (ctypes.c_int, [ctypes.c_int, _U64, _P, _P, _P, _U32, _U32, _P, _P]),
     "ep_knn_cosine": (ctypes.c_int, [ctypes.c_int, _U64, _U32, _P, _U64, _P, _P, _U32, _P, _P]),
+    "ep_align": (ctypes.c_int, [ctypes.c_int, _U64, _P, _P, _P, _U32, _P, ctypes.c_float, _U64, _P]),
     "ep_knn_last_error": (ctypes.c_char_p, []),
     "ep_knn_last_kernel_ms": (ctypes.c_float, []),
     "ep_ag_forward": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), ctypes.c_int, _P, _P, _P]),
@@ -360,6 +361,21 @@ def embed_features(fptr, fids, table, weights=None, device=0):
     out = np.zeros((n, table.shape[1]), np.float32)
     _knn_check(lib().ep_embed_features(int(device), n, ptr(fptr), ptr(fids), ptr(w), table.shape[0], table.shape[1],
                                        ptr(table), ptr(out)), "ep_embed_features")
+    return out
+
+
+def align(row_ptr, cols, w_cdf, emb, alpha=None, max_neighbors=None, device=0):
+    """GPU NeighborhoodAligner (``ep_align``): each node blended with the
+    probability-weighted sum of its first max_neighbors neighbours' rows;
+    alpha None = adaptive."""
+    rp = np.ascontiguousarray(row_ptr, np.uint64)
+    c = np.ascontiguousarray(cols, np.uint32)
+    w = np.ascontiguousarray(w_cdf, np.float32)
+    e = np.ascontiguousarray(emb, np.float32)
+    n = len(rp) - 1
+    out = np.zeros((n, e.shape[1]), np.float32)
+    _knn_check(lib().ep_align(int(device), n, ptr(rp), ptr(c), ptr(w), e.shape[1], ptr(e),
+                              -1.0 if alpha is None else float(alpha), int(max_neighbors or 0), ptr(out)), "ep_align")
     return out
 
 

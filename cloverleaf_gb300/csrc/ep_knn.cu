@@ -4,6 +4,8 @@
 //   ep_embed_features  NodeEmbedder.embed_feature_set (src/lib.rs:2092-2124)
 //                      with AvgAggregator / WeightedAggregator
 //                      (src/algos/aggregator.rs:17-120): warp per node.
+//   ep_align           NeighborhoodAligner.align (src/algos/alignment.rs,
+//                      src/lib.rs:3040-3110): warp per node.
 //   ep_knn_cosine      NodeEmbeddings.nearest_neighbor for many queries at
 //                      once (src/embeddings.rs:149-173, cosine distance):
 //                      rows normalised to BF16, then a tcgen05 GEMM (FP32
@@ -26,7 +28,7 @@ namespace ep {
 namespace {
 
 thread_local std::string g_knn_err;
-thread_local float g_knn_ms = 0.f;     // CUDA-event time of the last top-k kernel
+thread_local float g_knn_ms = 0.f;     // CUDA-event time of the last top-k or alignment kernel
 
 int knn_fail(int code, const char* msg) {
     g_knn_err = msg;
@@ -82,6 +84,45 @@ __global__ void __launch_bounds__(256) k_embed(uint64_t n, const uint64_t* __res
     for (int i = 0; i < 16; ++i) {
         const uint32_t k = (uint32_t)lane + 32u * i;
         if (k < d) out[v * d + k] = e > b ? acc[i] / wsum : 0.f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Neighbourhood alignment (NeighborhoodAligner.align, src/algos/alignment.rs:
+// 25-75): out[v] = (1 - a) * sum_j p_j E[u_j] + a * E[v] over the first
+// min(deg, kmax) edges in CSR order, p_j the edge probability recovered from
+// the CDF weights (w_0, w_j - w_{j-1}), a = alpha, or min(1, 1 / ln(deg + 1))
+// when alpha < 0.  f32 as the reference: every product rounded, then added,
+// per element in edge order.  Warp per node, up to 16 elements per lane.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_align(uint64_t n, const uint64_t* __restrict__ rp,
+                                               const uint32_t* __restrict__ cols, const float* __restrict__ cdf,
+                                               uint32_t d, const float* __restrict__ E, float alpha, uint64_t kmax,
+                                               float* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t v = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (v >= n) return;
+    float acc[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) acc[i] = 0.f;
+    const uint64_t b = rp[v], deg = rp[v + 1] - b;
+    const uint64_t m = deg < kmax ? deg : kmax;
+    for (uint64_t j = 0; j < m; ++j) {
+        const float p = j ? __fsub_rn(cdf[b + j], cdf[b + j - 1]) : cdf[b];
+        const float* row = E + (uint64_t)cols[b + j] * d;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const uint32_t k = (uint32_t)lane + 32u * i;
+            if (k < d) acc[i] = __fadd_rn(acc[i], __fmul_rn(p, row[k]));
+        }
+    }
+    const float a = alpha >= 0.f ? alpha : fminf(__fdiv_rn(1.f, logf(__fadd_rn((float)deg, 1.f))), 1.f);
+    const float c = __fsub_rn(1.f, a);
+    const float* own = E + v * d;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const uint32_t k = (uint32_t)lane + 32u * i;
+        if (k < d) out[v * d + k] = __fadd_rn(__fmul_rn(acc[i], c), __fmul_rn(own[k], a));
     }
 }
 
@@ -599,6 +640,51 @@ extern "C" int ep_embed_features(int device, uint64_t n_nodes, const uint64_t* f
     KCK(cudaGetLastError(), "embed launch");
     KCK(cudaMemcpyAsync(out, dout.p, (size_t)n_nodes * dims * 4, cudaMemcpyDeviceToHost, s), "download");
     KCK(cudaStreamSynchronize(s), "embed");
+    return EP_OK;
+}
+
+extern "C" int ep_align(int device, uint64_t n_nodes, const uint64_t* row_ptr, const uint32_t* cols,
+                        const float* w_cdf, uint32_t dims, const float* emb, float alpha, uint64_t max_neighbors,
+                        float* out) {
+    if (!row_ptr || (n_nodes && (!emb || !out)) || dims == 0 || dims > 512)
+        return knn_fail(EP_ERR_INVALID_ARG, "invalid arguments (dims must be in [1, 512])");
+    if (alpha > 1.f || alpha != alpha) return knn_fail(EP_ERR_INVALID_ARG, "alpha must be <= 1 (negative: adaptive)");
+    const uint64_t ne = row_ptr[n_nodes];
+    if (ne && (!cols || !w_cdf)) return knn_fail(EP_ERR_INVALID_ARG, "null edge arrays");
+    for (uint64_t v = 0; v < n_nodes; ++v)
+        if (row_ptr[v + 1] < row_ptr[v]) return knn_fail(EP_ERR_INVALID_ARG, "row_ptr is not monotone");
+    for (uint64_t j = 0; j < ne; ++j)
+        if (cols[j] >= n_nodes) return knn_fail(EP_ERR_INVALID_ARG, "column id out of range");
+    KCK(cudaSetDevice(device), "select device");
+    if (!n_nodes) return EP_OK;
+    cudaStream_t s;
+    KCK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+    struct SG { cudaStream_t s; ~SG() { cudaStreamDestroy(s); } } sg{s};
+    DevMem drp, dcols, dcdf, demb, dout;
+    KCK(drp.alloc((n_nodes + 1) * 8), "alloc");
+    KCK(dcols.alloc(ne * 4), "alloc");
+    KCK(dcdf.alloc(ne * 4), "alloc");
+    KCK(demb.alloc((size_t)n_nodes * dims * 4), "alloc");
+    KCK(dout.alloc((size_t)n_nodes * dims * 4), "alloc");
+    KCK(cudaMemcpyAsync(drp.p, row_ptr, (n_nodes + 1) * 8, cudaMemcpyHostToDevice, s), "upload");
+    if (ne) {
+        KCK(cudaMemcpyAsync(dcols.p, cols, ne * 4, cudaMemcpyHostToDevice, s), "upload");
+        KCK(cudaMemcpyAsync(dcdf.p, w_cdf, ne * 4, cudaMemcpyHostToDevice, s), "upload");
+    }
+    KCK(cudaMemcpyAsync(demb.p, emb, (size_t)n_nodes * dims * 4, cudaMemcpyHostToDevice, s), "upload");
+    cudaEvent_t e0, e1;
+    KCK(cudaEventCreate(&e0), "events");
+    KCK(cudaEventCreate(&e1), "events");
+    struct EG { cudaEvent_t a, b; ~EG() { cudaEventDestroy(a); cudaEventDestroy(b); } } eg{e0, e1};
+    cudaEventRecord(e0, s);
+    k_align<<<(unsigned)((n_nodes * 32 + 255) / 256), 256, 0, s>>>(
+        n_nodes, (const uint64_t*)drp.p, (const uint32_t*)dcols.p, (const float*)dcdf.p, dims,
+        (const float*)demb.p, alpha, max_neighbors ? max_neighbors : ~0ull, (float*)dout.p);
+    cudaEventRecord(e1, s);
+    KCK(cudaGetLastError(), "align launch");
+    KCK(cudaMemcpyAsync(out, dout.p, (size_t)n_nodes * dims * 4, cudaMemcpyDeviceToHost, s), "download");
+    KCK(cudaStreamSynchronize(s), "align");
+    cudaEventElapsedTime(&g_knn_ms, e0, e1);
     return EP_OK;
 }
 

@@ -285,12 +285,23 @@ int ep_embed_features(int device, uint64_t n_nodes, const uint64_t* fptr, const 
 int ep_knn_cosine(int device, uint64_t n_db, uint32_t dims, const float* db, uint64_t n_q, const float* q,
                   const uint64_t* q_self, uint32_t k, uint32_t* idx_out, float* sim_out);
 
-/* Message of the last failing ep_embed_features / ep_knn_cosine call of this
- * host thread. */
+/* NeighborhoodAligner.align (src/algos/alignment.rs:25-75, src/lib.rs:
+ * 3040-3110): out[v] = (1 - a) * sum_j p_j emb[cols[j]] + a * emb[v] over
+ * the first min(deg, max_neighbors) edges of v (max_neighbors 0 = all), p_j
+ * the edge probabilities of the CDF weights w_cdf, a = alpha, or
+ * min(1, 1 / ln(deg + 1)) when alpha < 0.  f32 arithmetic in the reference's
+ * order.  A node without edges gets a * emb[v] (the reference indexes the
+ * empty weight list).  emb / out: n_nodes x dims (<= 512).  Host buffers. */
+int ep_align(int device, uint64_t n_nodes, const uint64_t* row_ptr, const uint32_t* cols, const float* w_cdf,
+             uint32_t dims, const float* emb, float alpha, uint64_t max_neighbors, float* out);
+
+/* Message of the last failing ep_embed_features / ep_align / ep_knn_cosine
+ * call of this host thread. */
 const char* ep_knn_last_error(void);
 
 /* Measurement hook (no counterpart in the reference): CUDA-event time in ms
- * of the top-k kernel of this host thread's last ep_knn_cosine call. */
+ * of the GPU kernel of this host thread's last ep_knn_cosine (the top-k
+ * kernel) or ep_align call. */
 float ep_knn_last_kernel_ms(void);
 
 /* ---- host-side graph construction (src/graph.rs) --------------------- */

@@ -357,3 +357,37 @@ def batch_autograd(fptr, fids, n_feat, table, graph_rows, anchors, nbr_ptr, nbr,
                 grad[f] += g
                 touched[f] = True
     return losses, status, grad, touched
+
+
+# ---------------------------------------------------------------------------
+# Neighbourhood alignment (src/algos/alignment.rs:25-75), f32 as the reference
+# ---------------------------------------------------------------------------
+def align(rows, cols, wcdf, emb, alpha=None, max_neighbors=None):
+    """out[v] = (1 - a) * sum_j p_j emb[cols[j]] + a * emb[v] over the first
+    max_neighbors edges of v in CSR order; p_j = w_0, w_j - w_{j-1} from the
+    CDF weights; a = alpha or min(1, 1 / ln(deg + 1)).  Every product is
+    rounded to f32 before it is added, element by element in edge order.  A
+    node without edges gets a * emb[v] (the reference indexes the empty
+    weight list there)."""
+    rows = np.asarray(rows, np.uint64)
+    cols = np.asarray(cols, np.int64)
+    wcdf = np.asarray(wcdf, np.float32)
+    emb = np.asarray(emb, np.float32)
+    n, d = emb.shape
+    out = np.zeros_like(emb)
+    one = np.float32(1)
+    for v in range(len(rows) - 1):
+        s, e = int(rows[v]), int(rows[v + 1])
+        deg = e - s
+        m = deg if max_neighbors is None else min(deg, int(max_neighbors))
+        acc = np.zeros(d, np.float32)
+        for j in range(m):
+            p = wcdf[s] if j == 0 else np.float32(wcdf[s + j] - wcdf[s + j - 1])
+            acc = acc + p * emb[cols[s + j]]
+        if alpha is None:
+            with np.errstate(divide="ignore"):
+                a = np.float32(min(np.float32(one / np.log(np.float32(deg) + one)), one))
+        else:
+            a = np.float32(alpha)
+        out[v] = acc * (one - a) + emb[v] * a
+    return out

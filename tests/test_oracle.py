@@ -205,3 +205,24 @@ def test_oracle_training_learns_communities(oracle):
     assert st.batches == 5 * 40 and st.anchors == 5 * 10_000
     r = community_recall(w["fptr"], w["fids"], table, w["community"])
     assert r > 0.5, r
+
+
+def test_align_known_answer(oracle):
+    # node 0 -> (1, p=.25), (2, p=.75); node 1 -> (0, p=1); node 2 no edges
+    rows = np.array([0, 2, 3, 3], np.uint64)
+    cols = np.array([1, 2, 0], np.uint32)
+    wcdf = np.array([0.25, 1.0, 1.0], np.float32)
+    emb = np.array([[1.0, 0.0], [0.0, 2.0], [4.0, 4.0]], np.float32)
+    out = oracle.align(rows, cols, wcdf, emb, alpha=0.5)
+    np.testing.assert_allclose(out[0], 0.5 * (0.25 * emb[1] + 0.75 * emb[2]) + 0.5 * emb[0], atol=1e-7)
+    np.testing.assert_allclose(out[1], 0.5 * emb[0] + 0.5 * emb[1], atol=1e-7)
+    np.testing.assert_allclose(out[2], 0.5 * emb[2], atol=1e-7)
+    # max_neighbors 1: only the first edge, its probability not renormalised
+    out = oracle.align(rows, cols, wcdf, emb, alpha=0.0, max_neighbors=1)
+    np.testing.assert_allclose(out[0], 0.25 * emb[1], atol=1e-7)
+    # adaptive: a = min(1, 1/ln(deg + 1)); deg 2 -> 1/ln 3, deg 1 -> 1 (1/ln 2 > 1)
+    out = oracle.align(rows, cols, wcdf, emb)
+    a = 1 / math.log(3)
+    np.testing.assert_allclose(out[0], (1 - a) * (0.25 * emb[1] + 0.75 * emb[2]) + a * emb[0], rtol=1e-6)
+    np.testing.assert_allclose(out[1], emb[1], atol=1e-7)
+    np.testing.assert_allclose(out[2], emb[2], atol=1e-7)
