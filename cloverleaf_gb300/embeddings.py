@@ -3,8 +3,9 @@
 Mirrors ``src/lib.rs:2009-2207`` (NodeEmbedder), ``:2536-2900``
 (NodeEmbeddings), ``src/embeddings.rs:24-173`` (EmbeddingStore),
 ``src/distance.rs:132-198`` (distances) and ``src/algos/aggregator.rs:17-120``
-(Averaged / Weighted aggregators).  These run on the host with numpy: they
-are the inputs and outputs around the GPU training path, not part of it.
+(Averaged / Weighted aggregators).  NodeEmbedder.embed_feature_set and
+NodeEmbeddings.nearest_neighbors (many queries) run on the GPU through the C
+ABI; vocabularies, text I/O and single-query lookups stay on the host.
 """
 from __future__ import annotations
 
@@ -13,6 +14,7 @@ from typing import Iterator, List, Optional, Sequence, Tuple, Union
 
 import numpy as np
 
+from . import _native
 from .graph import FQNode, Graph, Vocab, _node_id
 
 
@@ -159,6 +161,17 @@ class NodeEmbeddings:
         idx = idx[np.argsort(d[idx], kind="stable")]
         return [(self.vocab_.get_name(int(i)), float(d[i])) for i in idx]
 
+    def nearest_neighbors(self, queries, k: int, exclude=None, device: int = 0):
+        """Exact cosine top-k of many query vectors at once on the tensor
+        cores (``ep_knn_cosine``): (row ids [n_q, k], cosine distances
+        1 - cos [n_q, k]) in increasing distance; exclude[i] names a row to
+        skip for query i.  Rows are compared after rounding the unit vectors
+        to BF16.  For a Cosine store, k <= 32, dims <= 256."""
+        if self.distance is not Distance.Cosine:
+            raise _native.UnsupportedOption(-6, "batched nearest neighbours are implemented for cosine distance")
+        ids, sim = _native.knn_cosine(self.table, queries, k, exclude, device)
+        return ids, (np.float32(1) - sim).astype(np.float32)
+
     def save(self, path: str, comp_level: Optional[int] = None) -> None:
         """``node_type\\tname\\t[v1,v2,...]`` lines (io.rs:44-76)."""
         import gzip
@@ -242,25 +255,29 @@ class NodeEmbedder:
                 tr[i] = j
         return fptr, tr[fids]
 
-    def embed_feature_set(self, feat_set, feature_embeddings: NodeEmbeddings) -> NodeEmbeddings:
-        """Mean (or SIF-weighted mean) of each node's feature rows;
-        nodes without known features stay zero (lib.rs:2092-2124)."""
+    def embed_feature_set(self, feat_set, feature_embeddings: NodeEmbeddings, device: int = 0) -> NodeEmbeddings:
+        """Mean (or SIF-weighted mean) of each node's known feature rows on the
+        GPU (``ep_embed_features``); nodes without known features stay zero
+        (lib.rs:2092-2124).  As the reference, the SIF weight of a feature is
+        looked up by its row in feature_embeddings (aggregator.rs:103-110)."""
         fptr, ids = self._translate(feat_set, feature_embeddings)
         T = feature_embeddings.table
         n = len(fptr) - 1
         node = np.repeat(np.arange(n), np.diff(fptr).astype(np.int64))
         keep = ids >= 0
-        node, ids = node[keep], ids[keep]
+        kept = np.zeros(n + 1, np.uint64)
+        kept[1:] = np.cumsum(np.bincount(node[keep], minlength=n))
+        ids = ids[keep]
+        fw = None
         if self.feat_agg.kind == "weighted":
-            p = self.feat_agg.unigrams
-            w = (self.feat_agg.alpha / (self.feat_agg.alpha + p[ids])).astype(np.float32)
-        else:
-            w = np.ones(len(ids), np.float32)
-        out = np.zeros((n, T.shape[1]), np.float32)
-        np.add.at(out, node, T[ids] * w[:, None])
-        den = np.bincount(node, weights=w, minlength=n).astype(np.float32)
-        nz = den > 0
-        out[nz] /= den[nz, None]
+            p = np.asarray(self.feat_agg.unigrams, np.float32)
+            if len(ids) and ids.max() >= len(p):
+                raise IndexError("a feature row beyond the aggregator's unigram table")
+            a = np.float32(self.feat_agg.alpha)
+            fw = np.ones(T.shape[0], np.float32)
+            m = min(len(p), T.shape[0])
+            fw[:m] = a / (a + p[:m])
+        out = _native.embed_features(kept, ids.astype(np.uint32), T, fw, device)
         return NodeEmbeddings(feat_set.vocab_, out, Distance.Cosine)
 
     def embed_adhoc(self, features: Sequence[FQNode], feature_embeddings: NodeEmbeddings,

@@ -133,3 +133,57 @@ def test_knn_cosine_fewer_rows_than_k():
         assert (idx[i, n_ok:] == 0xFFFFFFFF).all() and np.isneginf(sim[i, n_ok:]).all()
     e_idx, e_sim = _native.knn_cosine(np.zeros((0, 48), np.float32), q, 4)
     assert (e_idx == 0xFFFFFFFF).all() and np.isneginf(e_sim).all()
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_node_embedder_class_translates_vocabularies(weighted):
+    # NodeEmbedder.embed_feature_set (lib.rs:2092-2124) through the Python
+    # class: feature ids are translated into the embeddings' own vocabulary,
+    # features it lacks are skipped, and SIF weights are looked up by the
+    # translated row (aggregator.rs:103-110)
+    import cloverleaf_gb300 as cl
+    from tests._cases import random_problem
+    prob = random_problem(8, n=500, n_feat=120, dims=4)
+    g = cl.Graph.from_csr(prob["rows"], prob["cols"])
+    fs = cl.FeatureSet.from_csr(g, prob["fptr"], prob["fids"], prob["n_feat"])
+    rng = np.random.default_rng(9)
+    order = rng.permutation(120)[:100]             # 20 features unknown to the embeddings
+    ev = cl.Vocab()
+    for f in order.tolist():
+        ev.get_or_insert("feat", str(f))
+    table = rng.standard_normal((100, 48)).astype(np.float32)
+    femb = cl.NodeEmbeddings(ev, table)
+    agg = cl.FeatureAggregator.Weighted(0.1, fs) if weighted else cl.FeatureAggregator.Averaged()
+    out = cl.NodeEmbedder(agg).embed_feature_set(fs, femb)
+    tr = np.full(120, -1, np.int64)
+    tr[order] = np.arange(100)
+    fptr, fids = prob["fptr"], prob["fids"]
+    kept_ptr, kept = [0], []
+    for v in range(500):
+        t = [int(tr[f]) for f in fids[int(fptr[v]):int(fptr[v + 1])] if tr[f] >= 0]
+        kept += t
+        kept_ptr.append(len(kept))
+    w = None
+    if weighted:
+        a = np.float32(0.1)
+        w = a / (a + agg.unigrams[:100])
+    want = _ref_embed(np.array(kept_ptr, np.uint64), np.array(kept, np.uint32), table, w)
+    assert np.array_equal(out.table, want)
+    assert out.vocab_ is fs.vocab_
+
+
+def test_nearest_neighbors_batch_matches_exact():
+    import cloverleaf_gb300 as cl
+    rng = np.random.default_rng(21)
+    table = rng.standard_normal((3000, 64)).astype(np.float32)
+    e = cl.NodeEmbeddings(cl.Vocab.anonymous(3000), table)
+    ids, dist = e.nearest_neighbors(table[:200], 5, exclude=np.arange(200))
+    S = _exact(table, table[:200])
+    S[np.arange(200), np.arange(200)] = -np.inf
+    kth = -np.sort(-S, axis=1)[:, 4]
+    ex = S[np.arange(200)[:, None], ids.astype(np.int64)]
+    assert (ex >= kth[:, None] - TOL_BF16).all()
+    assert np.abs((1 - ex) - dist).max() < TOL_BF16
+    assert (np.diff(dist, axis=1) >= 0).all()
+    with pytest.raises(cl.UnsupportedOption):
+        cl.NodeEmbeddings(e.vocab_, table, cl.Distance.Euclidean).nearest_neighbors(table[:2], 3)
