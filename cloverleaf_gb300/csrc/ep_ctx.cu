@@ -81,6 +81,7 @@ struct ep_ctx {
     DevBuf anchors, nbr, nbr_w, nbr_cnt, neg, occ, dir, dir16, scale, valid, loss, status, deferred;
     DevBuf item_f, item_src, item_c, key_alt, idx, idx_alt, hist;
     DevBuf carry_head, carry_tail, carry_f, carry_flags, long_list, gdense, touched, n_touched, packed, xfer, bound;
+    DevBuf check;   // CSR validation result / bound histogram scratch
     uint64_t items_cap = 0;
     uint32_t buf_B = 0, buf_K = 0, buf_es = 0;
     uint32_t chunk = 128;
@@ -243,19 +244,48 @@ extern "C" void ep_destroy(ep_ctx* c) {
     delete c;
 }
 
-static int check_csr(ep_ctx* c, uint64_t n, const uint64_t* ptr, const uint32_t* ids, uint64_t id_bound,
-                     const char* what, uint32_t* max_row) {
-    if (ptr[0] != 0) return c->fail(EP_ERR_INVALID_ARG, "%s: row pointer must start at 0", what);
-    uint64_t mx = 0;
-    for (uint64_t i = 0; i < n; ++i) {
-        if (ptr[i + 1] < ptr[i]) return c->fail(EP_ERR_INVALID_ARG, "%s: row pointers decrease at row %llu", what, (unsigned long long)i);
-        mx = std::max<uint64_t>(mx, ptr[i + 1] - ptr[i]);
+// CSR validation on the device, after the upload: row pointers must not
+// decrease and every id must be below id_bound.  The first offending row and
+// id position (or ~0) and the longest row come back in one small copy.
+struct CsrCheck {
+    unsigned long long bad_row, bad_id, max_row;
+};
+
+__global__ void k_check_csr(uint64_t n, const uint64_t* __restrict__ ptr, const uint32_t* __restrict__ ids,
+                            uint64_t m, uint64_t id_bound, CsrCheck* out) {
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+    unsigned long long mx = 0;
+    for (uint64_t i = tid; i < n; i += stride) {
+        const uint64_t a = ptr[i], b = ptr[i + 1];
+        if (b < a) atomicMin(&out->bad_row, (unsigned long long)i);
+        else mx = b - a > mx ? b - a : mx;
     }
-    const uint64_t m = ptr[n];
-    for (uint64_t j = 0; j < m; ++j)
-        if (ids[j] >= id_bound) return c->fail(EP_ERR_INVALID_ARG, "%s: id %u at %llu out of range", what, ids[j], (unsigned long long)j);
-    if (mx > 0xffffffffull) return c->fail(EP_ERR_INVALID_ARG, "%s: row too long", what);
-    *max_row = (uint32_t)mx;
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = y > mx ? y : mx;
+    }
+    if ((threadIdx.x & 31) == 0 && mx) atomicMax(&out->max_row, mx);
+    for (uint64_t j = tid; j < m; j += stride)
+        if (ids[j] >= id_bound) atomicMin(&out->bad_id, (unsigned long long)j);
+}
+
+// Runs k_check_csr over uploaded arrays; fails with the first offence.
+static int check_csr(ep_ctx* c, uint64_t n, const uint64_t* d_ptr, const uint32_t* d_ids, uint64_t m,
+                     uint64_t id_bound, const char* what, uint32_t* max_row) {
+    if (!c->check.ensure(65536 * 12)) return c->fail(EP_ERR_OOM, "scratch allocation failed");
+    CsrCheck* dc = c->check.as<CsrCheck>();
+    const CsrCheck init{~0ull, ~0ull, 0ull};
+    CK(cudaMemcpyAsync(dc, &init, sizeof(init), cudaMemcpyHostToDevice, c->stream), "validate");
+    k_check_csr<<<152 * 8, 256, 0, c->stream>>>(n, d_ptr, d_ids, m, id_bound, dc);
+    CK(cudaGetLastError(), "validate");
+    CsrCheck r;
+    CK(cudaMemcpyAsync(&r, dc, sizeof(r), cudaMemcpyDeviceToHost, c->stream), "validate");
+    CK(cudaStreamSynchronize(c->stream), "validate");
+    if (r.bad_row != ~0ull)
+        return c->fail(EP_ERR_INVALID_ARG, "%s: row pointers decrease at row %llu", what, r.bad_row);
+    if (r.bad_id != ~0ull) return c->fail(EP_ERR_INVALID_ARG, "%s: id at %llu out of range", what, r.bad_id);
+    if (r.max_row > 0xffffffffull) return c->fail(EP_ERR_INVALID_ARG, "%s: row too long", what);
+    *max_row = (uint32_t)r.max_row;
     return EP_OK;
 }
 
@@ -265,18 +295,21 @@ extern "C" int ep_upload_graph(ep_ctx* c, uint64_t n_nodes, const uint64_t* row_
     if (!row_ptr || (!cols && n_nodes && row_ptr[n_nodes])) return c->fail(EP_ERR_INVALID_ARG, "null graph arrays");
     if (n_nodes == 0 || n_nodes > 0xfffffffeull) return c->fail(EP_ERR_INVALID_ARG, "n_nodes must be in [1, 2^32-1)");
     if (c->feats_ok && n_nodes != c->n_nodes) return c->fail(EP_ERR_INVALID_ARG, "graph and features disagree on node count");
-    uint32_t mx = 0;
-    int rc = check_csr(c, n_nodes, row_ptr, cols, n_nodes, "graph", &mx);
-    if (rc) return rc;
+    if (row_ptr[0] != 0) return c->fail(EP_ERR_INVALID_ARG, "graph: row pointer must start at 0");
     cudaSetDevice(c->device);
     const uint64_t E = row_ptr[n_nodes];
+    c->graph_ok = false;     // the device copy is replaced below; valid again once checked
+    c->prepared = false;
+    c->drop_graph();
     if (!c->row.ensure((n_nodes + 1) * 8) || !c->cols.ensure(E * 4) || !c->wcdf.ensure(E * 4))
         return c->fail(EP_ERR_OOM, "graph allocation failed");
     CK(cudaMemcpyAsync(c->row.p, row_ptr, (n_nodes + 1) * 8, cudaMemcpyHostToDevice, c->stream), "upload row_ptr");
     if (E) CK(cudaMemcpyAsync(c->cols.p, cols, E * 4, cudaMemcpyHostToDevice, c->stream), "upload cols");
     if (E && w_cdf) CK(cudaMemcpyAsync(c->wcdf.p, w_cdf, E * 4, cudaMemcpyHostToDevice, c->stream), "upload weights");
     c->has_w = w_cdf != nullptr;
-    CK(cudaStreamSynchronize(c->stream), "upload graph");
+    uint32_t mx = 0;
+    int rc = check_csr(c, n_nodes, c->row.as<uint64_t>(), c->cols.as<uint32_t>(), E, n_nodes, "graph", &mx);
+    if (rc) return rc;
     c->n_nodes = n_nodes;
     c->n_edges = E;
     c->max_deg = mx;
@@ -293,15 +326,18 @@ extern "C" int ep_upload_features(ep_ctx* c, uint64_t n_nodes, const uint64_t* f
     if (n_nodes == 0 || n_nodes > 0xfffffffeull) return c->fail(EP_ERR_INVALID_ARG, "n_nodes must be in [1, 2^32-1)");
     if (c->graph_ok && n_nodes != c->n_nodes) return c->fail(EP_ERR_INVALID_ARG, "graph and features disagree on node count");
     if (n_feat == 0) return c->fail(EP_ERR_INVALID_ARG, "n_feat must be > 0");
-    uint32_t mx = 0;
-    int rc = check_csr(c, n_nodes, fptr, fids, n_feat, "features", &mx);
-    if (rc) return rc;
+    if (fptr[0] != 0) return c->fail(EP_ERR_INVALID_ARG, "features: row pointer must start at 0");
     cudaSetDevice(c->device);
     const uint64_t F = fptr[n_nodes];
+    c->feats_ok = false;     // the device copy is replaced below; valid again once checked
+    c->prepared = false;
+    c->drop_graph();
     if (!c->fptr.ensure((n_nodes + 1) * 8) || !c->fids.ensure(F * 4)) return c->fail(EP_ERR_OOM, "feature allocation failed");
     CK(cudaMemcpyAsync(c->fptr.p, fptr, (n_nodes + 1) * 8, cudaMemcpyHostToDevice, c->stream), "upload fptr");
     if (F) CK(cudaMemcpyAsync(c->fids.p, fids, F * 4, cudaMemcpyHostToDevice, c->stream), "upload fids");
-    CK(cudaStreamSynchronize(c->stream), "upload features");
+    uint32_t mx = 0;
+    int rc = check_csr(c, n_nodes, c->fptr.as<uint64_t>(), c->fids.as<uint32_t>(), F, n_feat, "features", &mx);
+    if (rc) return rc;
     if (c->table_ok && n_feat != c->n_feat) c->table_ok = false;
     c->n_nodes = n_nodes;
     c->n_fids = F;
@@ -421,6 +457,71 @@ static uint32_t feistel_half(uint64_t n) {
 constexpr uint32_t kTuneChunks[3] = {64, 128, 256};
 constexpr uint32_t kTuneWarm = 2, kTuneTimed = 8;
 
+// An upper bound of the sum of the `top` largest per-anchor item bounds,
+// without copying the n bounds to the host: a 65,536-bin histogram of
+// bound >> shift (count and sum per bin) is walked from the top; the bins
+// taken whole add their exact sums, the partial bin its upper edge per
+// anchor.  Exact when every bound is below 65,536.
+__global__ void k_bound_max(const uint32_t* __restrict__ b, uint32_t n, uint32_t* mx) {
+    uint32_t m = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = max(m, b[i]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(mx, m);
+}
+
+// Warp-aggregated: the lanes holding the same bin add once (their sum split
+// into 16-bit halves so that 32 lanes cannot overflow a word).
+__global__ void k_bound_hist(const uint32_t* __restrict__ b, uint32_t n, uint32_t shift, uint32_t* cnt,
+                             unsigned long long* sum) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * blockDim.x / 32;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) / 32 * 32; base < n; base += warps * 32) {
+        const uint32_t i = base + lane;
+        const bool ok = i < n;                      // the whole warp iterates together
+        const uint32_t x = ok ? b[i] : 0u;
+        const uint32_t bin = ok ? x >> shift : 0xffffffffu;
+        const unsigned peers = __match_any_sync(0xffffffffu, bin);
+        const uint32_t lo = __reduce_add_sync(peers, x & 0xffffu), hi = __reduce_add_sync(peers, x >> 16);
+        if (ok && lane == __ffs(peers) - 1) {
+            atomicAdd(&cnt[bin], (uint32_t)__popc(peers));
+            atomicAdd(&sum[bin], ((unsigned long long)hi << 16) + lo);
+        }
+    }
+}
+
+static int top_sum_bound(ep_ctx* c, uint32_t n, uint32_t top, uint64_t* out) {
+    constexpr uint32_t BINS = 65536;
+    if (!c->check.ensure((size_t)BINS * 12 + 16)) return c->fail(EP_ERR_OOM, "scratch allocation failed");
+    unsigned long long* sum = c->check.as<unsigned long long>();
+    uint32_t* cnt = (uint32_t*)(sum + BINS);
+    uint32_t* dmx = cnt + BINS;
+    const uint32_t* b = c->bound.as<uint32_t>();
+    CK(cudaMemsetAsync(c->check.p, 0, (size_t)BINS * 12 + 16, c->stream), "bounds");
+    k_bound_max<<<152 * 4, 256, 0, c->stream>>>(b, n, dmx);
+    uint32_t mx = 0;
+    CK(cudaMemcpyAsync(&mx, dmx, 4, cudaMemcpyDeviceToHost, c->stream), "bounds");
+    CK(cudaStreamSynchronize(c->stream), "bounds");
+    uint32_t bits = 0;
+    while (bits < 32 && (mx >> bits)) ++bits;
+    const uint32_t shift = bits > 16 ? bits - 16 : 0;
+    k_bound_hist<<<152 * 4, 256, 0, c->stream>>>(b, n, shift, cnt, sum);
+    CK(cudaGetLastError(), "bounds");
+    std::vector<uint32_t> hc(BINS);
+    std::vector<unsigned long long> hs(BINS);
+    CK(cudaMemcpyAsync(hc.data(), cnt, (size_t)BINS * 4, cudaMemcpyDeviceToHost, c->stream), "bounds");
+    CK(cudaMemcpyAsync(hs.data(), sum, (size_t)BINS * 8, cudaMemcpyDeviceToHost, c->stream), "bounds");
+    CK(cudaStreamSynchronize(c->stream), "bounds");
+    uint64_t items = 0, left = top;
+    for (int64_t bin = BINS - 1; bin >= 0 && left; --bin) {
+        const uint64_t k = std::min<uint64_t>(hc[bin], left);
+        if (k == hc[bin]) items += hs[bin];
+        else items += k * ((((uint64_t)bin + 1) << shift) - 1);
+        left -= k;
+    }
+    *out = items;
+    return EP_OK;
+}
+
 static int prepare_train(ep_ctx* c) {
     if (!c->graph_ok || !c->feats_ok) return c->fail(EP_ERR_STATE, "upload the graph and the features first");
     if (!c->table_ok) return c->fail(EP_ERR_STATE, "set the table first");
@@ -448,13 +549,9 @@ static int prepare_train(ep_ctx* c) {
     launch_node_bound(c->row.as<uint64_t>(), c->cols.as<uint32_t>(), c->fptr.as<uint64_t>(), n, c->cfg.max_nodes_kind,
                       (uint32_t)c->cfg.max_nodes, c->R, c->max_feat, c->cfg.loss == EP_LOSS_PPR,
                       c->bound.as<uint32_t>(), c->stream);
-    std::vector<uint32_t> hb(n);
-    CK(cudaMemcpyAsync(hb.data(), c->bound.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream), "bounds");
-    CK(cudaStreamSynchronize(c->stream), "bounds");
-    const uint32_t top = std::min<uint32_t>(B, n);
-    std::nth_element(hb.begin(), hb.begin() + (top - 1), hb.end(), std::greater<uint32_t>());
     uint64_t items = 0;
-    for (uint32_t i = 0; i < top; ++i) items += hb[i];
+    int rcb = top_sum_bound(c, n, std::min<uint32_t>(B, n), &items);
+    if (rcb) return rcb;
     if (items > 0xfffffff0ull) return c->fail(EP_ERR_UNSUPPORTED, "a batch can emit more than 2^32 gradient items");
     // with the autotuner, size the reducer carries for its smallest chunk and
     // keep the dense gradient buffers for the split Adam placement

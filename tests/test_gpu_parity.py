@@ -179,7 +179,23 @@ def test_bad_inputs_fail_cleanly():
     cfg = _native.default_config()
     cfg.dims = 8
     c2 = _native.Context(cfg)
-    with pytest.raises(_native.NativeError):
+    with pytest.raises(_native.NativeError) as e:
         c2.upload_graph(bad["rows"], bad["cols"], None)
+    assert "out of range" in str(e.value)
+    rows = prob["rows"].copy()
+    rows[6] = rows[5] - 1              # every row has an edge, so rows[5] >= 5
+    with pytest.raises(_native.NativeError) as e:
+        c2.upload_graph(rows, prob["cols"], None)
+    assert "decrease at row 5" in str(e.value)
+    fids = prob["fids"].copy()
+    fids[-1] = prob["n_feat"]
+    with pytest.raises(_native.NativeError) as e:
+        c2.upload_features(prob["fptr"], fids, prob["n_feat"])
+    assert "out of range" in str(e.value)
     with pytest.raises(_native.NativeError):
-        c2.train(1)         # nothing uploaded
+        c2.train(1)         # nothing valid uploaded
+    # a context recovers from a rejected upload
+    c2.upload_graph(prob["rows"], prob["cols"], None)
+    c2.upload_features(prob["fptr"], prob["fids"], prob["n_feat"])
+    c2.set_table(prob["table"])
+    assert c2.train(1)[0]["anchors"] > 0
