@@ -191,24 +191,28 @@ constexpr uint32_t KNN_WAIT_LIMIT = 1u << 22;    // mbarrier polls (32 ns sleeps
 enum : uint32_t { KNN_ERR_TIMEOUT = 1u };
 
 // This warp's TMEM lane quarter, columns taddr .. taddr + N - 1 (one 32-bit
-// value per column) into r; waits for the load.
-__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[32]) {
+// value per column) into r, and the largest of the thread's N values in mx:
+// the reducing TMEM load of sm_103a, so that a block's skip test costs no
+// instructions.  The caller waits for the load.
+__device__ __forceinline__ void tmem_ld_max(uint32_t taddr, uint32_t (&r)[32], float& mx) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        "tcgen05.ld.red.sync.aligned.32x32b.x32.max.f32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, %32, [%33];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
           "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
           "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
-          "=r"(r[30]), "=r"(r[31])
+          "=r"(r[30]), "=r"(r[31]), "=f"(mx)
         : "r"(taddr)
         : "memory");
 }
-__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[16]) {
+__device__ __forceinline__ void tmem_ld_max(uint32_t taddr, uint32_t (&r)[16], float& mx) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        "tcgen05.ld.red.sync.aligned.32x32b.x16.max.f32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+        "%16, [%17];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=f"(mx)
         : "r"(taddr)
         : "memory");
 }
@@ -322,32 +326,6 @@ __device__ __forceinline__ void topk_push(float (&vals)[KMAX], uint32_t (&ids)[K
             ids[i - 1] = ti;
         }
     }
-}
-
-__device__ __forceinline__ float fmax3(float a, float b, float c) {
-    float r;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-
-// Largest of N floats held as bits in registers (N a multiple of 8): four
-// interleaved chains of three-input maxima, 8 instructions for 16 values and
-// 16 for 32, with few extra registers and short dependency chains.
-template <int N>
-__device__ __forceinline__ float max_of(const uint32_t (&r)[N]) {
-    static_assert(N >= 8 && N % 8 == 0, "N a multiple of 8");
-    auto x = [&](int t) { return __uint_as_float(r[t]); };
-    float m[4] = {x(0), x(1), x(2), x(3)};
-    int i = 4;
-#pragma unroll
-    for (; i + 7 < N; i += 8) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) m[j] = fmax3(m[j], x(i + 2 * j), x(i + 2 * j + 1));
-    }
-    // the last 4 values
-    m[0] = fmax3(m[0], x(i), x(i + 1));
-    m[1] = fmax3(m[1], x(i + 2), x(i + 3));
-    return fmaxf(fmax3(m[0], m[1], m[2]), m[3]);
 }
 
 // k-th largest of a list sorted in descending order (k in [1, KMAX]): the
@@ -492,7 +470,8 @@ __global__ void __launch_bounds__(KnnRoles<KMAX>::THREADS, 1)
                 __syncwarp();
                 uint32_t r[R::BW];
                 const uint32_t cofs = (uint32_t)(slice * R::CW + bl * R::BW);
-                tmem_ld(tmem + acc * KNN_BN + cofs + ((uint32_t)(32 * quarter) << 16), r);
+                float bmax;
+                tmem_ld_max(tmem + acc * KNN_BN + cofs + ((uint32_t)(32 * quarter) << 16), r, bmax);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 if (bl == R::BLOCKS - 1) {
                     // release the accumulator: this warp's values are all in registers
@@ -501,7 +480,7 @@ __global__ void __launch_bounds__(KnnRoles<KMAX>::THREADS, 1)
                     if (lane == 0) mbar_arrive(&bar_acc_free[acc]);
                 }
                 // the block's largest similarity first: most blocks cannot enter
-                if (max_of<R::BW>(r) > thr) {
+                if (bmax > thr) {
                     unsigned cand = 0;
 #pragma unroll
                     for (int t = 0; t < R::BW; ++t) cand |= (__uint_as_float(r[t]) > thr ? 1u : 0u) << t;
