@@ -363,6 +363,8 @@ def embed_features(fptr, fids, table, weights=None, device=0):
     table = np.ascontiguousarray(table, np.float32)
     w = None if weights is None else np.ascontiguousarray(weights, np.float32)
     n = len(fptr) - 1
+    if table.ndim != 2 or (n and int(fptr[-1]) != len(fids)) or (w is not None and len(w) != table.shape[0]):
+        raise ValueError("fptr / fids / table / weights shapes disagree")
     out = np.zeros((n, table.shape[1]), np.float32)
     _knn_check(lib().ep_embed_features(int(device), n, ptr(fptr), ptr(fids), ptr(w), table.shape[0], table.shape[1],
                                        ptr(table), ptr(out)), "ep_embed_features")
@@ -378,6 +380,10 @@ def align(row_ptr, cols, w_cdf, emb, alpha=None, max_neighbors=None, device=0):
     w = np.ascontiguousarray(w_cdf, np.float32)
     e = np.ascontiguousarray(emb, np.float32)
     n = len(rp) - 1
+    if e.ndim != 2 or e.shape[0] != n:
+        raise ValueError(f"emb must hold one row per node: shape {e.shape} for {n} nodes")
+    if len(w) != len(c) or (n and int(rp[-1]) != len(c)):
+        raise ValueError("row_ptr, cols and w_cdf disagree on the edge count")
     out = np.zeros((n, e.shape[1]), np.float32)
     _knn_check(lib().ep_align(int(device), n, ptr(rp), ptr(c), ptr(w), e.shape[1], ptr(e),
                               -1.0 if alpha is None else float(alpha), int(max_neighbors or 0), ptr(out)), "ep_align")
@@ -389,7 +395,11 @@ def knn_cosine(db, queries, k, q_self=None, device=0):
     (ids[n_q, k], similarities[n_q, k]) in decreasing similarity."""
     db = np.ascontiguousarray(db, np.float32)
     q = np.ascontiguousarray(queries, np.float32)
+    if db.ndim != 2 or q.ndim != 2 or db.shape[1] != q.shape[1]:
+        raise ValueError(f"db {db.shape} and queries {q.shape} must be 2-D with the same width")
     qs = None if q_self is None else np.ascontiguousarray(q_self, np.uint64)
+    if qs is not None and qs.shape != (len(q),):
+        raise ValueError("q_self must hold one entry per query")
     idx = np.zeros((len(q), k), np.uint32)
     sim = np.zeros((len(q), k), np.float32)
     _knn_check(lib().ep_knn_cosine(int(device), len(db), db.shape[1], ptr(db), len(q), ptr(q), ptr(qs), int(k),

@@ -192,3 +192,20 @@ def test_embeddings_io_roundtrip(tmp_path):
     nn = e.nearest_neighbor(t[2], 2)
     assert nn[0][0] == ("feat", "f2")
     assert cl.Distance.Euclidean.compute([1, 3], [3, 5]) == pytest.approx(8 ** 0.5)   # loss.rs:250-255
+
+
+def test_evaluation_wrappers_check_shapes():
+    # shape errors are caught before any host array is read past its end
+    rows = np.array([0, 1, 2], np.uint64)
+    cols = np.array([1, 0], np.uint32)
+    cdf = np.ones(2, np.float32)
+    with pytest.raises(ValueError):
+        _native.align(rows, cols, cdf, np.zeros((3, 4), np.float32))
+    with pytest.raises(ValueError):
+        _native.align(rows, cols, cdf[:1], np.zeros((2, 4), np.float32))
+    with pytest.raises(ValueError):
+        _native.knn_cosine(np.zeros((5, 8), np.float32), np.zeros((2, 7), np.float32), 3)
+    with pytest.raises(ValueError):
+        _native.knn_cosine(np.zeros((5, 8), np.float32), np.zeros((2, 8), np.float32), 3, q_self=[0])
+    with pytest.raises(ValueError):
+        _native.embed_features(np.array([0, 3], np.uint64), np.array([0, 1], np.uint32), np.zeros((4, 8), np.float32))
