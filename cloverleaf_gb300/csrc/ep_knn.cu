@@ -465,38 +465,60 @@ __global__ void __launch_bounds__(KnnRoles<KMAX>::THREADS, 1)
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll 1
-            for (int bl = 0; bl < R::BLOCKS; ++bl) {
+            // Blocks are software-pipelined where registers allow (16-column
+            // blocks): block bl+1's TMEM load is in flight while block bl is
+            // scanned, with two register sets alternating.  32-column blocks
+            // (k > 16) load and wait one block at a time.
+            constexpr int NB = R::BW <= 16 ? 2 : 1;
+            uint32_t r[NB][R::BW];
+            float bmax[NB];
+            const uint32_t tl = tmem + acc * KNN_BN + (uint32_t)(slice * R::CW) + ((uint32_t)(32 * quarter) << 16);
+            if constexpr (NB == 2) {
                 __syncwarp();
-                uint32_t r[R::BW];
-                const uint32_t cofs = (uint32_t)(slice * R::CW + bl * R::BW);
-                float bmax;
-                tmem_ld_max(tmem + acc * KNN_BN + cofs + ((uint32_t)(32 * quarter) << 16), r, bmax);
+                tmem_ld_max(tl, r[0], bmax[0]);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (bl == R::BLOCKS - 1) {
+            }
+            // (unrolled only when pipelined: four copies of the 32-entry
+            // insertion path would not fit the instruction cache)
+            constexpr int UNR = NB == 2 ? R::BLOCKS : 1;
+#pragma unroll UNR
+            for (int bl = 0; bl < R::BLOCKS; ++bl) {
+                const int cb = NB == 2 ? (bl & 1) : 0;
+                __syncwarp();
+                if constexpr (NB == 1) {
+                    tmem_ld_max(tl + (uint32_t)(bl * R::BW), r[0], bmax[0]);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                }
+                if (NB == 2 && bl + 1 < R::BLOCKS) {
+                    tmem_ld_max(tl + (uint32_t)((bl + 1) * R::BW), r[(cb ^ 1) % NB], bmax[(cb ^ 1) % NB]);
+                } else if (bl + 1 == R::BLOCKS) {
                     // release the accumulator: this warp's values are all in registers
                     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&bar_acc_free[acc]);
                 }
                 // the block's largest similarity first: most blocks cannot enter
-                if (bmax > thr) {
+                if (bmax[cb] > thr) {
                     unsigned cand = 0;
 #pragma unroll
-                    for (int t = 0; t < R::BW; ++t) cand |= (__uint_as_float(r[t]) > thr ? 1u : 0u) << t;
-                    const uint32_t col0 = (uint32_t)j * KNN_BN + cofs;
+                    for (int t = 0; t < R::BW; ++t) cand |= (__uint_as_float(r[cb][t]) > thr ? 1u : 0u) << t;
+                    const uint32_t col0 = (uint32_t)j * KNN_BN + (uint32_t)(slice * R::CW + bl * R::BW);
                     while (cand) {
                         const int t = __ffs(cand) - 1;
                         cand &= cand - 1;
-                        float v = __uint_as_float(r[0]);
+                        float v = __uint_as_float(r[cb][0]);
 #pragma unroll
-                        for (int u = 1; u < R::BW; ++u) v = t == u ? __uint_as_float(r[u]) : v;
+                        for (int u = 1; u < R::BW; ++u) v = t == u ? __uint_as_float(r[cb][u]) : v;
                         const uint32_t col = col0 + (uint32_t)t;
                         if (v > thr && col < ndb32 && col != self) {
                             topk_push<KMAX>(vals, ids, v, col);
                             thr = kth_value<KMAX>(vals, k);
                         }
                     }
+                }
+                if (NB == 2 && bl + 1 < R::BLOCKS) {
+                    __syncwarp();
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 }
             }
         }
