@@ -192,11 +192,6 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
         g_create_err = "probability max_features must be in (0, 1)";
         return EP_ERR_INVALID_ARG;
     }
-    if (cfg->loss != EP_LOSS_PPR && cfg->weighted_neighbor_sampling && cfg->weighted_neighbor_averaging &&
-        (cfg->max_nodes_kind == EP_SAMPLE_PROB || (cfg->max_nodes_kind == EP_SAMPLE_FIXED && cfg->max_nodes > 32.f))) {
-        g_create_err = "weighted neighbour sampling with weighted averaging is implemented for max_nodes <= 32 (Fixed) or all";
-        return EP_ERR_UNSUPPORTED;
-    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();

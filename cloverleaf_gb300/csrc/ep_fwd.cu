@@ -179,9 +179,130 @@ __global__ void k_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, ui
 }
 
 // ---------------------------------------------------------------------------
+// Weighted neighbour sampling with weighted averaging: weighted_reservoir_
+// sample (utils.rs:147-161) with the averaging weights w_i = scale * p_i * deg
+// (CDFtoP, graph.rs:630-661) keeps the r positions with the largest
+// U_i^(1/w_i) (Efraimidis-Spirakis A-Res), compared here as log(U_i) / w_i.
+// Both selectors write the chosen positions (as float bits) to outw[0, r)
+// and their node ids to out[0, r); the caller turns positions into weights.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float ares_key(const SampleParams& p, uint64_t rs, uint32_t i, uint32_t deg, float sw,
+                                          uint32_t v, uint32_t salt) {
+    const float pi = p.wcdf[rs + i] - (i ? p.wcdf[rs + i - 1] : 0.f);
+    const float wi = sw * pi * (float)deg;
+    const float u = ((float)(rand_u32(p.cfg.seed, v, salt, ST_WRES, i) >> 8) + 0.5f) * (1.0f / 16777216.0f);
+    return wi > 0.f ? __logf(u) / wi : -INFINITY;
+}
+
+// r <= 32: lane t < r holds one member of the running set; 32 candidates at a
+// time enter while they beat the set's smallest key.
+__device__ void ares_small(const SampleParams& p, uint64_t rs, uint32_t deg, float sw, uint32_t r, uint32_t v,
+                           uint32_t salt, uint32_t* out, float* outw, int lane) {
+    float skey = -INFINITY;
+    uint32_t spos = 0xffffffffu;
+    if ((uint32_t)lane < r) { spos = (uint32_t)lane; skey = ares_key(p, rs, lane, deg, sw, v, salt); }
+    for (uint32_t base = r; base < deg; base += 32) {
+        const uint32_t i = base + lane;
+        float ck = i < deg ? ares_key(p, rs, i, deg, sw, v, salt) : -INFINITY;
+        for (uint32_t guard = 0; guard <= 32; ++guard) {
+            // the set's smallest key and the lane holding it
+            float mk = (uint32_t)lane < r ? skey : INFINITY;
+            int ml = lane;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ok2 = __shfl_xor_sync(FULL, mk, o);
+                const int ol = __shfl_xor_sync(FULL, ml, o);
+                if (ok2 < mk || (ok2 == mk && ol < ml)) { mk = ok2; ml = ol; }
+            }
+            const bool better = ck > mk;
+            if (!__ballot_sync(FULL, better)) break;
+            // the best candidate replaces the smallest member
+            float bk = better ? ck : -INFINITY;
+            int bl = lane;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ok2 = __shfl_xor_sync(FULL, bk, o);
+                const int ol = __shfl_xor_sync(FULL, bl, o);
+                if (ok2 > bk || (ok2 == bk && ol < bl)) { bk = ok2; bl = ol; }
+            }
+            const uint32_t bpos = __shfl_sync(FULL, i, bl);
+            if (lane == ml) { skey = bk; spos = bpos; }
+            if (lane == bl) ck = -INFINITY;
+        }
+    }
+    if ((uint32_t)lane < r) { out[lane] = p.cols[rs + spos]; outw[lane] = __uint_as_float(spos); }
+}
+
+// Order-preserving image of a float key as an unsigned integer.
+__device__ __forceinline__ uint32_t key_ord(float k) {
+    const uint32_t b = __float_as_uint(k);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+// Any r < deg: the r-th largest key by an MSB-first radix select over key_ord
+// (four 8-bit passes over a 256-bin warp histogram in shared memory, the keys
+// recomputed from the same draws each pass), then every position above that
+// key plus the lowest-placed ties, in position order.
+__device__ void ares_select(const SampleParams& p, uint64_t rs, uint32_t deg, float sw, uint32_t r, uint32_t v,
+                            uint32_t salt, uint32_t* out, float* outw, uint32_t* hist, int lane) {
+    uint32_t prefix = 0, pmask = 0, need = r;        // need: rank of the target within the prefix group
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        for (uint32_t b = lane; b < 256; b += 32) hist[b] = 0;
+        __syncwarp();
+        for (uint32_t i0 = 0; i0 < deg; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            if (i < deg) {
+                const uint32_t o = key_ord(ares_key(p, rs, i, deg, sw, v, salt));
+                if ((o & pmask) == prefix) atomicAdd(&hist[(o >> shift) & 255u], 1u);
+            }
+        }
+        __syncwarp();
+        // bins from the top: lane l holds bins 255 - 8l ... 248 - 8l
+        uint32_t cnt[8], tot = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) { cnt[j] = hist[255 - (lane * 8 + j)]; tot += cnt[j]; }
+        const uint32_t incl = warp_incl_scan(tot, lane), excl = incl - tot;
+        const unsigned hit = __ballot_sync(FULL, excl < need && need <= incl);
+        const int L = __ffs(hit) - 1;                 // need <= group size, so one lane holds it
+        uint32_t dig = 0, above = 0;
+        if (lane == L) {
+            uint32_t acc = excl;
+            for (int j = 0; j < 8; ++j) {
+                if (acc + cnt[j] >= need) { dig = 255u - (uint32_t)(lane * 8 + j); above = acc; break; }
+                acc += cnt[j];
+            }
+        }
+        dig = __shfl_sync(FULL, dig, L);
+        above = __shfl_sync(FULL, above, L);
+        need -= above;
+        prefix |= dig << shift;
+        pmask |= 255u << shift;
+        __syncwarp();
+    }
+    // prefix: the r-th largest image; need: how many of its ties to keep
+    uint32_t taken = 0, ties = 0;
+    for (uint32_t i0 = 0; i0 < deg && taken < r; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const uint32_t o = i < deg ? key_ord(ares_key(p, rs, i, deg, sw, v, salt)) : 0u;
+        const bool eq = i < deg && o == prefix;
+        const unsigned em = __ballot_sync(FULL, eq);
+        const bool take = (i < deg && o > prefix) || (eq && ties + __popc(em & ((1u << lane) - 1u)) < need);
+        const unsigned tm = __ballot_sync(FULL, take);
+        if (take) {
+            const uint32_t slot = taken + __popc(tm & ((1u << lane) - 1u));
+            out[slot] = p.cols[rs + i];
+            outw[slot] = __uint_as_float(i);
+        }
+        taken += __popc(tm);
+        ties += __popc(em);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // k_sample: one warp per anchor.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
+    __shared__ uint32_t s_hist[8][256];   // per warp: ares_select's histogram
     pdl_wait();
     pdl_trigger();
     const int lane = threadIdx.x & 31;
@@ -265,52 +386,9 @@ __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
             sw = (float)deg / (float)r;
             if (r == deg) {
                 take_all = 1;
-            } else if (c.weighted_sampling && c.weighted_avg && p.wcdf && r <= 32) {
-                // weighted_reservoir_sample (utils.rs:147-161) with the
-                // averaging weights w_i = scale * p_i * deg: the r positions
-                // with the largest U_i^(1/w_i) (Efraimidis-Spirakis A-Res),
-                // compared as log(U_i) / w_i.  Lane t < r holds one member of
-                // the running set; 32 candidates at a time enter while they
-                // beat the set's smallest key.
-                auto key = [&](uint32_t i) -> float {
-                    const float pi = p.wcdf[rs + i] - (i ? p.wcdf[rs + i - 1] : 0.f);
-                    const float wi = sw * pi * (float)deg;
-                    const float u = ((float)(rand_u32(c.seed, v, salt, ST_WRES, i) >> 8) + 0.5f) * (1.0f / 16777216.0f);
-                    return wi > 0.f ? __logf(u) / wi : -INFINITY;
-                };
-                float skey = -INFINITY;
-                uint32_t spos = 0xffffffffu;
-                if ((uint32_t)lane < r) { spos = (uint32_t)lane; skey = key(lane); }
-                for (uint32_t base = r; base < deg; base += 32) {
-                    const uint32_t i = base + lane;
-                    float ck = i < deg ? key(i) : -INFINITY;
-                    for (uint32_t guard = 0; guard <= 32; ++guard) {
-                        // the set's smallest key and the lane holding it
-                        float mk = (uint32_t)lane < r ? skey : INFINITY;
-                        int ml = lane;
-#pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) {
-                            const float ok2 = __shfl_xor_sync(FULL, mk, o);
-                            const int ol = __shfl_xor_sync(FULL, ml, o);
-                            if (ok2 < mk || (ok2 == mk && ol < ml)) { mk = ok2; ml = ol; }
-                        }
-                        const bool better = ck > mk;
-                        if (!__ballot_sync(FULL, better)) break;
-                        // the best candidate replaces the smallest member
-                        float bk = better ? ck : -INFINITY;
-                        int bl = lane;
-#pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) {
-                            const float ok2 = __shfl_xor_sync(FULL, bk, o);
-                            const int ol = __shfl_xor_sync(FULL, bl, o);
-                            if (ok2 > bk || (ok2 == bk && ol < bl)) { bk = ok2; bl = ol; }
-                        }
-                        const uint32_t bpos = __shfl_sync(FULL, i, bl);
-                        if (lane == ml) { skey = bk; spos = bpos; }
-                        if (lane == bl) ck = -INFINITY;
-                    }
-                }
-                if ((uint32_t)lane < r) { out[lane] = p.cols[rs + spos]; outw[lane] = __uint_as_float(spos); }
+            } else if (c.weighted_sampling && c.weighted_avg && p.wcdf) {
+                if (r <= 32) ares_small(p, rs, deg, sw, r, v, salt, out, outw, lane);
+                else ares_select(p, rs, deg, sw, r, v, salt, out, outw, s_hist[(threadIdx.x >> 5) & 7], lane);
                 cnt = r;
             } else if (r <= 32) {
                 // Floyd's algorithm: a uniform r-subset of [0, deg); lane i
@@ -344,6 +422,28 @@ __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
                     outw[q] = __uint_as_float(pos2);
                     out[q] = p.cols[rs + pos2];
                 }
+                cnt = r;
+            } else {
+                if (lane == 0) atomicOr(&st->error, ERR_NBR_OVERFLOW);
+                cnt = 0;
+            }
+            __syncwarp();
+        } else if (c.weighted_sampling && c.weighted_avg && p.wcdf) {
+            // S_PROB with weighted sampling: the Binomial(deg, p) count (at
+            // least one), then that many by weight
+            const float pr = c.nodes_val;
+            uint32_t r = 0;
+            for (uint32_t b = 0; b < deg; b += 32) {
+                const uint32_t q = b + lane;
+                r += __popc(__ballot_sync(FULL, q < deg && unit_f32(rand_u32(c.seed, v, salt, ST_NSEL, q)) < pr));
+            }
+            sw = 1.f / pr;
+            if (r == 0 && deg > 0) { r = 1; sw = (1.f - powf(pr, (float)deg)) / pr; }
+            if (r == deg) {
+                take_all = 1;
+            } else if (r <= c.Kcap) {
+                if (r <= 32) ares_small(p, rs, deg, sw, r, v, salt, out, outw, lane);
+                else ares_select(p, rs, deg, sw, r, v, salt, out, outw, s_hist[(threadIdx.x >> 5) & 7], lane);
                 cnt = r;
             } else {
                 if (lane == 0) atomicOr(&st->error, ERR_NBR_OVERFLOW);

@@ -79,3 +79,13 @@ def test_neighborhood_aligner_class(oracle, tmp_path):
     na.align_to_disk(p, emb, g)
     back = cl.NodeEmbeddings.load(p)
     assert np.array_equal(back.table, out.table)
+
+
+def test_align_neighbour_cap_beyond_degree_and_zero_alpha(oracle):
+    rows, cols, cdf = _graph(21, 200, deg=(0, 4))
+    emb = np.random.default_rng(21).standard_normal((200, 32)).astype(np.float32)
+    a = _native.align(rows, cols, cdf, emb, alpha=0.0, max_neighbors=1000)     # cap above every degree
+    b = _native.align(rows, cols, cdf, emb, alpha=0.0)
+    assert np.array_equal(a, b)
+    z = np.nonzero(np.diff(rows) == 0)[0]
+    assert len(z) and not a[z].any()                 # no edges and alpha 0: zero rows

@@ -187,3 +187,21 @@ def test_nearest_neighbors_batch_matches_exact():
     assert (np.diff(dist, axis=1) >= 0).all()
     with pytest.raises(cl.UnsupportedOption):
         cl.NodeEmbeddings(e.vocab_, table, cl.Distance.Euclidean).nearest_neighbors(table[:2], 3)
+
+
+def test_knn_cosine_argument_limits():
+    rng = np.random.default_rng(5)
+    db = rng.standard_normal((300, 1)).astype(np.float32)        # one dimension: cosine is the sign
+    q = np.array([[2.0], [-3.0]], np.float32)
+    idx, sim = _native.knn_cosine(db, q, 4)
+    assert (np.sign(db[idx[0].astype(np.int64), 0]) == 1).all() and np.allclose(sim[0], 1.0)
+    assert (np.sign(db[idx[1].astype(np.int64), 0]) == -1).all() and np.allclose(sim[1], 1.0)
+    for bad in (dict(k=0), dict(k=33)):
+        with pytest.raises(_native.NativeError):
+            _native.knn_cosine(db, q, bad["k"])
+    with pytest.raises(_native.NativeError):
+        _native.knn_cosine(np.zeros((4, 257), np.float32), np.zeros((1, 257), np.float32), 2)
+    # zero rows have similarity 0 to everything and are still ranked
+    z = np.zeros((3, 8), np.float32)
+    idx, sim = _native.knn_cosine(z, rng.standard_normal((2, 8)).astype(np.float32), 3)
+    assert sorted(idx[0].tolist()) == [0, 1, 2] and np.allclose(sim, 0.0)

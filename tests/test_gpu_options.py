@@ -247,3 +247,63 @@ def test_weighted_sampling_matches_a_res_inclusion_probabilities():
     # far from uniform (K / D each): the heaviest 2.7x, the lightest rarely
     assert freq[-1] > 2 * K / D and want[-1] > 2 * K / D
     assert freq[0] < 0.25 * K / D
+
+
+@pytest.mark.parametrize("kind,val", [("fixed", 40.0), ("prob", 0.5)])
+def test_weighted_sampling_many_neighbours(kind, val):
+    # counts above 32 (Fixed 40 of 100) and Probability counts (Binomial(100,
+    # .5), then that many by weight) use the radix selection of the r largest
+    # A-Res keys; inclusion frequencies over 1024 draws match a numpy
+    # Monte-Carlo of the same rule, and Fixed draws exactly 40 distinct
+    A, D = 128, 100
+    n = A + D
+    rows = np.zeros(n + 1, np.uint64)
+    rows[1:A + 1] = np.arange(1, A + 1) * D
+    rows[A + 1:] = A * D
+    cols = np.tile(np.arange(A, A + D, dtype=np.uint32), A)
+    base = ((np.arange(D) + 1.0) ** 1.5).astype(np.float32)
+    wcdf = _native.cdf_convert(rows, np.tile(base, A).copy())
+    fptr = np.arange(n + 1, dtype=np.uint64)
+    fids = (np.arange(n) % 50).astype(np.uint32)
+    cfg = _native.default_config()
+    cfg.dims, cfg.negatives, cfg.batch_size, cfg.valid_pct = 16, 2, A, 0.0
+    cfg.max_nodes_kind = _native.SAMPLE_FIXED if kind == "fixed" else _native.SAMPLE_PROB
+    cfg.max_nodes = val
+    cfg.weighted_neighbor_sampling = cfg.weighted_neighbor_averaging = 1
+    ctx = _native.Context(cfg)
+    ctx.upload_graph(rows, cols, wcdf)
+    ctx.upload_features(fptr, fids, 50)
+    ctx.set_table(None)
+    counts = np.zeros(D)
+    sizes = []
+    anchors = np.arange(A, dtype=np.uint32)
+    p = base.astype(np.float64) / base.sum()
+    for step in range(1, 9):
+        cnt, nbr, w, _ = ctx.sample(anchors, step, D)
+        for a in range(A):
+            r = int(cnt[a])
+            got = nbr[a, :r].astype(np.int64) - A
+            assert len(set(got.tolist())) == r and (got >= 0).all() and (got < D).all()
+            counts[got] += 1
+            sizes.append(r)
+            scale = D / r if kind == "fixed" else 1 / val
+            assert np.allclose(w[a, :r], scale * p[got] * D, rtol=1e-3)
+    sizes = np.array(sizes)
+    rng = np.random.default_rng(1)
+    if kind == "fixed":
+        assert (sizes == 40).all()
+        want_sizes = np.full(20000, 40)
+    else:
+        assert abs(sizes.mean() - 50) < 1.5 and sizes.min() >= 1
+        want_sizes = rng.binomial(D, val, 20000)
+    # Monte-Carlo of the rule: per draw, the r largest U^(1/w) (w ~ p, scale-free)
+    u = rng.random((20000, D))
+    keys = np.log(u) / p
+    order = np.argsort(-keys, axis=1)
+    mask = np.arange(D)[None, :] < want_sizes[:, None]
+    want = np.zeros(D)
+    np.add.at(want, order[mask], 1)
+    want /= 20000
+    freq = counts / (8 * A)
+    assert np.abs(freq - want).max() < 0.06, np.abs(freq - want).max()
+    assert freq[-1] > freq[0] + 0.3          # heavy neighbours far more often

@@ -51,11 +51,6 @@ def test_create_rejects_bad_config(native):
     with pytest.raises(_native.NativeError) as e:
         _native.Context(cfg)
     assert e.value.code == -1
-    cfg = _native.default_config()
-    cfg.weighted_neighbor_sampling = cfg.weighted_neighbor_averaging = 1
-    cfg.max_nodes_kind, cfg.max_nodes = _native.SAMPLE_PROB, 0.5
-    with pytest.raises(_native.UnsupportedOption):
-        _native.Context(cfg)
     for loss, restart in ((_native.LOSS_PPR, 1.5), (_native.LOSS_PPR, -0.1), (9, 0.5)):
         cfg = _native.default_config()
         cfg.loss, cfg.ppr_restart_p = loss, restart
