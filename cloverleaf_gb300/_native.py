@@ -153,6 +153,8 @@ SIGNATURES = {
     "ep_destroy": (None, [_P]),
     "ep_csr_from_edges": (ctypes.c_int, [_U64, _P, _P, _P, ctypes.c_int, _P, _P, _P, _P, _P]),
     "ep_cdf_convert": (ctypes.c_int, [_U64, _P, _P]),
+    "ep_format_embeddings": (ctypes.c_int64, [_U64, _U32, _P, _P, _P, _P, _P, _U64, _P, _U64]),
+    "ep_parse_embeddings": (ctypes.c_int64, [_P, _U64, ctypes.POINTER(_U32), _P, _P]),
     "epg_sbm": (ctypes.c_int, [_U64, _U32, ctypes.c_double, ctypes.c_double, _U64, _P, _P, _P, _P, _P]),
     "epg_sbm_tokens": (ctypes.c_int, [_U64, _P, _U32, _U32, _U32, _U32, ctypes.c_double, _U32, _U64, _P, _P,
                                       _P, _P, _P]),
@@ -347,6 +349,79 @@ def cdf_convert(rows, w):
     w = np.ascontiguousarray(w, np.float32).copy()
     check(lib().ep_cdf_convert(len(rows) - 1, ptr(rows), ptr(w)), None, "ep_cdf_convert")
     return w
+
+
+def _strings(strs):
+    """A list of str as (utf-8 bytes as uint8, n+1 uint64 offsets)."""
+    enc = [x.encode() for x in strs]
+    off = np.zeros(len(enc) + 1, np.uint64)
+    np.cumsum([len(x) for x in enc], out=off[1:])
+    return np.frombuffer(b"".join(enc), np.uint8) if off[-1] else np.zeros(1, np.uint8), off
+
+
+def format_embeddings(table, types, names=None, first_id=0) -> bytes:
+    """EmbeddingWriter::stream (io.rs:44-76) for the rows of table: types is
+    one str for every row or a list of str; names a list of str, or None for
+    the decimal ids first_id, first_id + 1, ...  (``ep_format_embeddings``)."""
+    table = np.ascontiguousarray(table, np.float32)
+    n, dims = table.shape
+    if isinstance(types, str):
+        tbuf, toff = np.frombuffer(types.encode() + b"\0", np.uint8), None
+    else:
+        if len(types) != n:
+            raise ValueError(f"{len(types)} types for {n} rows")
+        tbuf, toff = _strings(types)
+    nbuf = noff = None
+    if names is not None:
+        if len(names) != n:
+            raise ValueError(f"{len(names)} names for {n} rows")
+        nbuf, noff = _strings(names)
+    cap = n * (16 * dims + 25) + (int(toff[-1]) if toff is not None else n * len(tbuf))
+    cap += int(noff[-1]) if noff is not None else 0
+    out = np.empty(max(cap, 1), np.uint8)
+    rc = lib().ep_format_embeddings(n, dims, ptr(table), ptr(tbuf), ptr(toff), ptr(nbuf), ptr(noff), int(first_id),
+                                    ptr(out), cap)
+    if rc < 0:
+        check(int(rc), None, "ep_format_embeddings")
+    return out[:rc].tobytes()
+
+
+def parse_embeddings(buf: bytes, dims=None):
+    """line_to_embedding (io.rs:246-262) over a block of whole lines:
+    (values [rows, dims] f32, token offsets [rows, 4] u64 as type begin/end,
+    name begin/end).  dims, when given, is the width every row must have.
+    Raises ValueError naming the first bad line.  (``ep_parse_embeddings``)"""
+    arr = np.frombuffer(buf, np.uint8)
+    d = _U32(0)
+    rows = int(lib().ep_parse_embeddings(ptr(arr), len(arr), ctypes.byref(d), None, None))
+    if rows < 0:
+        check(rows, None, "ep_parse_embeddings")
+    if rows and d.value == 0:
+        raise ValueError(f"Error parsing line: {_line(buf, 1)[:200]!r}")
+    if dims is not None:
+        d = _U32(int(dims))
+    vals = np.empty((max(rows, 1), d.value), np.float32)
+    tok = np.empty((max(rows, 1), 4), np.uint64)
+    got = lib().ep_parse_embeddings(ptr(arr), len(arr), ctypes.byref(d), ptr(vals), ptr(tok))
+    if got < 0:
+        line = _line(buf, -got)
+        alone = _U32(0)
+        one = np.frombuffer(line, np.uint8)
+        if lib().ep_parse_embeddings(ptr(one), len(one), ctypes.byref(alone), None, None) == 1 and alone.value:
+            raise ValueError(f"Embeddings have different sizes! ({alone.value} values, expected {d.value}, "
+                             f"line: {line[:200]!r})")
+        raise ValueError(f"Error parsing line: {line[:200]!r}")
+    return vals[:got], tok[:got]
+
+
+def _line(buf: bytes, k: int) -> bytes:
+    """The k-th (1-based) non-blank line of buf."""
+    for line in buf.split(b"\n"):
+        if line and line != b"\r":
+            k -= 1
+            if k == 0:
+                return line.rstrip(b"\r")
+    return b""
 
 
 def _knn_check(rc, what):

@@ -7,12 +7,15 @@
 // blocking does not depend on the thread count.
 #include <algorithm>
 #include <atomic>
+#include <charconv>
+#include <cctype>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <memory>
 #include <mutex>
 #include <numeric>
+#include <string>
 #include <unordered_map>
 #include <vector>
 #ifdef _OPENMP
@@ -489,4 +492,138 @@ extern "C" int epg_zipf_features(uint64_t n, double lambda, uint32_t cmin, uint3
             for (uint64_t j = fptr[v]; j < fptr[v + 1]; ++j) fids[j] = al.draw(r);
     }
     return EP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// NodeEmbeddings text format (EmbeddingWriter::stream, src/io.rs:44-76, and
+// line_to_embedding, src/io.rs:246-262): one line per node,
+// "<type>\t<name>\t[v0,v1,...]".  Values are written as the shortest decimal
+// that reads back to the same f32 (std::to_chars), and read with
+// std::from_chars; rows are formatted and parsed in parallel.
+// ---------------------------------------------------------------------------
+extern "C" int64_t ep_format_embeddings(uint64_t n, uint32_t dims, const float* table, const char* types,
+                                        const uint64_t* type_off, const char* names, const uint64_t* name_off,
+                                        uint64_t first_id, char* out, uint64_t out_cap) {
+    if (dims == 0 || (n && (!table || !types || !out)) || (names && !name_off)) return EP_ERR_INVALID_ARG;
+    const uint64_t one_type_len = type_off ? 0 : strlen(types);
+    constexpr uint32_t MAXV = 16;   // longest shortest-form f32, "-1.17549435e-38", and a comma
+    // each thread formats one contiguous range of rows into its own buffer;
+    // the buffers are then placed back to back
+    const int nt = (int)std::min<uint64_t>((uint64_t)omp_get_max_threads(), std::max<uint64_t>(1, n / 64));
+    std::vector<std::string> part(nt);
+    std::vector<uint64_t> part_off(nt + 1, 0);
+#pragma omp parallel num_threads(nt)
+    {
+        const int t = omp_get_thread_num();
+        const uint64_t lo = n * t / nt, hi = n * (t + 1) / nt;
+        std::string& o = part[t];
+        char num[32];
+        for (uint64_t i = lo; i < hi; ++i) {
+            if (type_off) o.append(types + type_off[i], type_off[i + 1] - type_off[i]);
+            else o.append(types, one_type_len);
+            o.push_back('\t');
+            if (names) {
+                o.append(names + name_off[i], name_off[i + 1] - name_off[i]);
+            } else {
+                char* z = std::to_chars(num, num + sizeof num, first_id + i).ptr;
+                o.append(num, z - num);
+            }
+            o.append("\t[", 2);
+            const size_t at = o.size();
+            o.resize(at + (size_t)dims * MAXV);
+            char* p = &o[at];
+            const float* row = table + i * dims;
+            for (uint32_t k = 0; k < dims; ++k) {
+                if (k) *p++ = ',';
+                p = std::to_chars(p, p + MAXV, row[k]).ptr;
+            }
+            o.resize((size_t)(p - o.data()));
+            o.append("]\n", 2);
+        }
+    }
+    for (int t = 0; t < nt; ++t) part_off[t + 1] = part_off[t] + part[t].size();
+    if (part_off[nt] > out_cap) return EP_ERR_INVALID_ARG;
+#pragma omp parallel for num_threads(nt)
+    for (int t = 0; t < nt; ++t) memcpy(out + part_off[t], part[t].data(), part[t].size());
+    return (int64_t)part_off[nt];
+}
+
+extern "C" int64_t ep_parse_embeddings(const char* buf, uint64_t len, uint32_t* dims, float* values,
+                                       uint64_t* tok_off) {
+    if ((len && !buf) || !dims) return EP_ERR_INVALID_ARG;
+    // line starts; blank lines are skipped
+    std::vector<uint64_t> start;
+    for (uint64_t i = 0; i < len;) {
+        const void* nl = memchr(buf + i, '\n', len - i);
+        const uint64_t e = nl ? (uint64_t)((const char*)nl - buf) : len;
+        if (e > i && !(e == i + 1 && buf[i] == '\r')) start.push_back(i);
+        i = e + 1;
+    }
+    const int64_t rows = (int64_t)start.size();
+    // line_to_embedding (src/io.rs:246-262): exactly three tab-separated
+    // fields; the third loses its first and last byte (the brackets) and is
+    // split on ',', each piece trimmed and read as an f32.  Values past cap
+    // are counted but not stored.
+    auto parse_row = [&](int64_t r, float* dst, uint32_t cap, uint64_t* tok, uint32_t* count) -> bool {
+        const uint64_t b = start[r];
+        const void* nl = memchr(buf + b, '\n', len - b);
+        uint64_t e = nl ? (uint64_t)((const char*)nl - buf) : len;
+        if (e > b && buf[e - 1] == '\r') --e;
+        const char* t1 = (const char*)memchr(buf + b, '\t', e - b);
+        if (!t1) return false;
+        const uint64_t f1 = (uint64_t)(t1 - buf);
+        const char* t2 = (const char*)memchr(buf + f1 + 1, '\t', e - f1 - 1);
+        if (!t2) return false;
+        const uint64_t f2 = (uint64_t)(t2 - buf);
+        if (memchr(buf + f2 + 1, '\t', e - f2 - 1)) return false;
+        if (tok) { tok[0] = b; tok[1] = f1; tok[2] = f1 + 1; tok[3] = f2; }
+        if (e - f2 - 1 < 2) return false;
+        uint64_t p = f2 + 2;
+        const uint64_t end = e - 1;
+        uint32_t k = 0;
+        for (;;) {
+            const void* c = memchr(buf + p, ',', end - p);
+            const uint64_t q = c ? (uint64_t)((const char*)c - buf) : end;
+            uint64_t a = p, z = q;
+            while (a < z && isspace((unsigned char)buf[a])) ++a;
+            while (z > a && isspace((unsigned char)buf[z - 1])) --z;
+            const char* s0 = buf + a;
+            if (a + 1 < z && *s0 == '+' && s0[1] != '-') ++s0;     // a leading '+' is allowed
+            float v = 0.f;
+            auto res = std::from_chars(s0, buf + z, v);
+            if (res.ec == std::errc::result_out_of_range) {
+                // beyond f32's range: round through f64 (overflow to inf,
+                // underflow to zero), as a saturating float parser does
+                double dv = 0.0;
+                res = std::from_chars(s0, buf + z, dv);
+                v = (float)dv;
+            }
+            // from_chars also takes the inf / infinity / nan spellings, in any case
+            if (a == z || res.ec != std::errc() || res.ptr != buf + z) return false;
+            if (dst && k < cap) dst[k] = v;
+            ++k;
+            if (q >= end) break;
+            p = q + 1;
+        }
+        *count = k;
+        return true;
+    };
+    if (!values) {      // counting call: rows, and the width of the first row (0: malformed)
+        uint32_t k = 0;
+        *dims = rows && parse_row(0, nullptr, 0, nullptr, &k) ? k : 0;
+        return rows;
+    }
+    const uint32_t d = *dims;
+    std::atomic<int64_t> first_bad{INT64_MAX};
+#pragma omp parallel for schedule(dynamic, 512)
+    for (int64_t r = 0; r < rows; ++r) {
+        uint32_t k = 0;
+        const bool ok = parse_row(r, values + (uint64_t)r * d, d, tok_off ? tok_off + 4 * (uint64_t)r : nullptr, &k);
+        if (!ok || k != d) {
+            int64_t cur = first_bad.load();
+            while (r < cur && !first_bad.compare_exchange_weak(cur, r)) {}
+        }
+    }
+    if (first_bad.load() != INT64_MAX) return -(first_bad.load() + 1);
+    return rows;
 }

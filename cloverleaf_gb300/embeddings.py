@@ -173,42 +173,141 @@ class NodeEmbeddings:
         return ids, (np.float32(1) - sim).astype(np.float32)
 
     def save(self, path: str, comp_level: Optional[int] = None) -> None:
-        """``node_type\\tname\\t[v1,v2,...]`` lines (io.rs:44-76)."""
-        import gzip
+        """``node_type\\tname\\t[v1,v2,...]`` lines (EmbeddingWriter,
+        io.rs:44-76), gzipped when the path ends with ``.gz`` (level
+        comp_level, default 1, io.rs:215-227).  Rows are formatted natively
+        in blocks (``ep_format_embeddings``), each value the shortest decimal
+        that reads back to the same f32."""
+        from .graph import RangeVocab
 
-        opener = gzip.open if path.endswith(".gz") or comp_level is not None else open
-        with opener(path, "wt") as f:
-            for i in range(self.len()):
-                nt, nn = self.vocab_.get_name(i)
-                vals = ",".join(repr(float(x)) for x in self.table[i])
-                f.write(f"{nt}\t{nn}\t[{vals}]\n")
+        v, n = self.vocab_, self.len()
+        if path.endswith(".gz"):
+            import gzip
+            f = gzip.open(path, "wb", compresslevel=1 if comp_level is None else int(comp_level))
+        else:
+            f = open(path, "wb")
+        step = max(1, (1 << 26) // (16 * max(self.table.shape[1], 1) + 32))
+        with f:
+            for lo in range(0, n, step):
+                hi = min(n, lo + step)
+                if isinstance(v, RangeVocab) and hi <= v._n:     # names are the decimal ids
+                    f.write(_native.format_embeddings(self.table[lo:hi], v._type, None, lo))
+                else:
+                    names = [v.get_name(i) for i in range(lo, hi)]
+                    f.write(_native.format_embeddings(self.table[lo:hi], [t for t, _ in names],
+                                                      [x for _, x in names]))
 
     @staticmethod
     def load(path: str, distance: Optional[Distance] = None, filter_type=None, chunk_size=None,
              skip_rows=None) -> "NodeEmbeddings":
-        """Reads the format written by save (io.rs:134-198)."""
-        import gzip
+        """Reads the format written by save (EmbeddingReader::load,
+        io.rs:134-198): skip_rows leading lines are skipped, filter_type keeps
+        the rows of those node types, a node seen twice raises KeyError, rows
+        of different widths raise ValueError.  Blocks of lines are parsed
+        natively (``ep_parse_embeddings``).  A file whose names are the
+        decimal ids 0..n-1 of one node type gets a RangeVocab.  chunk_size is
+        accepted for API parity."""
+        from .graph import RangeVocab
 
         types = None if filter_type is None else ({filter_type} if isinstance(filter_type, str) else set(filter_type))
+        tables, blocks, dims = [], [], None
+        for buf in _line_blocks(path, skip_rows or 0):
+            vals, tok = _native.parse_embeddings(buf, dims)
+            if not len(vals):
+                continue
+            dims = vals.shape[1]
+            raw = np.frombuffer(buf, np.uint8)
+            one = _one_type(raw, tok)
+            if one is not None:
+                if types is not None and one not in types:
+                    continue
+                first = _decimal_run(raw, tok)
+                if first is not None:
+                    tables.append(vals)
+                    blocks.append((one, first, len(vals)))
+                    continue
+            names = [(buf[a:b].decode(), buf[c:d].decode()) for a, b, c, d in tok.tolist()]
+            if types is not None:
+                keep = np.array([t in types for t, _ in names], bool)
+                vals = vals[keep]
+                names = [x for x, k in zip(names, keep) if k]
+            tables.append(vals)
+            blocks.append(names)
+        t = np.concatenate(tables) if tables else np.zeros((0, dims or 0), np.float32)
+        total = len(t)
+        # one node type whose names run 0, 1, ..., total - 1 in order: a RangeVocab
+        if blocks and all(isinstance(b, tuple) for b in blocks) and len({b[0] for b in blocks}) == 1:
+            expect = 0
+            for _, first, cnt in blocks:
+                if first != expect:
+                    break
+                expect += cnt
+            else:
+                return NodeEmbeddings(RangeVocab(total, blocks[0][0]), t, distance or Distance.Cosine)
         v = Vocab()
-        rows = []
-        opener = gzip.open if path.endswith(".gz") else open
-        with opener(path, "rt") as f:
-            for i, line in enumerate(f):
-                if skip_rows and i < skip_rows:
-                    continue
-                p = line.rstrip("\n").split("\t")
-                if len(p) != 3:
-                    raise ValueError(f"Line {i + 1}: expected node_type<TAB>name<TAB>[embedding]")
-                if types is not None and p[0] not in types:
-                    continue
-                v.get_or_insert(p[0], p[1])
-                rows.append(np.array([float(x) for x in p[2].strip("[]").split(",") if x], np.float32))
-        d = max((len(r) for r in rows), default=0)
-        t = np.zeros((len(rows), d), np.float32)
-        for i, r in enumerate(rows):
-            t[i, : len(r)] = r
+        i = 0
+        for b in blocks:
+            seq = ((b[0], str(x)) for x in range(b[1], b[1] + b[2])) if isinstance(b, tuple) else b
+            for nt, nn in seq:
+                if v.get_or_insert(nt, nn) < i:
+                    raise KeyError(f"found duplicate node at {i}!")
+                i += 1
         return NodeEmbeddings(v, t, distance or Distance.Cosine)
+
+
+def _line_blocks(path: str, skip_rows: int, block: int = 1 << 24):
+    """Blocks of whole lines of a (possibly gzipped) text file, after
+    skip_rows leading lines."""
+    import gzip
+
+    with (gzip.open(path, "rb") if path.endswith(".gz") else open(path, "rb")) as f:
+        for _ in range(skip_rows):
+            if not f.readline():
+                return
+        rest = b""
+        while True:
+            chunk = f.read(block)
+            if not chunk:
+                break
+            data = rest + chunk if rest else chunk
+            cut = data.rfind(b"\n")
+            if cut < 0:
+                rest = data
+                continue
+            yield data[: cut + 1]
+            rest = data[cut + 1:]
+        if rest:
+            yield rest
+
+
+def _one_type(raw: np.ndarray, tok: np.ndarray) -> Optional[str]:
+    """The node type when every row of the block has the same one."""
+    tl = (tok[:, 1] - tok[:, 0]).astype(np.int64)
+    if (tl != tl[0]).any():
+        return None
+    first = raw[int(tok[0, 0]): int(tok[0, 1])]
+    if tl[0] and (raw[tok[:, :1].astype(np.int64) + np.arange(tl[0])] != first).any():
+        return None
+    return first.tobytes().decode()
+
+
+def _decimal_run(raw: np.ndarray, tok: np.ndarray) -> Optional[int]:
+    """f when the names of the block are the decimals f, f + 1, ... (no
+    leading zeros), else None."""
+    beg = tok[:, 2].astype(np.int64)
+    ln = (tok[:, 3] - tok[:, 2]).astype(np.int64)
+    if not 1 <= ln.min() <= ln.max() <= 18:
+        return None
+    cols = np.arange(int(ln.max()))
+    m = cols < ln[:, None]
+    dig = raw[np.minimum(beg[:, None] + cols, len(raw) - 1)].astype(np.int64) - 48
+    if ((dig < 0) | (dig > 9))[m].any() or ((dig[:, 0] == 0) & (ln > 1)).any():
+        return None
+    val = np.zeros(len(beg), np.int64)
+    for j in range(len(cols)):
+        val = np.where(m[:, j], val * 10 + dig[:, j], val)
+    f = int(val[0])
+    return f if (val == f + np.arange(len(val))).all() else None
 
 
 class FeatureAggregator:

@@ -317,6 +317,32 @@ int ep_csr_from_edges(uint64_t n_edges, const uint32_t* from, const uint32_t* to
 /* CumCSR::convert (src/graph.rs:414-422, 664-691), in place. */
 int ep_cdf_convert(uint64_t n_nodes, const uint64_t* rows, float* w);
 
+/* ---- NodeEmbeddings text format (src/io.rs) -------------------------- */
+
+/* EmbeddingWriter::stream (src/io.rs:44-76): rows i < n as lines
+ * "<type>\t<name>\t[v0,...,v_{dims-1}]\n", each value the shortest decimal
+ * that reads back to the same f32.  Types: with type_off, a byte buffer and
+ * n+1 offsets; with type_off NULL, one NUL-terminated type for every row.
+ * Names: with names, a byte buffer and n+1 offsets; with names NULL, the
+ * decimal first_id + i.  Writes into out, which must hold the strings plus
+ * n * (16 * dims + 25) bytes.  Returns the bytes written, or a negative
+ * status. */
+int64_t ep_format_embeddings(uint64_t n, uint32_t dims, const float* table, const char* types,
+                             const uint64_t* type_off, const char* names, const uint64_t* name_off,
+                             uint64_t first_id, char* out, uint64_t out_cap);
+
+/* EmbeddingReader::load's line parser (src/io.rs:134-262) over a buffer of
+ * whole lines "<type>\t<name>\t[v,...]" (blank lines skipped; values may be
+ * padded with spaces and spell inf and NaN).  Counting call (values NULL):
+ * returns the row count and sets *dims to the first row's width (0 when the
+ * first row is malformed: a row holds at least one value).  Filling
+ * call: *dims is the expected width; fills values (rows x dims) and, when
+ * tok_off is given, 4 byte offsets per row (type begin/end, name begin/end),
+ * and returns the row count.  A malformed line, or one of another width,
+ * makes the filling call return -(its 1-based number among the non-blank
+ * lines). */
+int64_t ep_parse_embeddings(const char* buf, uint64_t len, uint32_t* dims, float* values, uint64_t* tok_off);
+
 #ifdef __cplusplus
 }
 #endif
