@@ -8,11 +8,11 @@ from ._native import NativeError, UnsupportedOption
 from .alignment import NeighborhoodAligner
 from .embeddings import Distance, FeatureAggregator, NodeEmbedder, NodeEmbeddings
 from .ep import EmbeddingPropagator, EPLoss, LossWeighting
-from .features import FeatureNamespace, FeatureSet
+from .features import FeatureNamespace, FeaturePropagator, FeatureSet
 from .graph import EdgeType, Graph, GraphBuilder, Vocab
 
 __all__ = [
-    "Distance", "EdgeType", "EmbeddingPropagator", "EPLoss", "FeatureAggregator", "FeatureNamespace", "FeatureSet",
+    "Distance", "EdgeType", "EmbeddingPropagator", "EPLoss", "FeatureAggregator", "FeatureNamespace", "FeaturePropagator", "FeatureSet",
     "Graph", "GraphBuilder", "LossWeighting", "NativeError", "NeighborhoodAligner", "NodeEmbedder", "NodeEmbeddings",
     "UnsupportedOption",
     "Vocab", "build",

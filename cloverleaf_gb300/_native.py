@@ -155,6 +155,7 @@ SIGNATURES = {
     "ep_cdf_convert": (ctypes.c_int, [_U64, _P, _P]),
     "ep_format_embeddings": (ctypes.c_int64, [_U64, _U32, _P, _P, _P, _P, _P, _U64, _P, _U64]),
     "ep_parse_embeddings": (ctypes.c_int64, [_P, _U64, ctypes.POINTER(_U32), _P, _P]),
+    "ep_propagate_features": (ctypes.c_int64, [_U64, _P, _P, _P, _P, _P, _U32, _U32, _F32, _P, _P, _U64]),
     "epg_sbm": (ctypes.c_int, [_U64, _U32, ctypes.c_double, ctypes.c_double, _U64, _P, _P, _P, _P, _P]),
     "epg_sbm_tokens": (ctypes.c_int, [_U64, _P, _U32, _U32, _U32, _U32, ctypes.c_double, _U32, _U64, _P, _P,
                                       _P, _P, _P]),
@@ -412,6 +413,28 @@ def parse_embeddings(buf: bytes, dims=None):
                              f"line: {line[:200]!r})")
         raise ValueError(f"Error parsing line: {line[:200]!r}")
     return vals[:got], tok[:got]
+
+
+def propagate_features(rows, cols, cdf, fptr, fids, max_iters: int, k: int, threshold: float):
+    """propagate_features (feat_propagation.rs:13-93) through
+    ``ep_propagate_features``: the new (fptr, fids)."""
+    rows = np.ascontiguousarray(rows, np.uint64)
+    cols = np.ascontiguousarray(cols, np.uint32)
+    cdf = np.ascontiguousarray(cdf, np.float32)
+    fptr = np.ascontiguousarray(fptr, np.uint64)
+    fids = np.ascontiguousarray(fids, np.uint32)
+    n = len(fptr) - 1
+    if len(rows) != n + 1:
+        raise ValueError(f"graph has {len(rows) - 1} nodes, feature set {n}")
+    missing = int((np.diff(fptr) == 0).sum())
+    cap = int(fptr[-1]) + missing * int(k)
+    fptr_out = np.zeros(n + 1, np.uint64)
+    fids_out = np.zeros(max(cap, 1), np.uint32)
+    rc = lib().ep_propagate_features(n, ptr(rows), ptr(cols), ptr(cdf), ptr(fptr), ptr(fids), int(max_iters), int(k),
+                                     float(threshold), ptr(fptr_out), ptr(fids_out), cap)
+    if rc < 0:
+        check(int(rc), None, "ep_propagate_features")
+    return fptr_out, fids_out[:rc]
 
 
 def _line(buf: bytes, k: int) -> bytes:

@@ -627,3 +627,92 @@ extern "C" int64_t ep_parse_embeddings(const char* buf, uint64_t len, uint32_t* 
     if (first_bad.load() != INT64_MAX) return -(first_bad.load() + 1);
     return rows;
 }
+
+// ---------------------------------------------------------------------------
+// propagate_features (src/algos/feat_propagation.rs:13-93).  Nodes without
+// features take the k heaviest features of their neighbours, each feature
+// weighted by the sum of the edge probabilities (differences of the row's
+// CDF) of the neighbours carrying it; features with weight / L2 norm <=
+// threshold are dropped.  Sweeps run over the nodes in order and update in
+// place, so a node sees the features its predecessors received in the same
+// sweep.  A node is final once every neighbour had features when it was
+// visited; sweeps stop when all are final or after max_iters.  Equal weights
+// are ordered by feature id (the reference leaves them in hash-map order).
+// ---------------------------------------------------------------------------
+extern "C" int64_t ep_propagate_features(uint64_t n, const uint64_t* rows, const uint32_t* cols, const float* cdf,
+                                         const uint64_t* fptr, const uint32_t* fids, uint32_t max_iters, uint32_t k,
+                                         float threshold, uint64_t* fptr_out, uint32_t* fids_out, uint64_t out_cap) {
+    if (n && (!rows || !cols || !cdf || !fptr || !fptr_out)) return EP_ERR_INVALID_ARG;
+    uint32_t n_feat = 0;
+    for (uint64_t i = 0; i < (n ? fptr[n] : 0); ++i) n_feat = std::max(n_feat, fids[i] + 1);
+    std::vector<std::vector<uint32_t>> own(n);      // lists of nodes that started without features
+    std::vector<uint8_t> done(n, 0);
+    uint64_t missing = 0;
+    for (uint64_t v = 0; v < n; ++v) {
+        if (fptr[v + 1] < fptr[v]) return EP_ERR_INVALID_ARG;
+        done[v] = fptr[v + 1] > fptr[v];
+        missing += !done[v];
+    }
+    for (uint64_t e = 0; e < (n ? rows[n] : 0); ++e)
+        if (cols[e] >= n) return EP_ERR_INVALID_ARG;
+    const std::vector<uint8_t> had(done);
+    auto feats = [&](uint64_t u, const uint32_t*& b, size_t& len) {
+        if (had[u]) { b = fids + fptr[u]; len = (size_t)(fptr[u + 1] - fptr[u]); }
+        else { b = own[u].data(); len = own[u].size(); }
+    };
+    std::vector<float> wsum(n_feat, 0.f);
+    std::vector<uint8_t> seen(n_feat, 0);
+    std::vector<uint32_t> touched;
+    std::vector<std::pair<float, uint32_t>> order;
+    for (uint32_t it = 0; it < max_iters && missing; ++it) {
+        bool all_final = true;
+        for (uint64_t v = 0; v < n; ++v) {
+            if (done[v]) continue;
+            bool nbrs_final = true;
+            float prev = 0.f;
+            for (uint64_t e = rows[v]; e < rows[v + 1]; ++e) {
+                const float px = cdf[e] - prev;
+                prev = cdf[e];
+                const uint32_t* b;
+                size_t len;
+                feats(cols[e], b, len);
+                nbrs_final = nbrs_final && len > 0;
+                for (size_t j = 0; j < len; ++j) {
+                    const uint32_t f = b[j];
+                    if (!seen[f]) { seen[f] = 1; wsum[f] = 0.f; touched.push_back(f); }
+                    wsum[f] += px;
+                }
+            }
+            order.clear();
+            for (uint32_t f : touched) { order.emplace_back(wsum[f], f); seen[f] = 0; }
+            touched.clear();
+            std::sort(order.begin(), order.end(), [](const std::pair<float, uint32_t>& a, const std::pair<float, uint32_t>& b) {
+                return a.first > b.first || (a.first == b.first && a.second < b.second);
+            });
+            float sq = 0.f;
+            for (const auto& x : order) sq += x.first * x.first;
+            const float norm = std::sqrt(sq);
+            std::vector<uint32_t>& out = own[v];
+            out.clear();
+            for (const auto& x : order) {
+                if (out.size() >= k) break;
+                if (x.first / norm > threshold) out.push_back(x.second);
+            }
+            if (nbrs_final) { done[v] = 1; --missing; }
+            else all_final = false;
+        }
+        if (all_final) break;
+    }
+    uint64_t o = 0;
+    fptr_out[0] = 0;
+    for (uint64_t v = 0; v < n; ++v) {
+        const uint32_t* b;
+        size_t len;
+        feats(v, b, len);
+        if (o + len > out_cap) return EP_ERR_INVALID_ARG;
+        if (len) memcpy(fids_out + o, b, len * sizeof(uint32_t));
+        o += len;
+        fptr_out[v + 1] = o;
+    }
+    return (int64_t)o;
+}

@@ -311,11 +311,16 @@ def _decimal_run(raw: np.ndarray, tok: np.ndarray) -> Optional[int]:
 
 
 class FeatureAggregator:
-    """How node embeddings are formed from feature embeddings."""
+    """How node embeddings are formed from feature embeddings
+    (lib.rs:1772-2000): Averaged, Weighted (SIF) or Attention.  Attention
+    aggregation is a separate model outside the EP training path: it can be
+    built, printed, saved and loaded, but embedding with it raises
+    UnsupportedOption."""
 
     def __init__(self, kind: str, alpha: float = 0.0, unigrams: Optional[np.ndarray] = None,
-                 vocab: Optional[Vocab] = None):
+                 vocab: Optional[Vocab] = None, heads: int = 0, d_k: int = 0, window: Optional[int] = None):
         self.kind, self.alpha, self.unigrams, self.vocab = kind, alpha, unigrams, vocab
+        self.heads, self.d_k, self.window = heads, d_k, window
 
     @staticmethod
     def Averaged() -> "FeatureAggregator":
@@ -328,8 +333,78 @@ class FeatureAggregator:
         p = (counts / max(counts.sum(), 1.0)).astype(np.float32)
         return FeatureAggregator("weighted", float(alpha), p, feature_set.feature_vocab)
 
+    @staticmethod
+    def Attention(num_heads: int, d_k: int, window: Optional[int] = None) -> "FeatureAggregator":
+        return FeatureAggregator("attention", heads=int(num_heads), d_k=int(d_k), window=window)
+
     def __repr__(self) -> str:
-        return f"FeatureAggregator<{self.kind}>"
+        if self.kind == "weighted":
+            t = f"Weighted<alpha={_rust_float(self.alpha, np.float32)}>"
+        elif self.kind == "attention":
+            w = "None" if self.window is None else f"Some({self.window})"
+            t = f"Attention<num_heads={self.heads},d_k={self.d_k},window={w}"
+        else:
+            t = "Averaged"
+        return f"FeatureAggregator<{t}>"
+
+    def save(self, path: str) -> None:
+        """The aggregator's text form (lib.rs:1876-1913): its kind, then
+        alpha and one ``type\\tname\\tp`` line per feature (Weighted), or
+        the head count, d_k and window (0 = none) (Attention)."""
+        with open(path, "w") as f:
+            if self.kind == "averaged":
+                f.write("Averaged\n")
+            elif self.kind == "attention":
+                f.write(f"Attention\n{self.heads}\n{self.d_k}\n{self.window or 0}\n")
+            else:
+                f.write(f"Weighted\n{_rust_float(self.alpha, np.float32)}\n")
+                for i, p in enumerate(np.asarray(self.unigrams, np.float32).tolist()):
+                    if i >= len(self.vocab):
+                        break
+                    nt, nn = self.vocab.get_name(i)
+                    f.write(f"{nt}\t{nn}\t{_rust_float(p, np.float64)}\n")
+
+    @staticmethod
+    def load(path: str) -> "FeatureAggregator":
+        """Reads the form written by save (lib.rs:1928-2000)."""
+        with open(path) as f:
+            kind = f.readline().rstrip("\r\n")
+            if kind == "Averaged":
+                return FeatureAggregator.Averaged()
+            if kind == "Attention":
+                vals = []
+                for _ in range(3):
+                    line = f.readline().rstrip("\r\n")
+                    if not line.isdigit():
+                        raise ValueError(f"invalid dim! {line!r}")
+                    vals.append(int(line))
+                return FeatureAggregator.Attention(vals[0], vals[1], vals[2] or None)
+            if kind != "Weighted":
+                raise ValueError(f"Unknown aggregator type: {kind}")
+            line = f.readline().rstrip("\r\n")
+            try:
+                alpha = float(np.float32(float(line)))
+            except ValueError:
+                raise ValueError(f"invalid dim! {line!r}") from None
+            v, p = Vocab(), []
+            for line in f:
+                pieces = line.rstrip("\n").split("\t")
+                if len(pieces) != 3:
+                    raise ValueError("Malformed feature line! Need node_type<TAB>name<TAB>weight ...")
+                try:
+                    pw = float(pieces[2])
+                except ValueError:
+                    raise ValueError(f"Tried to parse weight and failed:{line!r}") from None
+                if v.get_or_insert(pieces[0], pieces[1]) < len(p):
+                    raise ValueError(f"Duplicate feature found:{pieces[0]} {pieces[1]}")
+                p.append(pw)
+            return FeatureAggregator("weighted", alpha, np.array(p, np.float32), v)
+
+
+def _rust_float(x: float, ty) -> str:
+    """x as Rust's Display writes an f32 / f64: shortest round-trip digits of
+    that type, positional."""
+    return np.format_float_positional(ty(x), unique=True, trim="-")
 
 
 class NodeEmbedder:
@@ -359,6 +434,8 @@ class NodeEmbedder:
         GPU (``ep_embed_features``); nodes without known features stay zero
         (lib.rs:2092-2124).  As the reference, the SIF weight of a feature is
         looked up by its row in feature_embeddings (aggregator.rs:103-110)."""
+        if self.feat_agg.kind == "attention":
+            raise _native.UnsupportedOption(-6, "attention aggregation is not implemented")
         fptr, ids = self._translate(feat_set, feature_embeddings)
         T = feature_embeddings.table
         n = len(fptr) - 1

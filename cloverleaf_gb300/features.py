@@ -55,6 +55,23 @@ class FeatureSet:
     def new_from_graph(graph: Graph) -> "FeatureSet":
         return FeatureSet(graph.vocab_, graph.nodes())
 
+    @staticmethod
+    def new_from_file(path: str, namespace: Optional[FeatureNamespace] = None) -> "FeatureSet":
+        """A FeatureSet over the nodes named in a features file, in file
+        order (lib.rs:1440-1517), loaded with load_into."""
+        import gzip
+
+        v = Vocab()
+        with (gzip.open(path, "rt") if path.endswith(".gz") else open(path)) as f:
+            for line in f:
+                pieces = line.rstrip("\n").split("\t")
+                if len(pieces) != 3:
+                    raise ValueError("Malformed feature line! Need node_type<TAB>name<TAB>f1 f2 ...")
+                v.get_or_insert(pieces[0], pieces[1])
+        fs = FeatureSet(v, len(v))
+        fs.load_into(path, namespace)
+        return fs
+
     @classmethod
     def from_csr(cls, graph: Graph, fptr, fids, n_feat: int, feature_vocab: Optional[Vocab] = None) -> "FeatureSet":
         """Builds a FeatureSet from CSR arrays (an extension for large
@@ -162,3 +179,34 @@ class FeatureSet:
 
     def __repr__(self) -> str:
         return f"FeatureSet<Nodes={self.nodes()},UniqueFeatures={self.num_features()}>"
+
+
+class FeaturePropagator:
+    """Fills featureless nodes from their neighbours' features
+    (lib.rs:1695-1770; feat_propagation.rs:13-93), natively
+    (``ep_propagate_features``)."""
+
+    def __init__(self, k: int, threshold: Optional[float] = None, max_iters: Optional[int] = None):
+        if k < 0 or (max_iters is not None and max_iters < 0):
+            raise OverflowError("can't convert negative int to unsigned")
+        self.k = int(k)
+        self.threshold = 0.0 if threshold is None else float(threshold)
+        self.max_iters = 20 if max_iters is None else int(max_iters)
+
+    def __repr__(self) -> str:
+        return f"FeaturePropagator<k={self.k},threshold={_rust_f32(self.threshold)},max_iters={self.max_iters}>"
+
+    def propagate(self, graph: Graph, features: "FeatureSet") -> None:
+        from . import _native
+
+        fptr, fids = features.to_csr()
+        fptr2, fids2 = _native.propagate_features(graph.rows, graph.cols, graph.weights, fptr, fids, self.max_iters,
+                                                  self.k, self.threshold)
+        features._feats = None
+        features._csr = (fptr2, fids2)
+
+
+def _rust_f32(x: float) -> str:
+    """An f32 as Rust's Display writes it: the shortest round-trip digits,
+    positional."""
+    return np.format_float_positional(np.float32(x), unique=True, trim="-")

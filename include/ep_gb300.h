@@ -343,6 +343,17 @@ int64_t ep_format_embeddings(uint64_t n, uint32_t dims, const float* table, cons
  * lines). */
 int64_t ep_parse_embeddings(const char* buf, uint64_t len, uint32_t* dims, float* values, uint64_t* tok_off);
 
+/* FeaturePropagator::propagate (src/lib.rs:1695-1770, propagate_features in
+ * src/algos/feat_propagation.rs:13-93) over the graph CSR (per-row CDF
+ * weights) and the node -> feature CSR (fptr, fids).  Featureless nodes
+ * receive up to k features of their neighbours; at most max_iters in-place
+ * sweeps.  Writes the new node -> feature CSR to fptr_out (n+1) and fids_out
+ * (capacity out_cap ids: fptr[n] + k * featureless nodes suffices).  Returns
+ * the number of ids written, or a negative status. */
+int64_t ep_propagate_features(uint64_t n, const uint64_t* rows, const uint32_t* cols, const float* cdf,
+                              const uint64_t* fptr, const uint32_t* fids, uint32_t max_iters, uint32_t k,
+                              float threshold, uint64_t* fptr_out, uint32_t* fids_out, uint64_t out_cap);
+
 #ifdef __cplusplus
 }
 #endif
