@@ -62,6 +62,10 @@ struct ep_ctx {
     ep_config cfg{};
     int device = 0;
     cudaStream_t stream = nullptr;
+    // side branch of captured batches: k_batch_end runs beside the sort and
+    // reduction (it reads only the loss, status and sample counts)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string err;
 
     // sizes
@@ -113,6 +117,9 @@ struct ep_ctx {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (gexec_run) cudaGraphExecDestroy(gexec_run);
         if (h_st) cudaFreeHost(h_st);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -203,6 +210,9 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     c->cfg = *cfg;
     c->device = cfg->device;
     if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaMallocHost((void**)&c->h_st, sizeof(BatchState)) != cudaSuccess || reduce_kernels_setup() != cudaSuccess) {
         g_create_err = std::string("CUDA setup failed: ") + cudaGetErrorString(cudaGetLastError());
         delete c;
@@ -707,8 +717,10 @@ static uint32_t kernels_per_batch(const ep_ctx* c) {
 }
 
 // Issues one training batch on the context stream; ev (optional) receives an
-// event record after each stage (EP_N_STAGES events).
-static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr) {
+// event record after each stage (EP_N_STAGES events).  With fork (graph
+// capture), k_batch_end runs on the side stream beside the sort, reduction
+// and fix-ups, and the batch ends when both branches have.
+static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = false) {
     BatchState* st = c->st.as<BatchState>();
     cudaStream_t s = c->stream;
     launch_batch_begin(st, c->n_train, c->Bcap, c->steps_per_pass, c->total_steps, c->warmup, c->cfg.alpha, 0,
@@ -720,6 +732,13 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr) {
     ForwardParams fp = forward_params(c, st, c->table.p, true, false);
     launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_FORWARD], s);
+    if (fork) {
+        cudaEventRecord(c->ev_fork, s);
+        cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+        launch_batch_end(st, c->loss.p, c->status.as<int32_t>(), c->nbr_cnt.as<uint32_t>(), c->Bcap, c->steps_per_pass,
+                         0, 0, c->side);
+        cudaEventRecord(c->ev_join, c->side);
+    }
     launch_radix_sort(st, c->item_f.as<uint32_t>(), c->key_alt.as<uint32_t>(), c->item_src.as<uint32_t>(),
                       c->item_c.as<float>(), c->idx.as<uint2>(), c->idx_alt.as<uint2>(), c->hist.as<uint32_t>(),
                       c->items_cap, (int)bits_for(c->n_feat), &c->sorted_keys, &c->sorted_vals, s);
@@ -736,7 +755,8 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr) {
                           c->touched.as<uint32_t>(), c->n_touched.as<uint32_t>(), c->dpad,
                           (uint32_t)std::min<uint64_t>(c->n_feat, c->items_cap), c->cfg.seed, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_ADAM], s);
-    launch_batch_end(st, c->loss.p, c->status.as<int32_t>(), c->nbr_cnt.as<uint32_t>(), c->Bcap, c->steps_per_pass, 0, 0, s);
+    if (fork) cudaStreamWaitEvent(s, c->ev_join, 0);
+    else launch_batch_end(st, c->loss.p, c->status.as<int32_t>(), c->nbr_cnt.as<uint32_t>(), c->Bcap, c->steps_per_pass, 0, 0, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_END], s);
     c->launches += kernels_per_batch(c);
 }
@@ -811,7 +831,7 @@ static int launch_train_run(ep_ctx* c, uint32_t n) {
                 cudaGraph_t g = nullptr;
                 CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
                 const uint64_t before = c->launches;
-                for (uint32_t i = 0; i < k; ++i) issue_train_batch(c);
+                for (uint32_t i = 0; i < k; ++i) issue_train_batch(c, nullptr, true);
                 c->launches = before;
                 cudaError_t e = cudaStreamEndCapture(c->stream, &g);
                 if (e != cudaSuccess) return c->cuda_fail(e, "graph capture");
@@ -839,7 +859,7 @@ static int launch_train_batch(ep_ctx* c) {
             cudaGraph_t g = nullptr;
             CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
             const uint64_t before = c->launches;
-            issue_train_batch(c);
+            issue_train_batch(c, nullptr, true);
             c->launches = before;
             cudaError_t e = cudaStreamEndCapture(c->stream, &g);
             if (e != cudaSuccess) return c->cuda_fail(e, "graph capture");

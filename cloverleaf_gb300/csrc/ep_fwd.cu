@@ -169,6 +169,7 @@ __global__ void k_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, ui
         lr = min_alpha + ratio * (alpha - min_alpha);
     }
     st->lr = lr;
+    st->step_cur = (uint32_t)s;
     // gradient noise: LRScheduler::exp_decay(0, noise, decay) at this step
     // (mod.rs:140-146; scheduler.rs:50-52); injected batches keep their value
     if (!injected) st->noise_sigma = noise > 1e-9f ? fmaxf(noise * powf(noise_decay, (float)s), 0.f) : 0.f;

@@ -41,6 +41,8 @@ struct BatchState {
     uint32_t pass;          // 1-based pass index
     uint32_t batch;         // batch index within the pass
     uint64_t step;          // global optimizer step, starts at 1 (mod.rs:153)
+    uint32_t step_cur;      // low bits of the step of the batch in flight (set by k_batch_begin), read
+                            // by the Adam kernels while k_batch_end may already advance `step`
     uint32_t b0;            // first position of this batch in the pass order
     uint32_t n_anchors;     // anchors in this batch
     float lr;               // cos-decay learning rate for `step`

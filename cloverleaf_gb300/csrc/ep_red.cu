@@ -53,7 +53,7 @@ struct AdamStep {
         a.rb1 = 1.f / st->bc1;
         a.rb2 = 1.f / st->bc2;
         a.sigma = st->noise_sigma;
-        a.step = (uint32_t)st->step;
+        a.step = st->step_cur;
         return a;
     }
 };

@@ -143,7 +143,12 @@ def test_large_chung_lu_batches():
 
 
 def _cl_ctx(w, form=_native.FORM_FUSED_BF16, autotune=0):
+    return _cl_ctx_cfg(w, form=form, autotune=autotune)
+
+
+def _cl_ctx_cfg(w, form=_native.FORM_FUSED_BF16, autotune=0, use_graphs=1):
     cfg = _native.default_config()
+    cfg.use_graphs = use_graphs
     ep = w["ep"]
     cfg.dims, cfg.negatives, cfg.loss, cfg.gamma = ep["dims"], ep["negatives"], _native.LOSS_STARSPACE, ep["gamma"]
     cfg.batch_size, cfg.alpha, cfg.passes, cfg.valid_pct = 2048, ep["alpha"], 1, 0.0
@@ -168,6 +173,22 @@ def test_multi_batch_graph_matches_single_batch_graphs(monkeypatch):
         ctx.train_batches(37)
         tables.append(ctx.get_table(w["n_feat"], w["ep"]["dims"]))
     assert np.array_equal(tables[0], tables[1])
+
+
+def test_graph_replays_match_stream_launches():
+    # captured batches run k_batch_end on a side branch beside the sort and
+    # reduction; the table and the pass statistics must equal those of the
+    # same batches launched one kernel after another on one stream
+    w = datagen.workload("cl10m", scale=0.005)
+    out = []
+    for graphs in (1, 0):
+        ctx = _cl_ctx_cfg(w, use_graphs=graphs)
+        st = ctx.train_batches(37)
+        out.append((ctx.get_table(w["n_feat"], w["ep"]["dims"]), st))
+    assert np.array_equal(out[0][0], out[1][0])
+    same = ("pass", "batches", "train_loss", "lr_last", "anchors", "kept_anchors", "items", "gathered_rows",
+            "unique_rows", "sampled_neighbors")
+    assert {k: out[0][1][k] for k in same} == {k: out[1][1][k] for k in same}
 
 
 @pytest.mark.parametrize("form", [_native.FORM_FUSED_BF16, _native.FORM_PLAIN_FP32])
