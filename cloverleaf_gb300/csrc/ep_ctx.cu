@@ -62,10 +62,10 @@ struct ep_ctx {
     ep_config cfg{};
     int device = 0;
     cudaStream_t stream = nullptr;
-    // side branch of captured batches: k_batch_end runs beside the sort and
-    // reduction (it reads only the loss, status and sample counts)
+    // side branch of captured batches: the loss and k_batch_end run beside
+    // the sort (see issue_train_batch)
     cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_loss = nullptr, ev_join = nullptr;
     std::string err;
 
     // sizes
@@ -119,6 +119,7 @@ struct ep_ctx {
         if (h_st) cudaFreeHost(h_st);
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_join) cudaEventDestroy(ev_join);
+        if (ev_loss) cudaEventDestroy(ev_loss);
         if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -213,6 +214,7 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
         cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_loss, cudaEventDisableTiming) != cudaSuccess ||
         cudaMallocHost((void**)&c->h_st, sizeof(BatchState)) != cudaSuccess || reduce_kernels_setup() != cudaSuccess) {
         g_create_err = std::string("CUDA setup failed: ") + cudaGetErrorString(cudaGetLastError());
         delete c;
@@ -718,8 +720,9 @@ static uint32_t kernels_per_batch(const ep_ctx* c) {
 
 // Issues one training batch on the context stream; ev (optional) receives an
 // event record after each stage (EP_N_STAGES events).  With fork (graph
-// capture), k_batch_end runs on the side stream beside the sort, reduction
-// and fix-ups, and the batch ends when both branches have.
+// capture), the loss kernel and k_batch_end run on the side stream beside the
+// sort (which needs only the items the gathers emitted); the reduction waits
+// for the loss, and the batch ends when both branches have.
 static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = false) {
     BatchState* st = c->st.as<BatchState>();
     cudaStream_t s = c->stream;
@@ -730,19 +733,26 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = 
     launch_scan_occ(st, c->occ.as<uint32_t>(), c->Bcap, c->items_cap, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_SAMPLE], s);
     ForwardParams fp = forward_params(c, st, c->table.p, true, false);
-    launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, s);
-    if (ev) cudaEventRecord(ev[EP_STAGE_FORWARD], s);
     if (fork) {
+        // the gathers have emitted the items: the loss, then k_batch_end, run
+        // on the side stream while the items are sorted
+        launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, s, FWD_GATHER);
         cudaEventRecord(c->ev_fork, s);
         cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+        launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, c->side, FWD_LOSS);
+        cudaEventRecord(c->ev_loss, c->side);
         launch_batch_end(st, c->loss.p, c->status.as<int32_t>(), c->nbr_cnt.as<uint32_t>(), c->Bcap, c->steps_per_pass,
                          0, 0, c->side);
         cudaEventRecord(c->ev_join, c->side);
+    } else {
+        launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, s);
     }
+    if (ev) cudaEventRecord(ev[EP_STAGE_FORWARD], s);
     launch_radix_sort(st, c->item_f.as<uint32_t>(), c->key_alt.as<uint32_t>(), c->item_src.as<uint32_t>(),
                       c->item_c.as<float>(), c->idx.as<uint2>(), c->idx_alt.as<uint2>(), c->hist.as<uint32_t>(),
                       c->items_cap, (int)bits_for(c->n_feat), &c->sorted_keys, &c->sorted_vals, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_SORT], s);
+    if (fork) cudaStreamWaitEvent(s, c->ev_loss, 0);    // directions and scales for the reduction
     const bool plain = c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_mode == 1;
     if (plain) cudaMemsetAsync(c->n_touched.p, 0, 4, s);
     ReduceParams rp = reduce_params(c, st, plain ? OUT_DENSE : (c->fused_mode == 2 ? OUT_QUEUE : OUT_ADAM), c->table.p);

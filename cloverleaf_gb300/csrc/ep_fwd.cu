@@ -1563,7 +1563,7 @@ void launch_scan_occ(BatchState* st, uint32_t* occ, uint32_t cap, uint64_t items
 }
 
 template <typename T, typename A, int VPL>
-static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s) {
+static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s, int part) {
     const uint32_t blocks = (cap + FWD_WARPS - 1) / FWD_WARPS;
     const size_t smem = sizeof(WarpTables) * FWD_WARPS;
     static bool attr = false;   // opt in to > 48 KB of dynamic shared memory once
@@ -1571,26 +1571,28 @@ static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s) {
         cudaFuncSetAttribute(k_fwd_gather<T, A, VPL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
     }
-    launch_chain(k_fwd_gather<T, A, VPL, true>, blocks, 32 * FWD_WARPS, smem, s, p);
-    launch_chain(k_fwd_gather<T, A, VPL, false>, blocks, 32 * FWD_WARPS, 0, s, p);
-    launch_chain(k_fwd_loss<T, A, VPL>, (cap + 3) / 4, 128, 0, s, p);
+    if (part != FWD_LOSS) {
+        launch_chain(k_fwd_gather<T, A, VPL, true>, blocks, 32 * FWD_WARPS, smem, s, p);
+        launch_chain(k_fwd_gather<T, A, VPL, false>, blocks, 32 * FWD_WARPS, 0, s, p);
+    }
+    if (part != FWD_GATHER) launch_chain(k_fwd_loss<T, A, VPL>, (cap + 3) / 4, 128, 0, s, p);
 }
 
 template <typename T, typename A>
-static void fwd_dispatch(int vpl, const ForwardParams& p, uint32_t cap, cudaStream_t s) {
+static void fwd_dispatch(int vpl, const ForwardParams& p, uint32_t cap, cudaStream_t s, int part) {
     switch (vpl) {
-        case 1: fwd_launch<T, A, 1>(p, cap, s); break;
-        case 2: fwd_launch<T, A, 2>(p, cap, s); break;
-        case 4: fwd_launch<T, A, 4>(p, cap, s); break;
-        case 8: fwd_launch<T, A, 8>(p, cap, s); break;
-        default: fwd_launch<T, A, 16>(p, cap, s); break;
+        case 1: fwd_launch<T, A, 1>(p, cap, s, part); break;
+        case 2: fwd_launch<T, A, 2>(p, cap, s, part); break;
+        case 4: fwd_launch<T, A, 4>(p, cap, s, part); break;
+        case 8: fwd_launch<T, A, 8>(p, cap, s, part); break;
+        default: fwd_launch<T, A, 16>(p, cap, s, part); break;
     }
 }
 
-void launch_forward(int tt, int vpl, const ForwardParams& p, uint32_t cap, cudaStream_t s) {
-    if (tt == TT_F32) fwd_dispatch<float, float>(vpl, p, cap, s);
-    else if (tt == TT_BF16) fwd_dispatch<__nv_bfloat16, float>(vpl, p, cap, s);
-    else fwd_dispatch<double, double>(vpl, p, cap, s);
+void launch_forward(int tt, int vpl, const ForwardParams& p, uint32_t cap, cudaStream_t s, int part) {
+    if (tt == TT_F32) fwd_dispatch<float, float>(vpl, p, cap, s, part);
+    else if (tt == TT_BF16) fwd_dispatch<__nv_bfloat16, float>(vpl, p, cap, s, part);
+    else fwd_dispatch<double, double>(vpl, p, cap, s, part);
 }
 
 void launch_batch_end(BatchState* st, const void* loss, const int32_t* status, const uint32_t* nbr_cnt,
