@@ -89,15 +89,37 @@ __device__ __forceinline__ void adam_apply(T* __restrict__ table, float* __restr
             if (k + 1 < VPL) gn[k + 1] += as.sigma * rad * sn;
         }
     }
+    if constexpr (VPL % 2 == 0) {
+        // element pairs through the packed FP32 operations of sm_100+ (each
+        // lane of a pair rounded as the scalar operation would be)
+        const float2 B1 = make_float2(b1, b1), C1 = make_float2(1.f - b1, 1.f - b1);
+        const float2 B2 = make_float2(b2, b2), C2 = make_float2(1.f - b2, 1.f - b2);
+        const float2 R1 = make_float2(rb1, rb1), R2 = make_float2(rb2, rb2), E = make_float2(eps, eps);
+        const float2 NL = make_float2(-lr, -lr);
 #pragma unroll
-    for (int k = 0; k < VPL; ++k) {
-        const float gk = gn[k];
-        mm[k] = b1 * mm[k] + (1.f - b1) * gk;
-        vv[k] = b2 * vv[k] + (1.f - b2) * (gk * gk);
-        const float mh = mm[k] * rb1;
-        const float vh = vv[k] * rb2;
-        // the denominator is >= eps = 1e-8, inside __fdividef's full-accuracy range
-        ee[k] -= lr * __fdividef(mh, sqrtf(vh) + eps);
+        for (int k = 0; k < VPL; k += 2) {
+            const float2 g = make_float2(gn[k], gn[k + 1]);
+            const float2 m2 = __ffma2_rn(B1, make_float2(mm[k], mm[k + 1]), __fmul2_rn(C1, g));
+            const float2 v2 = __ffma2_rn(B2, make_float2(vv[k], vv[k + 1]), __fmul2_rn(C2, __fmul2_rn(g, g)));
+            const float2 mh = __fmul2_rn(m2, R1), vh = __fmul2_rn(v2, R2);
+            const float2 den = __fadd2_rn(make_float2(sqrtf(vh.x), sqrtf(vh.y)), E);
+            // the denominator is >= eps = 1e-8, inside __fdividef's full-accuracy range
+            const float2 q = make_float2(__fdividef(mh.x, den.x), __fdividef(mh.y, den.y));
+            const float2 e2 = __ffma2_rn(NL, q, make_float2(ee[k], ee[k + 1]));
+            mm[k] = m2.x; mm[k + 1] = m2.y;
+            vv[k] = v2.x; vv[k + 1] = v2.y;
+            ee[k] = e2.x; ee[k + 1] = e2.y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+            const float gk = gn[k];
+            mm[k] = fmaf(b1, mm[k], (1.f - b1) * gk);
+            vv[k] = fmaf(b2, vv[k], (1.f - b2) * (gk * gk));
+            const float mh = mm[k] * rb1;
+            const float vh = vv[k] * rb2;
+            ee[k] = fmaf(-lr, __fdividef(mh, sqrtf(vh) + eps), ee[k]);
+        }
     }
     RowIO<float, VPL>::store_raw(m + o, lane, mm);
     RowIO<float, VPL>::store_raw(v + o, lane, vv);
@@ -710,10 +732,12 @@ __global__ void __launch_bounds__(fixl_threads(VPL)) k_fixup_long(ReduceParams p
 #pragma unroll
         for (int k = 0; k < VPL; ++k) acc[k] = 0;
         uint32_t kept = 0;
-        for (uint32_t j = c + 1 + w; j <= last; j += 4 * NWARP) {
-            A h[4][VPL];
+        // FL head rows in flight per warp
+        constexpr int FL = sizeof(A) == 8 ? 4 : 8;
+        for (uint32_t j = c + 1 + w; j <= last; j += FL * NWARP) {
+            A h[FL][VPL];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < FL; ++u) {
                 const uint32_t jj = j + u * NWARP;
                 if (jj <= last) {
                     kept |= p.carry_flags[jj] & CF_HEAD_KEPT;
@@ -721,7 +745,7 @@ __global__ void __launch_bounds__(fixl_threads(VPL)) k_fixup_long(ReduceParams p
                 }
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < FL; ++u) {
                 if (j + u * NWARP <= last && lane_on) {
 #pragma unroll
                     for (int k = 0; k < VPL; ++k) acc[k] += h[u][k];
