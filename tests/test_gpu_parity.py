@@ -199,3 +199,17 @@ def test_bad_inputs_fail_cleanly():
     c2.upload_features(prob["fptr"], prob["fids"], prob["n_feat"])
     c2.set_table(prob["table"])
     assert c2.train(1)[0]["anchors"] > 0
+
+
+@pytest.mark.parametrize("n_feat", [600_000, (1 << 21) + 7])
+def test_batch_grad_wide_feature_ids(oracle, n_feat):
+    # 20- and 22-bit feature ids: three digit passes of the radix sort, the
+    # last one partial; a few hot features share many items
+    prob = random_problem(77, n=400, n_feat=n_feat, dims=8)
+    rng = np.random.default_rng(78)
+    hot = rng.random(len(prob["fids"])) < 0.5
+    prob["fids"][hot] = rng.integers(n_feat - 40, n_feat, int(hot.sum())).astype(np.uint32)
+    smp = sample_batch(79, prob, B=128, K=6, R=5)
+    ctx = make_ctx(prob, loss=1, gamma=0.5, R=5)
+    ids, _ = check_parity(oracle, prob, smp, ctx, prob["table"], loss=1, gamma=0.5)
+    assert ids.max() >= n_feat - 40 and ids.min() < n_feat // 2
