@@ -154,8 +154,19 @@ SIGNATURES = {
     "ep_csr_from_edges": (ctypes.c_int, [_U64, _P, _P, _P, ctypes.c_int, _P, _P, _P, _P, _P]),
     "ep_cdf_convert": (ctypes.c_int, [_U64, _P, _P]),
     "ep_format_embeddings": (ctypes.c_int64, [_U64, _U32, _P, _P, _P, _P, _P, _U64, _P, _U64]),
-    "ep_parse_embeddings": (ctypes.c_int64, [_P, _U64, ctypes.POINTER(_U32), _P, _P]),
+    "ep_parse_embeddings": (ctypes.c_int64, [_P, _U64, ctypes.POINTER(_U32), _P, _P, ctypes.POINTER(_U64)]),
     "ep_propagate_features": (ctypes.c_int64, [_U64, _P, _P, _P, _P, _P, _U32, _U32, _F32, _P, _P, _U64]),
+    "ep_vocab_create": (ctypes.c_int, [ctypes.POINTER(_P)]),
+    "ep_vocab_destroy": (None, [_P]),
+    "ep_vocab_len": (_U64, [_P]),
+    "ep_vocab_max_key": (_U64, [_P]),
+    "ep_vocab_intern": (ctypes.c_int64, [_P, ctypes.c_char_p, _U64, ctypes.c_char_p, _U64]),
+    "ep_vocab_find": (ctypes.c_int64, [_P, ctypes.c_char_p, _U64, ctypes.c_char_p, _U64]),
+    "ep_vocab_intern_tokens": (ctypes.c_int, [_P, _P, _P, _U64, _P]),
+    "ep_vocab_range_bytes": (ctypes.c_int, [_P, _U64, _U64, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
+    "ep_vocab_export": (ctypes.c_int, [_P, _U64, _U64, _P, _P, _P, _P]),
+    "ep_parse_edges": (ctypes.c_int64, [_P, _P, _U64, ctypes.c_int, _P, _P, _P, _U64, ctypes.POINTER(_U64)]),
+    "ep_format_edges": (ctypes.c_int64, [_P, _U64, _P, _P, _P, _U64, _U64, _P, _U64]),
     "epg_sbm": (ctypes.c_int, [_U64, _U32, ctypes.c_double, ctypes.c_double, _U64, _P, _P, _P, _P, _P]),
     "epg_sbm_tokens": (ctypes.c_int, [_U64, _P, _U32, _U32, _U32, _U32, ctypes.c_double, _U32, _U64, _P, _P,
                                       _P, _P, _P]),
@@ -394,7 +405,8 @@ def parse_embeddings(buf: bytes, dims=None):
     Raises ValueError naming the first bad line.  (``ep_parse_embeddings``)"""
     arr = np.frombuffer(buf, np.uint8)
     d = _U32(0)
-    rows = int(lib().ep_parse_embeddings(ptr(arr), len(arr), ctypes.byref(d), None, None))
+    bad = _U64(0)
+    rows = int(lib().ep_parse_embeddings(ptr(arr), len(arr), ctypes.byref(d), None, None, ctypes.byref(bad)))
     if rows < 0:
         check(rows, None, "ep_parse_embeddings")
     if rows and d.value == 0:
@@ -403,16 +415,105 @@ def parse_embeddings(buf: bytes, dims=None):
         d = _U32(int(dims))
     vals = np.empty((max(rows, 1), d.value), np.float32)
     tok = np.empty((max(rows, 1), 4), np.uint64)
-    got = lib().ep_parse_embeddings(ptr(arr), len(arr), ctypes.byref(d), ptr(vals), ptr(tok))
+    got = lib().ep_parse_embeddings(ptr(arr), len(arr), ctypes.byref(d), ptr(vals), ptr(tok), ctypes.byref(bad))
     if got < 0:
-        line = _line(buf, -got)
+        if not bad.value:
+            check(int(got), None, "ep_parse_embeddings")
+        line = _line(buf, bad.value)
         alone = _U32(0)
         one = np.frombuffer(line, np.uint8)
-        if lib().ep_parse_embeddings(ptr(one), len(one), ctypes.byref(alone), None, None) == 1 and alone.value:
+        if lib().ep_parse_embeddings(ptr(one), len(one), ctypes.byref(alone), None, None, None) == 1 and alone.value:
             raise ValueError(f"Embeddings have different sizes! ({alone.value} values, expected {d.value}, "
                              f"line: {line[:200]!r})")
         raise ValueError(f"Error parsing line: {line[:200]!r}")
     return vals[:got], tok[:got]
+
+
+class NativeVocabHandle:
+    """Owns an ``ep_vocab``."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        check(lib().ep_vocab_create(ctypes.byref(h)), None, "ep_vocab_create")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ep_vocab_destroy(self.h)
+            self.h = None
+
+    def __len__(self) -> int:
+        return int(lib().ep_vocab_len(self.h))
+
+    def intern(self, node_type: str, name: str) -> int:
+        t, n = node_type.encode(), name.encode()
+        r = int(lib().ep_vocab_intern(self.h, t, len(t), n, len(n)))
+        if r < 0:
+            check(r, None, "ep_vocab_intern")
+        return r
+
+    def find(self, node_type: str, name: str) -> int:
+        t, n = node_type.encode(), name.encode()
+        return int(lib().ep_vocab_find(self.h, t, len(t), n, len(n)))
+
+    def intern_tokens(self, buf: bytes, tok: np.ndarray) -> np.ndarray:
+        """Ids of the keys of buf at the (type, name) byte ranges tok [n, 4]."""
+        arr = np.frombuffer(buf, np.uint8)
+        tok = np.ascontiguousarray(tok, np.uint64)
+        ids = np.empty(max(len(tok), 1), np.uint32)
+        check(lib().ep_vocab_intern_tokens(self.h, ptr(arr), ptr(tok), len(tok), ptr(ids)), None,
+              "ep_vocab_intern_tokens")
+        return ids[:len(tok)]
+
+    def export(self, lo: int, hi: int):
+        """(types, names) of ids [lo, hi) as lists of str."""
+        tb, nb = _U64(0), _U64(0)
+        check(lib().ep_vocab_range_bytes(self.h, lo, hi, ctypes.byref(tb), ctypes.byref(nb)), None, "ep_vocab_export")
+        types = np.empty(max(tb.value, 1), np.uint8)
+        names = np.empty(max(nb.value, 1), np.uint8)
+        toff = np.empty(hi - lo + 1, np.uint64)
+        noff = np.empty(hi - lo + 1, np.uint64)
+        check(lib().ep_vocab_export(self.h, lo, hi, ptr(types), ptr(toff), ptr(names), ptr(noff)), None,
+              "ep_vocab_export")
+        tbytes, nbytes = types.tobytes(), names.tobytes()
+        to, no = toff.tolist(), noff.tolist()
+        return ([tbytes[to[i]:to[i + 1]].decode() for i in range(hi - lo)],
+                [nbytes[no[i]:no[i + 1]].decode() for i in range(hi - lo)])
+
+
+def parse_edges(vocab: NativeVocabHandle, buf: bytes, weighted: bool):
+    """GraphReader::load's line step (io.rs:270-323) through
+    ``ep_parse_edges``: (src ids, dst ids, weights) of the block's lines."""
+    arr = np.frombuffer(buf, np.uint8)
+    cap = buf.count(b"\n") + 1
+    src = np.empty(cap, np.uint32)
+    dst = np.empty(cap, np.uint32)
+    w = np.empty(cap, np.float32)
+    bad = _U64(0)
+    n = int(lib().ep_parse_edges(vocab.h, ptr(arr), len(arr), int(bool(weighted)), ptr(src), ptr(dst), ptr(w), cap,
+                                 ctypes.byref(bad)))
+    if n < 0:
+        if bad.value:
+            raise ValueError(f"Malformed graph file: expected 5 fields with a numeric weight, got "
+                             f"{_line(buf, bad.value)[:200]!r}")
+        check(n, None, "ep_parse_edges")
+    return src[:n], dst[:n], w[:n]
+
+
+def format_edges(vocab: NativeVocabHandle, rows, cols, cdf, lo: int, hi: int) -> bytes:
+    """Graph::save (lib.rs:414-430) lines of the rows of nodes [lo, hi)
+    (``ep_format_edges``)."""
+    rows = np.ascontiguousarray(rows, np.uint64)
+    cols = np.ascontiguousarray(cols, np.uint32)
+    cdf = np.ascontiguousarray(cdf, np.float32)
+    n = len(rows) - 1
+    ne = int(rows[hi] - rows[lo])
+    cap = ne * (2 * int(lib().ep_vocab_max_key(vocab.h)) + 54) + 1
+    out = np.empty(cap, np.uint8)
+    r = int(lib().ep_format_edges(vocab.h, n, ptr(rows), ptr(cols), ptr(cdf), lo, hi, ptr(out), cap))
+    if r < 0:
+        check(r, None, "ep_format_edges")
+    return out[:r].tobytes()
 
 
 def propagate_features(rows, cols, cdf, fptr, fids, max_iters: int, k: int, threshold: float):

@@ -1023,7 +1023,7 @@ __device__ __forceinline__ bool warp_all_finite(const A (&x)[VPL]) {
 // the flagged anchors only (every anchor when p.deferred is null).  Both
 // produce identical items, means and totals.
 template <typename T, typename A, int VPL, bool STAGED>
-__global__ void __launch_bounds__(256, STAGED ? (VPL <= 4 ? 4 : 3) : 1) k_fwd_gather(ForwardParams p) {
+__global__ void __launch_bounds__(256, STAGED ? (VPL <= 8 ? 4 : 3) : 1) k_fwd_gather(ForwardParams p) {
     pdl_wait();
     pdl_trigger();
     const int lane = threadIdx.x & 31;

@@ -549,8 +549,9 @@ extern "C" int64_t ep_format_embeddings(uint64_t n, uint32_t dims, const float* 
 }
 
 extern "C" int64_t ep_parse_embeddings(const char* buf, uint64_t len, uint32_t* dims, float* values,
-                                       uint64_t* tok_off) {
+                                       uint64_t* tok_off, uint64_t* bad_line) {
     if ((len && !buf) || !dims) return EP_ERR_INVALID_ARG;
+    if (bad_line) *bad_line = 0;
     // line starts; blank lines are skipped
     std::vector<uint64_t> start;
     for (uint64_t i = 0; i < len;) {
@@ -624,7 +625,10 @@ extern "C" int64_t ep_parse_embeddings(const char* buf, uint64_t len, uint32_t* 
             while (r < cur && !first_bad.compare_exchange_weak(cur, r)) {}
         }
     }
-    if (first_bad.load() != INT64_MAX) return -(first_bad.load() + 1);
+    if (first_bad.load() != INT64_MAX) {
+        if (bad_line) *bad_line = (uint64_t)first_bad.load() + 1;
+        return EP_ERR_INVALID_ARG;
+    }
     return rows;
 }
 
@@ -715,4 +719,271 @@ extern "C" int64_t ep_propagate_features(uint64_t n, const uint64_t* rows, const
         fptr_out[v + 1] = o;
     }
     return (int64_t)o;
+}
+
+// ---------------------------------------------------------------------------
+// Vocabulary of (node type, name) pairs -> dense ids in first-seen order
+// (Vocab, src/vocab.rs), and the graph text format of GraphReader::load
+// (src/io.rs:270-323) and Graph::save (src/lib.rs:414-430):
+// "from_type\tfrom\tto_type\tto\tweight" lines.
+//
+// The vocabulary keeps every key as "type\0name" in one byte arena and an
+// open-addressing table of ids keyed by a 64-bit hash of the key.
+// ---------------------------------------------------------------------------
+namespace {
+inline uint64_t key_hash(const char* t, size_t tl, const char* n, size_t nl) {
+    // FNV-1a over type, a separator and name, then a murmur-style finalizer
+    uint64_t h = 1469598103934665603ull;
+    for (size_t i = 0; i < tl; ++i) h = (h ^ (unsigned char)t[i]) * 1099511628211ull;
+    h = (h ^ 0xffu) * 1099511628211ull;
+    for (size_t i = 0; i < nl; ++i) h = (h ^ (unsigned char)n[i]) * 1099511628211ull;
+    h ^= h >> 33;
+    h *= 0xff51afd7ed558ccdull;
+    h ^= h >> 33;
+    return h;
+}
+}  // namespace
+
+struct ep_vocab {
+    std::vector<char> arena;            // keys back to back: type, '\0', name
+    std::vector<uint64_t> off;          // key i is arena[off[i], off[i+1]); off.size() = size + 1
+    std::vector<uint32_t> type_len;     // bytes of the type of key i
+    std::vector<uint32_t> slots;        // id + 1, 0 = empty
+    uint64_t mask = 0;
+    uint64_t max_key = 0;               // longest type + name, in bytes
+    ep_vocab() : off(1, 0) {}
+    uint64_t size() const { return off.size() - 1; }
+    bool same(uint64_t id, const char* t, size_t tl, const char* n, size_t nl) const {
+        if (type_len[id] != tl || off[id + 1] - off[id] != tl + 1 + nl) return false;
+        const char* k = arena.data() + off[id];
+        return memcmp(k, t, tl) == 0 && memcmp(k + tl + 1, n, nl) == 0;
+    }
+    void grow() {
+        const uint64_t cap = slots.empty() ? 1024 : slots.size() * 2;
+        slots.assign(cap, 0);
+        mask = cap - 1;
+        for (uint64_t id = 0; id < size(); ++id) {
+            const char* k = arena.data() + off[id];
+            const uint32_t tl = type_len[id];
+            uint64_t h = key_hash(k, tl, k + tl + 1, off[id + 1] - off[id] - tl - 1) & mask;
+            while (slots[h]) h = (h + 1) & mask;
+            slots[h] = (uint32_t)(id + 1);
+        }
+    }
+    int64_t find(const char* t, size_t tl, const char* n, size_t nl, uint64_t hash) const {
+        if (slots.empty()) return -1;
+        for (uint64_t h = hash & mask;; h = (h + 1) & mask) {
+            const uint32_t s = slots[h];
+            if (!s) return -1;
+            if (same(s - 1, t, tl, n, nl)) return (int64_t)(s - 1);
+        }
+    }
+    // id of the key, inserted at the end when new; -1 when the vocabulary is full
+    int64_t intern(const char* t, size_t tl, const char* n, size_t nl, uint64_t hash) {
+        if ((size() + 1) * 2 > slots.size()) grow();
+        uint64_t h = hash & mask;
+        for (;; h = (h + 1) & mask) {
+            const uint32_t s = slots[h];
+            if (!s) break;
+            if (same(s - 1, t, tl, n, nl)) return (int64_t)(s - 1);
+        }
+        const uint64_t id = size();
+        if (id >= 0xffffffffull) return -1;
+        arena.insert(arena.end(), t, t + tl);
+        arena.push_back('\0');
+        arena.insert(arena.end(), n, n + nl);
+        off.push_back(arena.size());
+        type_len.push_back((uint32_t)tl);
+        max_key = std::max<uint64_t>(max_key, tl + nl);
+        slots[h] = (uint32_t)(id + 1);
+        return (int64_t)id;
+    }
+};
+
+extern "C" int ep_vocab_create(ep_vocab** out) {
+    if (!out) return EP_ERR_INVALID_ARG;
+    *out = new (std::nothrow) ep_vocab();
+    return *out ? EP_OK : EP_ERR_OOM;
+}
+
+extern "C" void ep_vocab_destroy(ep_vocab* v) { delete v; }
+
+extern "C" uint64_t ep_vocab_len(const ep_vocab* v) { return v ? v->size() : 0; }
+
+extern "C" uint64_t ep_vocab_max_key(const ep_vocab* v) { return v ? v->max_key : 0; }
+
+extern "C" int64_t ep_vocab_intern(ep_vocab* v, const char* type, uint64_t type_len, const char* name,
+                                   uint64_t name_len) {
+    if (!v || (type_len && !type) || (name_len && !name)) return EP_ERR_INVALID_ARG;
+    const int64_t id = v->intern(type, type_len, name, name_len, key_hash(type, type_len, name, name_len));
+    return id < 0 ? EP_ERR_INVALID_ARG : id;
+}
+
+extern "C" int64_t ep_vocab_find(const ep_vocab* v, const char* type, uint64_t type_len, const char* name,
+                                 uint64_t name_len) {
+    if (!v || (type_len && !type) || (name_len && !name)) return EP_ERR_INVALID_ARG;
+    return v->find(type, type_len, name, name_len, key_hash(type, type_len, name, name_len));
+}
+
+extern "C" int ep_vocab_intern_tokens(ep_vocab* v, const char* buf, const uint64_t* tok, uint64_t n, uint32_t* ids) {
+    if (!v || (n && (!buf || !tok || !ids))) return EP_ERR_INVALID_ARG;
+    std::vector<uint64_t> h(n);
+#pragma omp parallel for schedule(static) if (n > 4096)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        const uint64_t* t = tok + 4 * i;
+        h[i] = key_hash(buf + t[0], t[1] - t[0], buf + t[2], t[3] - t[2]);
+    }
+    for (uint64_t i = 0; i < n; ++i) {
+        const uint64_t* t = tok + 4 * i;
+        const int64_t id = v->intern(buf + t[0], t[1] - t[0], buf + t[2], t[3] - t[2], h[i]);
+        if (id < 0) return EP_ERR_INVALID_ARG;
+        ids[i] = (uint32_t)id;
+    }
+    return EP_OK;
+}
+
+extern "C" int ep_vocab_range_bytes(const ep_vocab* v, uint64_t lo, uint64_t hi, uint64_t* type_bytes,
+                                    uint64_t* name_bytes) {
+    if (!v || lo > hi || hi > v->size()) return EP_ERR_INVALID_ARG;
+    uint64_t tb = 0, nb = 0;
+    for (uint64_t i = lo; i < hi; ++i) {
+        tb += v->type_len[i];
+        nb += v->off[i + 1] - v->off[i] - v->type_len[i] - 1;
+    }
+    if (type_bytes) *type_bytes = tb;
+    if (name_bytes) *name_bytes = nb;
+    return EP_OK;
+}
+
+extern "C" int ep_vocab_export(const ep_vocab* v, uint64_t lo, uint64_t hi, char* types, uint64_t* type_off,
+                               char* names, uint64_t* name_off) {
+    if (!v || lo > hi || hi > v->size() || !type_off || !name_off) return EP_ERR_INVALID_ARG;
+    uint64_t tb = 0, nb = 0;
+    type_off[0] = name_off[0] = 0;
+    for (uint64_t i = lo; i < hi; ++i) {
+        const char* k = v->arena.data() + v->off[i];
+        const uint64_t tl = v->type_len[i], nl = v->off[i + 1] - v->off[i] - tl - 1;
+        if (types) memcpy(types + tb, k, tl);
+        if (names) memcpy(names + nb, k + tl + 1, nl);
+        tb += tl;
+        nb += nl;
+        type_off[i - lo + 1] = tb;
+        name_off[i - lo + 1] = nb;
+    }
+    return EP_OK;
+}
+
+extern "C" int64_t ep_parse_edges(ep_vocab* v, const char* buf, uint64_t len, int weighted, uint32_t* src,
+                                  uint32_t* dst, float* w, uint64_t cap, uint64_t* bad_line) {
+    if (!v || (len && !buf) || !src || !dst || !w) return EP_ERR_INVALID_ARG;
+    if (bad_line) *bad_line = 0;
+    std::vector<uint64_t> start;
+    for (uint64_t i = 0; i < len;) {
+        const void* nl = memchr(buf + i, '\n', len - i);
+        const uint64_t e = nl ? (uint64_t)((const char*)nl - buf) : len;
+        if (e > i && !(e == i + 1 && buf[i] == '\r')) start.push_back(i);
+        i = e + 1;
+    }
+    const int64_t rows = (int64_t)start.size();
+    if ((uint64_t)rows > cap) return EP_ERR_INVALID_ARG;
+    // fields and key hashes in parallel; ids in line order afterwards
+    struct Line { uint64_t f[5][2]; uint64_t h0, h1; };
+    std::vector<Line> L((size_t)rows);
+    std::atomic<int64_t> first_bad{INT64_MAX};
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t r = 0; r < rows; ++r) {
+        const uint64_t b = start[r];
+        const void* nl = memchr(buf + b, '\n', len - b);
+        uint64_t e = nl ? (uint64_t)((const char*)nl - buf) : len;
+        if (e > b && buf[e - 1] == '\r') --e;
+        Line& x = L[r];
+        uint64_t p = b;
+        bool ok = true;
+        for (int k = 0; k < 5 && ok; ++k) {
+            const void* t = k < 4 ? memchr(buf + p, '\t', e - p) : nullptr;
+            const uint64_t q = k < 4 ? (t ? (uint64_t)((const char*)t - buf) : e) : e;
+            if (k < 4 && !t) ok = false;
+            x.f[k][0] = p;
+            x.f[k][1] = q;
+            p = q + 1;
+        }
+        if (ok && memchr(buf + x.f[4][0], '\t', x.f[4][1] - x.f[4][0])) ok = false;     // more than 5 fields
+        float wt = 1.f;
+        if (ok && weighted) {
+            const char* s0 = buf + x.f[4][0];
+            const char* s1 = buf + x.f[4][1];
+            if (s1 - s0 > 1 && *s0 == '+' && s0[1] != '-') ++s0;
+            auto res = std::from_chars(s0, s1, wt);
+            if (res.ec == std::errc::result_out_of_range) {
+                double dv = 0.0;
+                res = std::from_chars(s0, s1, dv);
+                wt = (float)dv;
+            }
+            ok = s0 < s1 && res.ec == std::errc() && res.ptr == s1;
+        }
+        if (!ok) {
+            int64_t cur = first_bad.load();
+            while (r < cur && !first_bad.compare_exchange_weak(cur, r)) {}
+            continue;
+        }
+        w[r] = wt;
+        x.h0 = key_hash(buf + x.f[0][0], x.f[0][1] - x.f[0][0], buf + x.f[1][0], x.f[1][1] - x.f[1][0]);
+        x.h1 = key_hash(buf + x.f[2][0], x.f[2][1] - x.f[2][0], buf + x.f[3][0], x.f[3][1] - x.f[3][0]);
+    }
+    if (first_bad.load() != INT64_MAX) {
+        if (bad_line) *bad_line = (uint64_t)first_bad.load() + 1;
+        return EP_ERR_INVALID_ARG;
+    }
+    for (int64_t r = 0; r < rows; ++r) {
+        const Line& x = L[r];
+        const int64_t a = v->intern(buf + x.f[0][0], x.f[0][1] - x.f[0][0], buf + x.f[1][0], x.f[1][1] - x.f[1][0], x.h0);
+        const int64_t c = v->intern(buf + x.f[2][0], x.f[2][1] - x.f[2][0], buf + x.f[3][0], x.f[3][1] - x.f[3][0], x.h1);
+        if (a < 0 || c < 0) return EP_ERR_INVALID_ARG;
+        src[r] = (uint32_t)a;
+        dst[r] = (uint32_t)c;
+    }
+    return rows;
+}
+
+extern "C" int64_t ep_format_edges(const ep_vocab* v, uint64_t n_nodes, const uint64_t* rows, const uint32_t* cols,
+                                   const float* cdf, uint64_t lo, uint64_t hi, char* out, uint64_t out_cap) {
+    if (!v || !rows || lo > hi || hi > n_nodes || v->size() < n_nodes || (hi > lo && !out)) return EP_ERR_INVALID_ARG;
+    const int nt = (int)std::min<uint64_t>((uint64_t)omp_get_max_threads(), std::max<uint64_t>(1, (hi - lo) / 256));
+    std::vector<std::string> part(nt);
+    std::atomic<int> bad{0};
+#pragma omp parallel num_threads(nt)
+    {
+        const int t = omp_get_thread_num();
+        const uint64_t a = lo + (hi - lo) * t / nt, b = lo + (hi - lo) * (t + 1) / nt;
+        std::string& o = part[t];
+        char num[64];
+        for (uint64_t u = a; u < b; ++u) {
+            const char* fk = v->arena.data() + v->off[u];
+            const uint64_t ftl = v->type_len[u], fnl = v->off[u + 1] - v->off[u] - ftl - 1;
+            float prev = 0.f;
+            for (uint64_t e = rows[u]; e < rows[u + 1]; ++e) {
+                const uint32_t x = cols[e];
+                if (x >= n_nodes) { bad = 1; break; }
+                const float p = cdf[e] - prev;     // CDFtoP (src/graph.rs:630-661)
+                prev = cdf[e];
+                const char* tk = v->arena.data() + v->off[x];
+                const uint64_t ttl = v->type_len[x], tnl = v->off[x + 1] - v->off[x] - ttl - 1;
+                o.append(fk, ftl); o.push_back('\t');
+                o.append(fk + ftl + 1, fnl); o.push_back('\t');
+                o.append(tk, ttl); o.push_back('\t');
+                o.append(tk + ttl + 1, tnl); o.push_back('\t');
+                // f32 as Rust's Display writes it: shortest round-trip digits, positional
+                char* z = std::to_chars(num, num + sizeof num, p, std::chars_format::fixed).ptr;
+                o.append(num, z - num);
+                o.push_back('\n');
+            }
+        }
+    }
+    if (bad) return EP_ERR_INVALID_ARG;
+    uint64_t total = 0;
+    for (const auto& x : part) total += x.size();
+    if (total > out_cap) return EP_ERR_INVALID_ARG;
+    uint64_t o = 0;
+    for (const auto& x : part) { memcpy(out + o, x.data(), x.size()); o += x.size(); }
+    return (int64_t)total;
 }

@@ -178,7 +178,7 @@ class NodeEmbeddings:
         comp_level, default 1, io.rs:215-227).  Rows are formatted natively
         in blocks (``ep_format_embeddings``), each value the shortest decimal
         that reads back to the same f32."""
-        from .graph import RangeVocab
+        from .graph import NativeVocab, RangeVocab
 
         v, n = self.vocab_, self.len()
         if path.endswith(".gz"):
@@ -193,7 +193,7 @@ class NodeEmbeddings:
                 if isinstance(v, RangeVocab) and hi <= v._n:     # names are the decimal ids
                     f.write(_native.format_embeddings(self.table[lo:hi], v._type, None, lo))
                 else:
-                    names = [v.get_name(i) for i in range(lo, hi)]
+                    names = v.names(lo, hi) if isinstance(v, NativeVocab) else [v.get_name(i) for i in range(lo, hi)]
                     f.write(_native.format_embeddings(self.table[lo:hi], [t for t, _ in names],
                                                       [x for _, x in names]))
 
@@ -204,13 +204,16 @@ class NodeEmbeddings:
         io.rs:134-198): skip_rows leading lines are skipped, filter_type keeps
         the rows of those node types, a node seen twice raises KeyError, rows
         of different widths raise ValueError.  Blocks of lines are parsed
-        natively (``ep_parse_embeddings``).  A file whose names are the
-        decimal ids 0..n-1 of one node type gets a RangeVocab.  chunk_size is
-        accepted for API parity."""
-        from .graph import RangeVocab
+        natively (``ep_parse_embeddings``) and their names interned into a
+        NativeVocab (``ep_vocab_intern_tokens``); a file whose names are the
+        decimal ids 0..n-1 of one node type gets a RangeVocab instead.
+        chunk_size is accepted for API parity."""
+        from .graph import NativeVocab, RangeVocab
 
         types = None if filter_type is None else ({filter_type} if isinstance(filter_type, str) else set(filter_type))
-        tables, blocks, dims = [], [], None
+        tables, dims = [], None
+        run_type, total = None, 0     # while every kept row so far is (run_type, str(its index))
+        v = None                      # a NativeVocab once that stops
         for buf in _line_blocks(path, skip_rows or 0):
             vals, tok = _native.parse_embeddings(buf, dims)
             if not len(vals):
@@ -218,40 +221,32 @@ class NodeEmbeddings:
             dims = vals.shape[1]
             raw = np.frombuffer(buf, np.uint8)
             one = _one_type(raw, tok)
-            if one is not None:
-                if types is not None and one not in types:
-                    continue
-                first = _decimal_run(raw, tok)
-                if first is not None:
-                    tables.append(vals)
-                    blocks.append((one, first, len(vals)))
-                    continue
-            names = [(buf[a:b].decode(), buf[c:d].decode()) for a, b, c, d in tok.tolist()]
             if types is not None:
-                keep = np.array([t in types for t, _ in names], bool)
-                vals = vals[keep]
-                names = [x for x, k in zip(names, keep) if k]
-            tables.append(vals)
-            blocks.append(names)
-        t = np.concatenate(tables) if tables else np.zeros((0, dims or 0), np.float32)
-        total = len(t)
-        # one node type whose names run 0, 1, ..., total - 1 in order: a RangeVocab
-        if blocks and all(isinstance(b, tuple) for b in blocks) and len({b[0] for b in blocks}) == 1:
-            expect = 0
-            for _, first, cnt in blocks:
-                if first != expect:
-                    break
-                expect += cnt
+                if one is not None:
+                    if one not in types:
+                        continue
+                else:
+                    keep = np.array([buf[a:b].decode() in types for a, b in tok[:, :2].tolist()], bool)
+                    vals, tok = vals[keep], tok[keep]
+                    if not len(vals):
+                        continue
+            if v is None and one is not None and (run_type is None or one == run_type) and \
+                    _decimal_run(raw, tok) == total:
+                run_type = one
             else:
-                return NodeEmbeddings(RangeVocab(total, blocks[0][0]), t, distance or Distance.Cosine)
-        v = Vocab()
-        i = 0
-        for b in blocks:
-            seq = ((b[0], str(x)) for x in range(b[1], b[1] + b[2])) if isinstance(b, tuple) else b
-            for nt, nn in seq:
-                if v.get_or_insert(nt, nn) < i:
-                    raise KeyError(f"found duplicate node at {i}!")
-                i += 1
+                if v is None:
+                    v = NativeVocab()
+                    for i in range(total):
+                        v.get_or_insert(run_type, str(i))
+                ids = v._v.intern_tokens(buf, tok)
+                bad = np.nonzero(ids != np.arange(total, total + len(ids)))[0]
+                if len(bad):
+                    raise KeyError(f"found duplicate node at {total + int(bad[0])}!")
+            tables.append(vals)
+            total += len(vals)
+        t = np.concatenate(tables) if tables else np.zeros((0, dims or 0), np.float32)
+        if v is None:
+            v = RangeVocab(total, run_type) if run_type is not None else Vocab()
         return NodeEmbeddings(v, t, distance or Distance.Cosine)
 
 

@@ -105,6 +105,59 @@ class RangeVocab(Vocab):
             yield self.get_name(i)
 
 
+class NativeVocab(Vocab):
+    """A Vocab held by the native library (``ep_vocab_*``): the vocabulary
+    of graphs read by Graph.load, whose millions of names would otherwise be
+    Python objects.  Same ids and lookups as Vocab."""
+
+    def __init__(self, handle=None):
+        from . import _native
+
+        self._v = handle if handle is not None else _native.NativeVocabHandle()
+
+    def get_or_insert(self, node_type: str, name: str) -> int:
+        return self._v.intern(node_type, name)
+
+    def get_node_id(self, node_type: str, name: str) -> Optional[int]:
+        i = self._v.find(node_type, name)
+        return None if i < 0 else i
+
+    def get_name(self, idx: int) -> FQNode:
+        if not 0 <= idx < len(self):
+            raise IndexError(f"node id {idx} out of range")
+        t, n = self._v.export(idx, idx + 1)
+        return t[0], n[0]
+
+    def get_node_type(self, idx: int) -> str:
+        return self.get_name(idx)[0]
+
+    def names(self, lo: int, hi: int) -> List[FQNode]:
+        """The names of ids [lo, hi) in one native call."""
+        t, n = self._v.export(lo, hi)
+        return list(zip(t, n))
+
+    def __len__(self) -> int:
+        return len(self._v)
+
+    def __iter__(self) -> Iterator[FQNode]:
+        n = len(self)
+        for lo in range(0, n, 65536):
+            yield from self.names(lo, min(n, lo + 65536))
+
+
+def _as_native_vocab(vocab: Vocab, n: int):
+    """The vocabulary's first n names in a native handle (itself when it
+    already is one)."""
+    from . import _native
+
+    if isinstance(vocab, NativeVocab):
+        return vocab._v
+    h = _native.NativeVocabHandle()
+    for i in range(n):
+        h.intern(*vocab.get_name(i))
+    return h
+
+
 def _node_id(vocab: Vocab, node: FQNode) -> int:
     i = vocab.get_node_id(node[0], node[1])
     if i is None:
@@ -166,48 +219,65 @@ class Graph:
         return f"Graph<Nodes={self.nodes()}, Edges={self.edges()}>"
 
     def save(self, path: str, comp_level: Optional[int] = None) -> None:
-        """Writes ``from_type\\tfrom\\tto_type\\tto\\tweight`` lines with
-        transition probabilities (lib.rs:414-430)."""
-        import gzip
+        """Writes ``from_type\\tfrom\\tto_type\\tto\\tweight`` lines, the
+        weight each edge's transition probability written as Rust writes an
+        f32 (Graph::save, lib.rs:414-430), gzipped (level comp_level,
+        default 1) when the path ends with ``.gz``.  Rows are formatted
+        natively in blocks (``ep_format_edges``)."""
+        from . import _native
 
-        opener = gzip.open if path.endswith(".gz") or comp_level is not None else open
-        with opener(path, "wt") as f:
-            for v in range(self.nodes()):
-                ft, fn = self.vocab_.get_name(v)
-                s, e = int(self.rows[v]), int(self.rows[v + 1])
-                prev = 0.0
-                for j in range(s, e):
-                    tt, tn = self.vocab_.get_name(int(self.cols[j]))
-                    p = float(self.weights[j]) - prev
-                    prev = float(self.weights[j])
-                    f.write(f"{ft}\t{fn}\t{tt}\t{tn}\t{p}\n")
+        n = self.nodes()
+        h = _as_native_vocab(self.vocab_, n)
+        if path.endswith(".gz"):
+            import gzip
+            f = gzip.open(path, "wb", compresslevel=1 if comp_level is None else int(comp_level))
+        else:
+            f = open(path, "wb")
+        with f:
+            lo = 0
+            while lo < n:
+                # blocks of about 1M edges
+                hi = int(np.searchsorted(self.rows, self.rows[lo] + (1 << 20), side="right")) - 1
+                hi = min(n, max(hi, lo + 1))
+                f.write(_native.format_edges(h, self.rows, self.cols, self.weights, lo, hi))
+                lo = hi
 
     @staticmethod
     def load(path: str, edge_type: EdgeType, chunk_size: Optional[int] = None, skip_rows: Optional[int] = None,
              weighted: Optional[bool] = None, deduplicate: Optional[bool] = None) -> "Graph":
         """Reads ``from_type\\tfrom\\tto_type\\tto\\tweight`` lines, optionally
-        gzipped (io.rs:270-323).  chunk_size is accepted for API parity."""
-        import gzip
+        gzipped (GraphReader::load, io.rs:270-323): skip_rows leading lines
+        skipped, weights read unless weighted is False, both directions of
+        each line for an undirected graph, duplicate edges merged when
+        deduplicate.  Lines are parsed and names interned natively
+        (``ep_parse_edges``) into a NativeVocab; blank lines are skipped.
+        chunk_size is accepted for API parity."""
+        from . import _native
+        from .embeddings import _line_blocks
 
         weighted = True if weighted is None else weighted
-        b = GraphBuilder()
-        opener = gzip.open if path.endswith(".gz") else open
-        with opener(path, "rt") as f:
-            for i, line in enumerate(f):
-                if skip_rows and i < skip_rows:
-                    continue
-                line = line.rstrip("\n")
-                if not line:
-                    continue
-                p = line.split("\t")
-                if len(p) != 5:
-                    raise ValueError(f"Line {i + 1}: expected 5 tab-separated fields")
-                w = float(p[4]) if weighted else 1.0
-                b.add_edge((p[0], p[1]), (p[2], p[3]), w, edge_type)
-        g = b.build_graph(deduplicate=bool(deduplicate))
-        if g is None:
+        v = NativeVocab()
+        src, dst, w = [], [], []
+        for buf in _line_blocks(path, skip_rows or 0):
+            a, b, c = _native.parse_edges(v._v, buf, weighted)
+            src.append(a)
+            dst.append(b)
+            w.append(c)
+        if not src or not sum(len(x) for x in src):
             raise ValueError("graph file has no edges")
-        return g
+        src, dst, w = np.concatenate(src), np.concatenate(dst), np.concatenate(w)
+        if edge_type == EdgeType.Undirected:
+            # (f, t, w), (t, f, w) per line, as GraphReader::load pushes them
+            s2 = np.empty(2 * len(src), np.uint32)
+            d2 = np.empty(2 * len(src), np.uint32)
+            s2[0::2], s2[1::2] = src, dst
+            d2[0::2], d2[1::2] = dst, src
+            src, dst, w = s2, d2, np.repeat(w, 2)
+        n = len(v)
+        rows, cols, wr = _native.csr_from_edges(src, dst, w, bool(deduplicate))
+        if len(rows) - 1 < n:     # nodes past the largest edge endpoint id have no edges
+            rows = np.concatenate([rows, np.full(n - (len(rows) - 1), rows[-1], np.uint64)])
+        return Graph(rows, cols, _native.cdf_convert(rows, wr), v)
 
 
 class GraphBuilder:

@@ -339,9 +339,52 @@ int64_t ep_format_embeddings(uint64_t n, uint32_t dims, const float* table, cons
  * call: *dims is the expected width; fills values (rows x dims) and, when
  * tok_off is given, 4 byte offsets per row (type begin/end, name begin/end),
  * and returns the row count.  A malformed line, or one of another width,
- * makes the filling call return -(its 1-based number among the non-blank
- * lines). */
-int64_t ep_parse_embeddings(const char* buf, uint64_t len, uint32_t* dims, float* values, uint64_t* tok_off);
+ * makes the filling call return EP_ERR_INVALID_ARG with *bad_line (when
+ * given) set to its 1-based number among the non-blank lines (0 otherwise). */
+int64_t ep_parse_embeddings(const char* buf, uint64_t len, uint32_t* dims, float* values, uint64_t* tok_off,
+                            uint64_t* bad_line);
+
+/* ---- Vocabulary and graph text files (src/vocab.rs, src/io.rs) --------- */
+
+/* (node type, name) pairs -> dense ids in first-seen order (Vocab). */
+typedef struct ep_vocab ep_vocab;
+int ep_vocab_create(ep_vocab** out);
+void ep_vocab_destroy(ep_vocab* v);
+uint64_t ep_vocab_len(const ep_vocab* v);
+/* Longest type + name of the vocabulary, in bytes. */
+uint64_t ep_vocab_max_key(const ep_vocab* v);
+/* Vocab::get_or_insert: the key's id, a new one when unseen. */
+int64_t ep_vocab_intern(ep_vocab* v, const char* type, uint64_t type_len, const char* name, uint64_t name_len);
+/* Vocab::get_node_id: the key's id, or -1. */
+int64_t ep_vocab_find(const ep_vocab* v, const char* type, uint64_t type_len, const char* name, uint64_t name_len);
+/* Interns n keys of buf given by 4 byte offsets each (type begin/end, name
+ * begin/end, as ep_parse_embeddings writes them), in order; their ids to ids. */
+int ep_vocab_intern_tokens(ep_vocab* v, const char* buf, const uint64_t* tok, uint64_t n, uint32_t* ids);
+/* Bytes of the types and names of ids [lo, hi). */
+int ep_vocab_range_bytes(const ep_vocab* v, uint64_t lo, uint64_t hi, uint64_t* type_bytes, uint64_t* name_bytes);
+/* Types and names of ids [lo, hi) back to back, with hi-lo+1 offsets each. */
+int ep_vocab_export(const ep_vocab* v, uint64_t lo, uint64_t hi, char* types, uint64_t* type_off, char* names,
+                    uint64_t* name_off);
+
+/* GraphReader::load's line step (src/io.rs:270-323) over a buffer of whole
+ * lines "from_type\tfrom\tto_type\tto\tweight" (blank lines skipped):
+ * interns from, then to, of each line in order and writes the ids and the
+ * weight (1 when weighted is 0).  cap: capacity of src/dst/w in lines.
+ * Returns the number of lines, or a negative status; for a malformed line
+ * (not five fields, or a weight that is not a number) EP_ERR_INVALID_ARG
+ * with *bad_line (when given) set to its 1-based number among the non-blank
+ * lines, and nothing interned. */
+int64_t ep_parse_edges(ep_vocab* v, const char* buf, uint64_t len, int weighted, uint32_t* src, uint32_t* dst,
+                       float* w, uint64_t cap, uint64_t* bad_line);
+
+/* Graph::save (src/lib.rs:414-430) for the rows of nodes [lo, hi): one line
+ * per edge, the weight the edge's transition probability (difference of the
+ * row's CDF) written as Rust's Display writes an f32.  Names come from v
+ * (ids < n_nodes).  out must hold (2 * ep_vocab_max_key + 54) bytes per
+ * edge.  Returns the bytes written into out, or a negative status (also when
+ * out_cap is too small). */
+int64_t ep_format_edges(const ep_vocab* v, uint64_t n_nodes, const uint64_t* rows, const uint32_t* cols,
+                        const float* cdf, uint64_t lo, uint64_t hi, char* out, uint64_t out_cap);
 
 /* FeaturePropagator::propagate (src/lib.rs:1695-1770, propagate_features in
  * src/algos/feat_propagation.rs:13-93) over the graph CSR (per-row CDF
