@@ -213,3 +213,19 @@ def test_batch_grad_wide_feature_ids(oracle, n_feat):
     ctx = make_ctx(prob, loss=1, gamma=0.5, R=5)
     ids, _ = check_parity(oracle, prob, smp, ctx, prob["table"], loss=1, gamma=0.5)
     assert ids.max() >= n_feat - 40 and ids.min() < n_feat // 2
+
+
+@pytest.mark.parametrize("chunk", ["32", "48", "128"])
+@pytest.mark.parametrize("grad_mode", [0, 1])
+def test_batch_grad_chunk_boundaries(oracle, monkeypatch, chunk, grad_mode):
+    # features of at most one chunk of items are reduced whole by the warp of
+    # the chunk they start in; longer ones are split into partial sums that
+    # the fix-up kernels add: small chunks make both kinds common
+    monkeypatch.setenv("EP_REDUCE_CHUNK", chunk)
+    prob = random_problem(91, n=400, n_feat=3000, dims=64)
+    rng = np.random.default_rng(92)
+    hot = rng.random(len(prob["fids"])) < 0.4
+    prob["fids"][hot] = rng.integers(0, 12, int(hot.sum())).astype(np.uint32)
+    smp = sample_batch(93, prob, B=128, K=6, R=5)
+    ctx = make_ctx(prob, loss=1, gamma=0.5, R=5, grad_mode=grad_mode)
+    check_parity(oracle, prob, smp, ctx, prob["table"], loss=1, gamma=0.5, grad_mode=grad_mode)
