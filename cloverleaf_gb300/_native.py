@@ -166,7 +166,7 @@ SIGNATURES = {
     "ep_vocab_range_bytes": (ctypes.c_int, [_P, _U64, _U64, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     "ep_vocab_export": (ctypes.c_int, [_P, _U64, _U64, _P, _P, _P, _P]),
     "ep_parse_edges": (ctypes.c_int64, [_P, _P, _U64, ctypes.c_int, _P, _P, _P, _U64, ctypes.POINTER(_U64)]),
-    "ep_format_edges": (ctypes.c_int64, [_P, _U64, _P, _P, _P, _U64, _U64, _P, _U64]),
+    "ep_format_edges": (ctypes.c_int64, [_P, ctypes.c_char_p, _U64, _P, _P, _P, _U64, _U64, _P, _U64]),
     "epg_sbm": (ctypes.c_int, [_U64, _U32, ctypes.c_double, ctypes.c_double, _U64, _P, _P, _P, _P, _P]),
     "epg_sbm_tokens": (ctypes.c_int, [_U64, _P, _U32, _U32, _U32, _U32, ctypes.c_double, _U32, _U64, _P, _P,
                                       _P, _P, _P]),
@@ -500,17 +500,24 @@ def parse_edges(vocab: NativeVocabHandle, buf: bytes, weighted: bool):
     return src[:n], dst[:n], w[:n]
 
 
-def format_edges(vocab: NativeVocabHandle, rows, cols, cdf, lo: int, hi: int) -> bytes:
+def format_edges(vocab, rows, cols, cdf, lo: int, hi: int) -> bytes:
     """Graph::save (lib.rs:414-430) lines of the rows of nodes [lo, hi)
-    (``ep_format_edges``)."""
+    (``ep_format_edges``).  vocab: a NativeVocabHandle, or a str naming the
+    node type of a vocabulary whose names are the decimal ids."""
     rows = np.ascontiguousarray(rows, np.uint64)
     cols = np.ascontiguousarray(cols, np.uint32)
     cdf = np.ascontiguousarray(cdf, np.float32)
     n = len(rows) - 1
     ne = int(rows[hi] - rows[lo])
-    cap = ne * (2 * int(lib().ep_vocab_max_key(vocab.h)) + 54) + 1
+    if isinstance(vocab, str):
+        h, anon = None, vocab.encode()
+        longest = len(anon) + 20
+    else:
+        h, anon = vocab.h, None
+        longest = int(lib().ep_vocab_max_key(vocab.h))
+    cap = ne * (2 * longest + 54) + 1
     out = np.empty(cap, np.uint8)
-    r = int(lib().ep_format_edges(vocab.h, n, ptr(rows), ptr(cols), ptr(cdf), lo, hi, ptr(out), cap))
+    r = int(lib().ep_format_edges(h, anon, n, ptr(rows), ptr(cols), ptr(cdf), lo, hi, ptr(out), cap))
     if r < 0:
         check(r, None, "ep_format_edges")
     return out[:r].tobytes()

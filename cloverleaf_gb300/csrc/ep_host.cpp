@@ -945,9 +945,26 @@ extern "C" int64_t ep_parse_edges(ep_vocab* v, const char* buf, uint64_t len, in
     return rows;
 }
 
-extern "C" int64_t ep_format_edges(const ep_vocab* v, uint64_t n_nodes, const uint64_t* rows, const uint32_t* cols,
-                                   const float* cdf, uint64_t lo, uint64_t hi, char* out, uint64_t out_cap) {
-    if (!v || !rows || lo > hi || hi > n_nodes || v->size() < n_nodes || (hi > lo && !out)) return EP_ERR_INVALID_ARG;
+extern "C" int64_t ep_format_edges(const ep_vocab* v, const char* anon_type, uint64_t n_nodes, const uint64_t* rows,
+                                   const uint32_t* cols, const float* cdf, uint64_t lo, uint64_t hi, char* out,
+                                   uint64_t out_cap) {
+    if ((!v && !anon_type) || !rows || lo > hi || hi > n_nodes || (v && v->size() < n_nodes) || (hi > lo && !out))
+        return EP_ERR_INVALID_ARG;
+    const uint64_t anon_len = v ? 0 : strlen(anon_type);
+    // the key of node u: its vocabulary entry, or (anon_type, decimal u)
+    auto key = [&](uint64_t u, char* dec, const char*& t, uint64_t& tl, const char*& nm, uint64_t& nl) {
+        if (v) {
+            t = v->arena.data() + v->off[u];
+            tl = v->type_len[u];
+            nm = t + tl + 1;
+            nl = v->off[u + 1] - v->off[u] - tl - 1;
+        } else {
+            t = anon_type;
+            tl = anon_len;
+            nm = dec;
+            nl = (uint64_t)(std::to_chars(dec, dec + 24, u).ptr - dec);
+        }
+    };
     const int nt = (int)std::min<uint64_t>((uint64_t)omp_get_max_threads(), std::max<uint64_t>(1, (hi - lo) / 256));
     std::vector<std::string> part(nt);
     std::atomic<int> bad{0};
@@ -956,22 +973,24 @@ extern "C" int64_t ep_format_edges(const ep_vocab* v, uint64_t n_nodes, const ui
         const int t = omp_get_thread_num();
         const uint64_t a = lo + (hi - lo) * t / nt, b = lo + (hi - lo) * (t + 1) / nt;
         std::string& o = part[t];
-        char num[64];
+        char num[64], fdec[24], tdec[24];
         for (uint64_t u = a; u < b; ++u) {
-            const char* fk = v->arena.data() + v->off[u];
-            const uint64_t ftl = v->type_len[u], fnl = v->off[u + 1] - v->off[u] - ftl - 1;
+            const char *ft, *fn;
+            uint64_t ftl, fnl;
+            key(u, fdec, ft, ftl, fn, fnl);
             float prev = 0.f;
             for (uint64_t e = rows[u]; e < rows[u + 1]; ++e) {
                 const uint32_t x = cols[e];
                 if (x >= n_nodes) { bad = 1; break; }
                 const float p = cdf[e] - prev;     // CDFtoP (src/graph.rs:630-661)
                 prev = cdf[e];
-                const char* tk = v->arena.data() + v->off[x];
-                const uint64_t ttl = v->type_len[x], tnl = v->off[x + 1] - v->off[x] - ttl - 1;
-                o.append(fk, ftl); o.push_back('\t');
-                o.append(fk + ftl + 1, fnl); o.push_back('\t');
-                o.append(tk, ttl); o.push_back('\t');
-                o.append(tk + ttl + 1, tnl); o.push_back('\t');
+                const char *tt, *tn;
+                uint64_t ttl, tnl;
+                key(x, tdec, tt, ttl, tn, tnl);
+                o.append(ft, ftl); o.push_back('\t');
+                o.append(fn, fnl); o.push_back('\t');
+                o.append(tt, ttl); o.push_back('\t');
+                o.append(tn, tnl); o.push_back('\t');
                 // f32 as Rust's Display writes it: shortest round-trip digits, positional
                 char* z = std::to_chars(num, num + sizeof num, p, std::chars_format::fixed).ptr;
                 o.append(num, z - num);

@@ -147,11 +147,13 @@ class NativeVocab(Vocab):
 
 def _as_native_vocab(vocab: Vocab, n: int):
     """The vocabulary's first n names in a native handle (itself when it
-    already is one)."""
+    already is one), or the node type when every name is the decimal id."""
     from . import _native
 
     if isinstance(vocab, NativeVocab):
         return vocab._v
+    if isinstance(vocab, RangeVocab) and vocab._n >= n:
+        return vocab._type
     h = _native.NativeVocabHandle()
     for i in range(n):
         h.intern(*vocab.get_name(i))

@@ -380,11 +380,12 @@ int64_t ep_parse_edges(ep_vocab* v, const char* buf, uint64_t len, int weighted,
 /* Graph::save (src/lib.rs:414-430) for the rows of nodes [lo, hi): one line
  * per edge, the weight the edge's transition probability (difference of the
  * row's CDF) written as Rust's Display writes an f32.  Names come from v
- * (ids < n_nodes).  out must hold (2 * ep_vocab_max_key + 54) bytes per
- * edge.  Returns the bytes written into out, or a negative status (also when
- * out_cap is too small). */
-int64_t ep_format_edges(const ep_vocab* v, uint64_t n_nodes, const uint64_t* rows, const uint32_t* cols,
-                        const float* cdf, uint64_t lo, uint64_t hi, char* out, uint64_t out_cap);
+ * (ids < n_nodes), or, with v NULL, node u is (anon_type, decimal u).  out
+ * must hold (2 * longest type + name + 54) bytes per edge (the longest key
+ * of v is ep_vocab_max_key).  Returns the bytes written into out, or a
+ * negative status (also when out_cap is too small). */
+int64_t ep_format_edges(const ep_vocab* v, const char* anon_type, uint64_t n_nodes, const uint64_t* rows,
+                        const uint32_t* cols, const float* cdf, uint64_t lo, uint64_t hi, char* out, uint64_t out_cap);
 
 /* FeaturePropagator::propagate (src/lib.rs:1695-1770, propagate_features in
  * src/algos/feat_propagation.rs:13-93) over the graph CSR (per-row CDF
