@@ -27,7 +27,6 @@ from typing import Dict
 
 import numpy as np
 
-from . import _native
 from ._native import check, lib, ptr
 
 

@@ -9,7 +9,7 @@ training call.
 from __future__ import annotations
 
 import enum
-from typing import Iterable, Iterator, List, Optional, Sequence, Tuple
+from typing import Iterator, List, Optional, Tuple
 
 import numpy as np
 

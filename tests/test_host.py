@@ -1,5 +1,4 @@
 """Host-side logic and the C-ABI library, without a GPU."""
-import ctypes
 import glob
 import os
 import re
