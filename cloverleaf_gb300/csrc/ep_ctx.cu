@@ -435,7 +435,7 @@ static int ensure_bufs(ep_ctx* c, uint32_t B, uint32_t K, uint64_t items, uint32
                   c->key_alt.ensure(items * 4) && c->idx.ensure(items * 8) && c->idx_alt.ensure(items * 8) &&
                   c->hist.ensure(radix_hist_entries(items) * 4) && c->carry_head.ensure((size_t)nch * c->dpad * es) &&
                   c->carry_tail.ensure((size_t)nch * c->dpad * es) && c->carry_f.ensure((size_t)nch * 4) &&
-                  c->carry_flags.ensure((size_t)nch * 4) && c->long_list.ensure((size_t)nch * 4) &&
+                  c->carry_flags.ensure((size_t)nch * 4) && c->long_list.ensure((size_t)nch * 8) &&
                   c->n_touched.ensure(4);
         if (!ok) return c->fail(EP_ERR_OOM, "batch scratch allocation failed (B=%u K=%u items=%llu)", B, K, (unsigned long long)items);
         c->buf_B = B;

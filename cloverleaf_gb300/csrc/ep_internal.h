@@ -173,7 +173,7 @@ struct ReduceParams {
     void* carry_tail;
     uint32_t* carry_f;
     uint32_t* carry_flags;
-    uint32_t* long_list;    // owner chunks of long spans [n_chunks]
+    uint32_t* long_list;    // long spans: (owner chunk, last chunk) pairs [n_chunks][2]
 };
 
 // ---- launchers (defined in the kernel translation units) -----------------

@@ -663,7 +663,11 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
         }
         const uint32_t last = owner_last(p, c, f, M, C, lane);
         if (last - c > FIX_SHORT) {
-            if (lane == 0) p.long_list[atomicAdd(&p.st->n_long, 1u)] = c;
+            if (lane == 0) {
+                const uint32_t q = atomicAdd(&p.st->n_long, 1u);
+                p.long_list[2 * q] = c;
+                p.long_list[2 * q + 1] = last;
+            }
             continue;
         }
         A acc[VPL];
@@ -699,7 +703,8 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
     if (lane == 0 && u_cnt) atomicAdd(&p.st->unique_rows, u_cnt);
 }
 
-// k_fixup_long: one CTA of NWARP warps per queued long span.  Warp w adds
+// k_fixup_long: one CTA of NWARP warps per queued long span (owner chunk c
+// and the span's last chunk, as k_fixup found them).  Warp w adds
 // the heads of chunks c+1+w, c+1+w+NWARP, ... in increasing order; warp 0 then
 // adds the owner's tail and the NWARP warp sums in warp order: a fixed order,
 // independent of timing and of the queue order.
@@ -710,24 +715,19 @@ __global__ void __launch_bounds__(fixl_threads(VPL)) k_fixup_long(ReduceParams p
     constexpr int NWARP = fixl_threads(VPL) / 32;
     extern __shared__ __align__(16) unsigned char fixl_smem[];
     A* wsum = reinterpret_cast<A*>(fixl_smem);          // [NWARP][dpad]
-    __shared__ uint32_t s_last, s_kept;
+    __shared__ uint32_t s_kept;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const uint32_t M = p.st->n_items;
-    const uint32_t C = p.chunk;
     const uint32_t n_long = p.st->n_long;
     const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
     const AdamStep as = AdamStep::load(p.st);
     unsigned long long u_cnt = 0;
     for (uint32_t q = blockIdx.x; q < n_long; q += gridDim.x) {
-        const uint32_t c = p.long_list[q];
+        const uint32_t c = p.long_list[2 * q];
+        const uint32_t last = p.long_list[2 * q + 1];   // found by k_fixup
         const uint32_t fl = p.carry_flags[c];
         const uint32_t f = p.carry_f[c];
-        if (w == 0) {
-            const uint32_t last = owner_last(p, c, f, M, C, lane);
-            if (lane == 0) { s_last = last; s_kept = 0; }
-        }
+        if (threadIdx.x == 0) s_kept = 0;
         __syncthreads();
-        const uint32_t last = s_last;
         A acc[VPL];
 #pragma unroll
         for (int k = 0; k < VPL; ++k) acc[k] = 0;
