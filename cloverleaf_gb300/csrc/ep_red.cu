@@ -58,6 +58,15 @@ struct AdamStep {
     }
 };
 
+// Square root of Adam's second-moment estimate on the SFU (PTX sqrt.approx:
+// relative error within a few units of 2^-23); the denominator sqrt(v) + eps
+// tolerates that, as it tolerates the fast divide.
+__device__ __forceinline__ float sqrt_sfu(float x) {
+    float y;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // Adam on one row (optimizer.rs:43-81): t = pass + 1, beta1 0.9, beta2 0.999,
 // eps 1e-8; rows containing NaN are skipped (optimizer.rs:56).  adam_apply
 // takes the row's loaded moments and weights (mm, vv, ee) and stores the
@@ -102,7 +111,7 @@ __device__ __forceinline__ void adam_apply(T* __restrict__ table, float* __restr
             const float2 m2 = __ffma2_rn(B1, make_float2(mm[k], mm[k + 1]), __fmul2_rn(C1, g));
             const float2 v2 = __ffma2_rn(B2, make_float2(vv[k], vv[k + 1]), __fmul2_rn(C2, __fmul2_rn(g, g)));
             const float2 mh = __fmul2_rn(m2, R1), vh = __fmul2_rn(v2, R2);
-            const float2 den = __fadd2_rn(make_float2(sqrtf(vh.x), sqrtf(vh.y)), E);
+            const float2 den = __fadd2_rn(make_float2(sqrt_sfu(vh.x), sqrt_sfu(vh.y)), E);
             // the denominator is >= eps = 1e-8, inside __fdividef's full-accuracy range
             const float2 q = make_float2(__fdividef(mh.x, den.x), __fdividef(mh.y, den.y));
             const float2 e2 = __ffma2_rn(NL, q, make_float2(ee[k], ee[k + 1]));
@@ -118,7 +127,7 @@ __device__ __forceinline__ void adam_apply(T* __restrict__ table, float* __restr
             vv[k] = fmaf(b2, vv[k], (1.f - b2) * (gk * gk));
             const float mh = mm[k] * rb1;
             const float vh = vv[k] * rb2;
-            ee[k] = fmaf(-lr, __fdividef(mh, sqrtf(vh) + eps), ee[k]);
+            ee[k] = fmaf(-lr, __fdividef(mh, sqrt_sfu(vh) + eps), ee[k]);
         }
     }
     RowIO<float, VPL>::store_raw(m + o, lane, mm);
