@@ -210,8 +210,12 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     ep_ctx* c = new ep_ctx();
     c->cfg = *cfg;
     c->device = cfg->device;
-    if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+    // the main stream (sort, reduction: the critical path) at the highest
+    // priority, the side branch (loss, batch end) at the lowest
+    int prio_lo = 0, prio_hi = 0;
+    if (cudaSetDevice(c->device) != cudaSuccess || cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_loss, cudaEventDisableTiming) != cudaSuccess ||
@@ -845,7 +849,7 @@ static int launch_train_run(ep_ctx* c, uint32_t n) {
                 c->launches = before;
                 cudaError_t e = cudaStreamEndCapture(c->stream, &g);
                 if (e != cudaSuccess) return c->cuda_fail(e, "graph capture");
-                e = cudaGraphInstantiate(&c->gexec_run, g, 0);
+                e = cudaGraphInstantiate(&c->gexec_run, g, cudaGraphInstantiateFlagUseNodePriority);
                 cudaGraphDestroy(g);
                 if (e != cudaSuccess) { c->gexec_run = nullptr; return c->cuda_fail(e, "graph instantiate"); }
             }
@@ -873,7 +877,7 @@ static int launch_train_batch(ep_ctx* c) {
             c->launches = before;
             cudaError_t e = cudaStreamEndCapture(c->stream, &g);
             if (e != cudaSuccess) return c->cuda_fail(e, "graph capture");
-            e = cudaGraphInstantiate(&c->gexec, g, 0);
+            e = cudaGraphInstantiate(&c->gexec, g, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) { c->gexec = nullptr; return c->cuda_fail(e, "graph instantiate"); }
         }
