@@ -66,6 +66,10 @@ struct ep_ctx {
     // the sort (see issue_train_batch)
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_loss = nullptr, ev_join = nullptr;
+    // second branch: a batch's fix-ups beside the next batch's sampling
+    cudaStream_t fix = nullptr;
+    cudaEvent_t ev_red = nullptr, ev_fix = nullptr;
+    bool fix_pending = false;   // the last issued fix-ups have not been joined yet
     std::string err;
 
     // sizes
@@ -120,6 +124,9 @@ struct ep_ctx {
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_join) cudaEventDestroy(ev_join);
         if (ev_loss) cudaEventDestroy(ev_loss);
+        if (ev_red) cudaEventDestroy(ev_red);
+        if (ev_fix) cudaEventDestroy(ev_fix);
+        if (fix) cudaStreamDestroy(fix);
         if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -216,6 +223,9 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     if (cudaSetDevice(c->device) != cudaSuccess || cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess ||
         cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
         cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&c->fix, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_red, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fix, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_loss, cudaEventDisableTiming) != cudaSuccess ||
@@ -726,8 +736,12 @@ static uint32_t kernels_per_batch(const ep_ctx* c) {
 // event record after each stage (EP_N_STAGES events).  With fork (graph
 // capture), the loss kernel and k_batch_end run on the side stream beside the
 // sort (which needs only the items the gathers emitted); the reduction waits
-// for the loss, and the batch ends when both branches have.
-static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = false) {
+// for the loss.  The fix-ups run on the fix stream beside the next batch's
+// k_batch_begin, sampler and scan (which read neither the table nor what the
+// fix-ups read: those use k_reduce's copy of the item count and Adam
+// constants), and that batch's gathers wait for them; the last batch of a
+// capture (last) joins its fix-ups before it ends.
+static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = false, bool last = true) {
     BatchState* st = c->st.as<BatchState>();
     cudaStream_t s = c->stream;
     launch_batch_begin(st, c->n_train, c->Bcap, c->steps_per_pass, c->total_steps, c->warmup, c->cfg.alpha, 0,
@@ -736,6 +750,10 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = 
     launch_sample(sp, s);
     launch_scan_occ(st, c->occ.as<uint32_t>(), c->Bcap, c->items_cap, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_SAMPLE], s);
+    if (fork && c->fix_pending) {    // the previous batch's fix-ups have updated the table
+        cudaStreamWaitEvent(s, c->ev_fix, 0);
+        c->fix_pending = false;
+    }
     ForwardParams fp = forward_params(c, st, c->table.p, true, false);
     if (fork) {
         // the gathers have emitted the items: the loss, then k_batch_end, run
@@ -762,7 +780,16 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = 
     ReduceParams rp = reduce_params(c, st, plain ? OUT_DENSE : (c->fused_mode == 2 ? OUT_QUEUE : OUT_ADAM), c->table.p);
     launch_reduce(c->tt, (int)c->vpl, rp, c->items_cap, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_REDUCE], s);
-    launch_fixup(c->tt, (int)c->vpl, rp, c->items_cap, s);
+    if (fork && !plain) {
+        cudaEventRecord(c->ev_red, s);
+        cudaStreamWaitEvent(c->fix, c->ev_red, 0);
+        launch_fixup(c->tt, (int)c->vpl, rp, c->items_cap, c->fix);
+        cudaEventRecord(c->ev_fix, c->fix);
+        if (last) cudaStreamWaitEvent(s, c->ev_fix, 0);
+        else c->fix_pending = true;
+    } else {
+        launch_fixup(c->tt, (int)c->vpl, rp, c->items_cap, s);
+    }
     if (ev) cudaEventRecord(ev[EP_STAGE_FIXUP], s);
     if (plain)
         launch_adam_dense(c->tt, (int)c->vpl, st, c->table.p, c->m.as<float>(), c->v.as<float>(), c->gdense.as<float>(),
@@ -845,7 +872,7 @@ static int launch_train_run(ep_ctx* c, uint32_t n) {
                 cudaGraph_t g = nullptr;
                 CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
                 const uint64_t before = c->launches;
-                for (uint32_t i = 0; i < k; ++i) issue_train_batch(c, nullptr, true);
+                for (uint32_t i = 0; i < k; ++i) issue_train_batch(c, nullptr, true, i + 1 == k);
                 c->launches = before;
                 cudaError_t e = cudaStreamEndCapture(c->stream, &g);
                 if (e != cudaSuccess) return c->cuda_fail(e, "graph capture");

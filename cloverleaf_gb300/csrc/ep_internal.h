@@ -57,6 +57,11 @@ struct BatchState {
     double pass_err_sum;
     uint32_t pass_batches;
     uint32_t n_long;        // long-span fixups queued by k_fixup for k_fixup_long
+    // the batch's item count and Adam constants as k_reduce found them: the
+    // fix-up and dense Adam kernels read these, so that in replayed graphs
+    // the next batch's k_batch_begin and sampler may run beside them
+    uint32_t fx_items, fx_step;
+    float fx_lr, fx_bc1, fx_bc2, fx_sigma;
     unsigned long long anchors, kept, nan_anchors, items, gathered, unique_rows, sampled;
     double valid_sum;
 };

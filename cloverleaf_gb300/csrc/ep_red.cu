@@ -56,6 +56,16 @@ struct AdamStep {
         a.step = st->step_cur;
         return a;
     }
+    // the copy k_reduce made (kernels that run after it)
+    static __device__ __forceinline__ AdamStep load_fx(const BatchState* st) {
+        AdamStep a;
+        a.lr = st->fx_lr;
+        a.rb1 = 1.f / st->fx_bc1;
+        a.rb2 = 1.f / st->fx_bc2;
+        a.sigma = st->fx_sigma;
+        a.step = st->fx_step;
+        return a;
+    }
 };
 
 // Square root of Adam's second-moment estimate on the SFU (PTX sqrt.approx:
@@ -398,7 +408,16 @@ __global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREAD
     q.f = reinterpret_cast<uint32_t*>(red_queue + (size_t)(blockDim.x >> 5) * QN * q.sb) + (threadIdx.x >> 5) * QN;
     q.head = 0;
     q.n = 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) p.st->n_long = 0;   // read by k_fixup / k_fixup_long
+    if (blockIdx.x == 0 && threadIdx.x == 0) {   // read by k_fixup / k_fixup_long / k_adam_dense
+        BatchState* st = p.st;
+        st->n_long = 0;
+        st->fx_items = st->n_items;
+        st->fx_step = st->step_cur;
+        st->fx_lr = st->lr;
+        st->fx_bc1 = st->bc1;
+        st->fx_bc2 = st->bc2;
+        st->fx_sigma = st->noise_sigma;
+    }
     const unsigned lt_mask = (1u << lane) - 1u;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -657,11 +676,11 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
     const int lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t M = p.st->n_items;
+    const uint32_t M = p.st->fx_items;
     const uint32_t C = p.chunk;
     const uint32_t nchunks = (M + C - 1) / C;
     const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
-    const AdamStep as = AdamStep::load(p.st);
+    const AdamStep as = AdamStep::load_fx(p.st);
     unsigned long long u_cnt = 0;
     for (uint32_t c = gw; c < nchunks; c += nw) {
         const uint32_t fl = p.carry_flags[c];
@@ -728,7 +747,7 @@ __global__ void __launch_bounds__(fixl_threads(VPL)) k_fixup_long(ReduceParams p
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint32_t n_long = p.st->n_long;
     const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
-    const AdamStep as = AdamStep::load(p.st);
+    const AdamStep as = AdamStep::load_fx(p.st);
     unsigned long long u_cnt = 0;
     for (uint32_t q = blockIdx.x; q < n_long; q += gridDim.x) {
         const uint32_t c = p.long_list[2 * q];
@@ -802,7 +821,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_adam_dense(BatchState* st, T* t
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t n = *n_touched;
     const bool lane_on = (uint32_t)(lane * VPL) < dpad;
-    const AdamStep as = AdamStep::load(st);
+    const AdamStep as = AdamStep::load_fx(st);
     for (uint32_t r0 = 2 * gw; r0 < n; r0 += 2 * nw) {
         uint32_t f[2];
         bool on[2];
