@@ -65,7 +65,7 @@ struct ep_ctx {
     // side branch of captured batches: the loss and k_batch_end run beside
     // the sort (see issue_train_batch)
     cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_loss = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_loss = nullptr, ev_join = nullptr, ev_sorted = nullptr;
     // second branch: a batch's fix-ups beside the next batch's sampling
     cudaStream_t fix = nullptr;
     cudaEvent_t ev_red = nullptr, ev_fix = nullptr;
@@ -124,6 +124,7 @@ struct ep_ctx {
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_join) cudaEventDestroy(ev_join);
         if (ev_loss) cudaEventDestroy(ev_loss);
+        if (ev_sorted) cudaEventDestroy(ev_sorted);
         if (ev_red) cudaEventDestroy(ev_red);
         if (ev_fix) cudaEventDestroy(ev_fix);
         if (fix) cudaStreamDestroy(fix);
@@ -217,8 +218,8 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     ep_ctx* c = new ep_ctx();
     c->cfg = *cfg;
     c->device = cfg->device;
-    // the main stream (sort, reduction: the critical path) at the highest
-    // priority, the side branch (loss, batch end) at the lowest
+    // the main stream (gathers, loss, reduction: the critical path) at the
+    // highest priority, the side branch (items, sort, batch end) at the lowest
     int prio_lo = 0, prio_hi = 0;
     if (cudaSetDevice(c->device) != cudaSuccess || cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess ||
         cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
@@ -229,6 +230,7 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_loss, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_sorted, cudaEventDisableTiming) != cudaSuccess ||
         cudaMallocHost((void**)&c->h_st, sizeof(BatchState)) != cudaSuccess || reduce_kernels_setup() != cudaSuccess) {
         g_create_err = std::string("CUDA setup failed: ") + cudaGetErrorString(cudaGetLastError());
         delete c;
@@ -724,19 +726,20 @@ static void sort_and_reduce(ep_ctx* c, BatchState* st, int tt, int out_mode, voi
 }
 
 // Kernels launched per training batch.
-static uint32_t kernels_per_batch(const ep_ctx* c) {
+static uint32_t kernels_per_batch(const ep_ctx* c, bool fork) {
     const uint32_t b = bits_for(c->n_feat);
     const uint32_t radix = 3 * (b ? (b + 7) / 8 : 1);
-    return 3 /* begin, sample, scan */ + 3 /* forward: staged, direct gather; loss */ + radix +
+    return 3 /* begin, sample, scan */ + 3 /* forward: staged, direct gather; loss */ + (fork ? 1 : 0) /* emit */ + radix +
            3 /* reduce, fixup x2 */ +
            (c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_mode == 1 ? 1 : 0) + 1 /* end */;
 }
 
 // Issues one training batch on the context stream; ev (optional) receives an
 // event record after each stage (EP_N_STAGES events).  With fork (graph
-// capture), the loss kernel and k_batch_end run on the side stream beside the
-// sort (which needs only the items the gathers emitted); the reduction waits
-// for the loss.  The fix-ups run on the fix stream beside the next batch's
+// capture), the items are emitted by k_fwd_emit and sorted on the side stream
+// beside the gathers and the loss (which then skip the emission), and
+// k_batch_end follows the loss there; the reduction waits for the sorted
+// items.  The fix-ups run on the fix stream beside the next batch's
 // k_batch_begin, sampler and scan (which read neither the table nor what the
 // fix-ups read: those use k_reduce's copy of the item count and Adam
 // constants), and that batch's gathers wait for them; the last batch of a
@@ -750,31 +753,39 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = 
     launch_sample(sp, s);
     launch_scan_occ(st, c->occ.as<uint32_t>(), c->Bcap, c->items_cap, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_SAMPLE], s);
-    if (fork && c->fix_pending) {    // the previous batch's fix-ups have updated the table
-        cudaStreamWaitEvent(s, c->ev_fix, 0);
-        c->fix_pending = false;
-    }
-    ForwardParams fp = forward_params(c, st, c->table.p, true, false);
     if (fork) {
-        // the gathers have emitted the items: the loss, then k_batch_end, run
-        // on the side stream while the items are sorted
-        launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, s, FWD_GATHER);
+        // side stream: the items (k_fwd_emit) and their sort, beside the
+        // gathers and the loss on the main stream; then k_batch_end
         cudaEventRecord(c->ev_fork, s);
         cudaStreamWaitEvent(c->side, c->ev_fork, 0);
-        launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, c->side, FWD_LOSS);
-        cudaEventRecord(c->ev_loss, c->side);
+        if (c->fix_pending) {   // the previous batch's fix-ups: the table, and the sorted items they read
+            cudaStreamWaitEvent(s, c->ev_fix, 0);
+            cudaStreamWaitEvent(c->side, c->ev_fix, 0);
+            c->fix_pending = false;
+        }
+        ForwardParams fe = forward_params(c, st, c->table.p, true, false);
+        launch_forward(c->tt, (int)c->vpl, fe, c->Bcap, c->side, FWD_EMIT);
+        launch_radix_sort(st, c->item_f.as<uint32_t>(), c->key_alt.as<uint32_t>(), c->item_src.as<uint32_t>(),
+                          c->item_c.as<float>(), c->idx.as<uint2>(), c->idx_alt.as<uint2>(), c->hist.as<uint32_t>(),
+                          c->items_cap, (int)bits_for(c->n_feat), &c->sorted_keys, &c->sorted_vals, c->side);
+        cudaEventRecord(c->ev_sorted, c->side);
+        ForwardParams fp = forward_params(c, st, c->table.p, false, false);
+        launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, s);
+        cudaEventRecord(c->ev_loss, s);
+        cudaStreamWaitEvent(c->side, c->ev_loss, 0);
         launch_batch_end(st, c->loss.p, c->status.as<int32_t>(), c->nbr_cnt.as<uint32_t>(), c->Bcap, c->steps_per_pass,
                          0, 0, c->side);
         cudaEventRecord(c->ev_join, c->side);
+        cudaStreamWaitEvent(s, c->ev_sorted, 0);   // sorted items for the reduction
     } else {
+        ForwardParams fp = forward_params(c, st, c->table.p, true, false);
         launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, s);
+        if (ev) cudaEventRecord(ev[EP_STAGE_FORWARD], s);
+        launch_radix_sort(st, c->item_f.as<uint32_t>(), c->key_alt.as<uint32_t>(), c->item_src.as<uint32_t>(),
+                          c->item_c.as<float>(), c->idx.as<uint2>(), c->idx_alt.as<uint2>(), c->hist.as<uint32_t>(),
+                          c->items_cap, (int)bits_for(c->n_feat), &c->sorted_keys, &c->sorted_vals, s);
+        if (ev) cudaEventRecord(ev[EP_STAGE_SORT], s);
     }
-    if (ev) cudaEventRecord(ev[EP_STAGE_FORWARD], s);
-    launch_radix_sort(st, c->item_f.as<uint32_t>(), c->key_alt.as<uint32_t>(), c->item_src.as<uint32_t>(),
-                      c->item_c.as<float>(), c->idx.as<uint2>(), c->idx_alt.as<uint2>(), c->hist.as<uint32_t>(),
-                      c->items_cap, (int)bits_for(c->n_feat), &c->sorted_keys, &c->sorted_vals, s);
-    if (ev) cudaEventRecord(ev[EP_STAGE_SORT], s);
-    if (fork) cudaStreamWaitEvent(s, c->ev_loss, 0);    // directions and scales for the reduction
     const bool plain = c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_mode == 1;
     if (plain) cudaMemsetAsync(c->n_touched.p, 0, 4, s);
     ReduceParams rp = reduce_params(c, st, plain ? OUT_DENSE : (c->fused_mode == 2 ? OUT_QUEUE : OUT_ADAM), c->table.p);
@@ -799,7 +810,7 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = 
     if (fork) cudaStreamWaitEvent(s, c->ev_join, 0);
     else launch_batch_end(st, c->loss.p, c->status.as<int32_t>(), c->nbr_cnt.as<uint32_t>(), c->Bcap, c->steps_per_pass, 0, 0, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_END], s);
-    c->launches += kernels_per_batch(c);
+    c->launches += kernels_per_batch(c, fork);
 }
 
 static void advance_host_batch(ep_ctx* c) {
@@ -881,7 +892,7 @@ static int launch_train_run(ep_ctx* c, uint32_t n) {
                 if (e != cudaSuccess) { c->gexec_run = nullptr; return c->cuda_fail(e, "graph instantiate"); }
             }
             CK(cudaGraphLaunch(c->gexec_run, c->stream), "graph launch");
-            c->launches += (uint64_t)k * kernels_per_batch(c);
+            c->launches += (uint64_t)k * kernels_per_batch(c, true);
             for (uint32_t i = 0; i < k; ++i) advance_host_batch(c);
             n -= k;
         } else {
@@ -909,7 +920,7 @@ static int launch_train_batch(ep_ctx* c) {
             if (e != cudaSuccess) { c->gexec = nullptr; return c->cuda_fail(e, "graph instantiate"); }
         }
         CK(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
-        c->launches += kernels_per_batch(c);
+        c->launches += kernels_per_batch(c, true);
     } else {
         issue_train_batch(c);
         CK(cudaGetLastError(), "batch launch");

@@ -1072,6 +1072,43 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 8 ? 4 : 3) : 1) k_fwd_ga
     }
 }
 
+// k_fwd_emit: the gradient items of every anchor (feature id, role src,
+// count weight at the anchor's item positions), exactly as the gathers emit
+// them, without reading the table: the staged path's tables, or the direct
+// path's role walk with no lane reading rows.  In replayed graphs it runs
+// ahead of the radix sort on a second stream, so that the sort overlaps the
+// gathers, which then run with emission off.
+template <typename T, typename A, int VPL>
+__global__ void __launch_bounds__(256) k_fwd_emit(ForwardParams p) {
+    pdl_wait();
+    pdl_trigger();
+    const int lane = threadIdx.x & 31;
+    const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t n = p.st->n_anchors;
+    if (a >= n || p.st->n_items == 0) return;
+    const uint32_t R = p.R, NR = R + 2;
+    const uint32_t v = p.anchors[a];
+    uint64_t pos = p.occ_off[a];
+    const uint64_t sbase = (uint64_t)a * NR;
+    const uint32_t cnt = p.nbr_cnt[a];
+    const uint32_t salt = p.eval ? 0xffffffffu : (uint32_t)p.st->step;   // as k_sample
+    extern __shared__ __align__(16) unsigned char fwd_smem[];
+    WarpTables& W = reinterpret_cast<WarpTables*>(fwd_smem)[threadIdx.x >> 5];
+    if (stage_anchor<A>(p, W, a, v, cnt, pos, true, (uint32_t)sbase, salt, lane)) return;
+    for (uint32_t r = 0; r < NR; ++r) {
+        const uint32_t* nodes = r == 0 ? &v : (r == 1 ? p.nbr + (uint64_t)a * p.Kcap : p.neg + (uint64_t)a * R + (r - 2));
+        const float* w = r == 1 ? p.nbr_w + (uint64_t)a * p.Kcap : nullptr;
+        const uint32_t count = r == 1 ? cnt : 1u;
+        const uint32_t slot0 = r == 0 ? 0u : (r == 1 ? 1u : 1u + cnt + (r - 2));
+        A acc[VPL];
+        if (p.fd.kind == S_ALL)
+            gather_role<T, A, VPL>(p, nullptr, nodes, w, count, (uint32_t)(sbase + r), pos, true, acc, lane, false);
+        else
+            gather_role_fd<T, A, VPL>(p, nullptr, nodes, w, count, slot0, v, salt, (uint32_t)(sbase + r), pos, true, acc,
+                                      lane, false);
+    }
+}
+
 // k_fwd_loss: one warp per anchor; reads the role means and totals written by
 // k_fwd_gather, evaluates the loss (loss.rs:56-129) and overwrites each role's
 // mean with its gradient direction and its total with its gradient scale.
@@ -1570,6 +1607,10 @@ static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s, int
     if (!attr) {
         cudaFuncSetAttribute(k_fwd_gather<T, A, VPL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
+    }
+    if (part == FWD_EMIT) {
+        launch_chain(k_fwd_emit<T, A, VPL>, blocks, 32 * FWD_WARPS, smem, s, p);
+        return;
     }
     if (part != FWD_LOSS) {
         launch_chain(k_fwd_gather<T, A, VPL, true>, blocks, 32 * FWD_WARPS, smem, s, p);

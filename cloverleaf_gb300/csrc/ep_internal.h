@@ -188,8 +188,9 @@ void launch_batch_begin(BatchState* st, uint32_t n_order, uint32_t batch_cap,
 void launch_sample(const SampleParams& p, cudaStream_t s);
 void launch_scan_occ(BatchState* st, uint32_t* occ, uint32_t cap, uint64_t items_cap,
                      cudaStream_t s);
-// part: FWD_ALL, or the gathers alone (they emit the items), or the loss alone
-enum ForwardPart : int { FWD_ALL = 0, FWD_GATHER = 1, FWD_LOSS = 2 };
+// part: FWD_ALL, the gathers alone (they emit the items when ForwardParams
+// says so), the loss alone, or the item emission alone (k_fwd_emit)
+enum ForwardPart : int { FWD_ALL = 0, FWD_GATHER = 1, FWD_LOSS = 2, FWD_EMIT = 3 };
 void launch_forward(int tt, int vpl, const ForwardParams& p, uint32_t cap, cudaStream_t s, int part = FWD_ALL);
 void launch_radix_sort(BatchState* st, uint32_t* keys, uint32_t* keys_alt, const uint32_t* item_src,
                        const float* item_c, uint2* vals, uint2* vals_alt, uint32_t* hist, uint64_t cap,
