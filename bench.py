@@ -368,6 +368,41 @@ def main():
                 "per_batch": {"G": G, "U": U, "S": S, "items": items}}
     log(f"[bench] stages (ms/batch): " + ", ".join(f"{k} {v:.3f}" for k, v in stage_ms.items()))
 
+    # --- end to end through the C ABI from pinned host buffers (one pass) ---
+    e2e = None
+    if not args.no_e2e:
+        from cloverleaf_gb300 import _native
+
+        out = pinned_copy(np.zeros((w["n_feat"], d), np.float32))    # the caller's result buffer
+        # a single pass takes under a second and its wall time varies with the
+        # host (allocator state after the other legs): time E2E_PASSES whole
+        # passes, each a fresh context, and report the median
+        secs, phases = [], []
+        for _ in range(E2E_PASSES):
+            barrier(world)
+            t = [time.perf_counter()]
+            ectx = _native.Context(make_config(ep, "fused", args.loss, passes=1))
+            ectx.upload_graph(w["rows"], w["cols"], w["weights"])
+            ectx.upload_features(w["fptr"], w["fids"], w["n_feat"])
+            ectx.set_table(None)
+            t.append(time.perf_counter())
+            est = ectx.train(1)[0]
+            t.append(time.perf_counter())
+            table = ectx.get_table(w["n_feat"], d, out=out)
+            ectx.close()
+            t.append(time.perf_counter())
+            secs.append(allmax(t[-1] - t[0], world))
+            phases.append({"setup": round(t[1] - t[0], 4), "train": round(t[2] - t[1], 4),
+                           "download_close": round(t[3] - t[2], 4), "train_device_ms": round(est["ms"], 2)})
+        e_sec = float(np.median(secs))
+        h2d = sum(w[k].nbytes for k in ("rows", "cols", "weights", "fptr", "fids"))
+        nb = max(est["batches"], 1)
+        e2e = {"value": allsum(est["anchors"], world) / e_sec, "unit": UNIT, "h2d_bytes_per_step": h2d / nb,
+               "d2h_bytes_per_step": table.nbytes / nb, "steps": nb, "seconds": e_sec,
+               "passes_timed": E2E_PASSES, "seconds_each": [round(x, 4) for x in secs], "phases": phases,
+               "note": "one full pass via ep_create/upload/set_table/ep_train/ep_get_table; median of the passes"}
+        log(f"[bench] e2e: {e2e['value'] / 1e6:.2f} M nodes/s over {nb} steps ({e_sec:.2f}s)")
+
     # --- plain FP32 ---
     plain = None
     if not args.no_plain:
@@ -378,37 +413,6 @@ def main():
         plain = {"value": pv, "unit": UNIT, "ms_per_step": pms / max(pst2["batches"], 1),
                  "fused_speedup": value / pv}
         log(f"[bench] plain fp32: {pv / 1e6:.2f} M nodes/s (fused {value / pv:.2f}x)")
-
-    # --- end to end through the C ABI from pinned host buffers (one pass) ---
-    e2e = None
-    if not args.no_e2e:
-        from cloverleaf_gb300 import _native
-
-        out = pinned_copy(np.zeros((w["n_feat"], d), np.float32))    # the caller's result buffer
-        # a single pass takes under a second and its wall time varies with the
-        # host (allocator state after the other legs): time E2E_PASSES whole
-        # passes, each a fresh context, and report the median
-        secs = []
-        for _ in range(E2E_PASSES):
-            barrier(world)
-            t1 = time.perf_counter()
-            ectx = _native.Context(make_config(ep, "fused", args.loss, passes=1))
-            ectx.upload_graph(w["rows"], w["cols"], w["weights"])
-            ectx.upload_features(w["fptr"], w["fids"], w["n_feat"])
-            ectx.set_table(None)
-            est = ectx.train(1)[0]
-            table = ectx.get_table(w["n_feat"], d, out=out)
-            ectx.close()
-            t2 = time.perf_counter()
-            secs.append(allmax(t2 - t1, world))
-        e_sec = float(np.median(secs))
-        h2d = sum(w[k].nbytes for k in ("rows", "cols", "weights", "fptr", "fids"))
-        nb = max(est["batches"], 1)
-        e2e = {"value": allsum(est["anchors"], world) / e_sec, "unit": UNIT, "h2d_bytes_per_step": h2d / nb,
-               "d2h_bytes_per_step": table.nbytes / nb, "steps": nb, "seconds": e_sec,
-               "passes_timed": E2E_PASSES, "seconds_each": [round(x, 4) for x in secs],
-               "note": "one full pass via ep_create/upload/set_table/ep_train/ep_get_table; median of the passes"}
-        log(f"[bench] e2e: {e2e['value'] / 1e6:.2f} M nodes/s over {nb} steps ({e_sec:.2f}s)")
 
     # --- CPU reference restatement (rank 0) ---
     cpu = None
