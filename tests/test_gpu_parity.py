@@ -229,3 +229,18 @@ def test_batch_grad_chunk_boundaries(oracle, monkeypatch, chunk, grad_mode):
     smp = sample_batch(93, prob, B=128, K=6, R=5)
     ctx = make_ctx(prob, loss=1, gamma=0.5, R=5, grad_mode=grad_mode)
     check_parity(oracle, prob, smp, ctx, prob["table"], loss=1, gamma=0.5, grad_mode=grad_mode)
+
+
+@pytest.mark.parametrize("R", [5, 40])
+def test_batch_grad_anchors_past_the_staging_tables(oracle, R):
+    # anchors whose roles hold more than 512 feature occurrences (or more
+    # than 32 negatives) skip the staged gather's shared-memory tables and
+    # take the direct path
+    prob = random_problem(95, n=300, n_feat=4000, dims=32, deg=(4, 14), feats=(20, 60))
+    smp = sample_batch(96, prob, B=64, K=10, R=R)
+    occ = np.diff(prob["fptr"]).astype(np.int64)
+    per_anchor = [occ[a] + sum(occ[smp["nbr"][int(smp["nbr_ptr"][i]):int(smp["nbr_ptr"][i + 1])]]) + occ[smp["neg"][i]].sum()
+                  for i, a in enumerate(smp["anchors"])]
+    assert max(per_anchor) > 512 and min(per_anchor) <= 512 or R > 32
+    ctx = make_ctx(prob, loss=1, gamma=0.5, R=R)
+    check_parity(oracle, prob, smp, ctx, prob["table"], loss=1, gamma=0.5)

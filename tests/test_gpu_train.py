@@ -191,6 +191,28 @@ def test_graph_replays_match_stream_launches():
     assert {k: out[0][1][k] for k in same} == {k: out[1][1][k] for k in same}
 
 
+def test_graph_replays_match_stream_launches_with_direct_gathers():
+    # anchors too big for the staged gather's tables take the direct path,
+    # in replayed graphs with their items from k_fwd_emit's direct walk
+    from tests._cases import random_problem
+    prob = random_problem(97, n=3000, n_feat=20000, dims=64, deg=(4, 30), feats=(10, 40))
+    tables = []
+    for graphs in (1, 0):
+        cfg = _native.default_config()
+        cfg.use_graphs = graphs
+        cfg.dims, cfg.negatives, cfg.loss, cfg.gamma = 64, 10, _native.LOSS_STARSPACE, 0.5
+        cfg.batch_size, cfg.passes, cfg.valid_pct = 256, 1, 0.0
+        cfg.max_nodes_kind, cfg.max_nodes = _native.SAMPLE_FIXED, 25.0
+        ctx = _native.Context(cfg)
+        ctx.upload_graph(prob["rows"], prob["cols"], None)
+        ctx.upload_features(prob["fptr"], prob["fids"], prob["n_feat"])
+        ctx.set_table(None)
+        st = ctx.train_batches(20)
+        assert st["kept_anchors"] > 0
+        tables.append(ctx.get_table(prob["n_feat"], 64))
+    assert np.array_equal(tables[0], tables[1])
+
+
 @pytest.mark.parametrize("form", [_native.FORM_FUSED_BF16, _native.FORM_PLAIN_FP32])
 def test_autotune_picks_a_candidate_and_trains(form):
     w = datagen.workload("cl10m", scale=0.01)
