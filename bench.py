@@ -296,7 +296,8 @@ def main():
     if rank == 0:
         log(f"[bench] {args.workload}: {n_nodes} nodes, {len(w['cols'])} directed edges, "
             f"{len(w['fids'])} feature occurrences, {w['n_feat']} slots ({time.time() - t0:.1f}s)")
-    wl = (f"{args.workload}: Chung-Lu {n_nodes} nodes / {len(w['cols'])} directed edges, dims {ep['dims']}, "
+    kind = "SBM" if args.workload.startswith("sbm") else "Chung-Lu"
+    wl = (f"{args.workload}: {kind} {n_nodes} nodes / {len(w['cols'])} directed edges, dims {ep['dims']}, "
           f"max_neighbors {ep['max_nodes']}, {ep['negatives']} negatives, batch {ep['batch_size']}, {args.loss} 0.5")
     config = {"workload": wl, "nodes": n_nodes, "edges": int(len(w["cols"])), "dims": ep["dims"],
               "batch": ep["batch_size"], "max_neighbors": ep["max_nodes"], "negatives": ep["negatives"],
