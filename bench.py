@@ -52,6 +52,30 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else platform)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                vendor = next((l.split(":", 1)[1].strip() for l in out.splitlines()
+                               if l.split(":")[0].strip() == "Vendor ID"), "")
+                name = line.split(":", 1)[1].strip()
+                return f"{vendor} {name}".strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -313,7 +337,7 @@ def main():
                 "steps": nb, "warmup": args.warmup, "ms_per_step": 1e3 * st.seconds / max(st.batches, 1),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic", "config": dict(config, table_dtype="f32"),
-                "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": "port",
                                  "sample": f"{st.batches} batches of {ep['batch_size']} anchors "
                                            f"({st.anchors} anchors) of the {args.workload} workload"},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -419,7 +443,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         cv, cst, cores, nb = cpu_reference(w, args.loss, args.cpu_seconds)
-        cpu = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
+        cpu = {"value": cv, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": "port",
                "sample": f"{cst.batches} batches of {ep['batch_size']} anchors ({cst.anchors} anchors) of "
                          f"{args.workload}, {cst.seconds:.1f}s"}
         log(f"[bench] cpu reference: {cv / 1e3:.1f} k nodes/s on {cores} threads")
@@ -437,7 +461,8 @@ def main():
                 f"{100 * knn['frac']:.1f}% of {pk_bf16:.0f}")
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / max(st["batches"], 1), "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+                "scaling": "weak", "vs_baseline": None, "dtype": "bf16 table storage, f32 accumulation and Adam moments",
+                "data": "synthetic", "config": config,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(st["launches"]),
                 "clocks": clocks, "plain_fp32": plain,
                 "speedup_vs_cpu": (value / cpu["value"]) if cpu else None,

@@ -1,7 +1,12 @@
-"""Builds the native library ``cloverleaf_gb300/_lib/libep_gb300.so`` in-tree.
+"""Builds the native libraries in-tree, under ``cloverleaf_gb300/_lib/``.
 
-CUDA translation units are compiled for sm_103a only (one ``-gencode``) in
-parallel with the host C++ unit; a source/flag hash stamp skips rebuilds.
+* ``libep_gb300.so``: the trainer.  CUDA translation units are compiled for
+  sm_103a only (one ``-gencode``) in parallel with the host C++ unit.
+* ``libep_datagen.so``: the synthetic workload generators (host C++ only),
+  kept apart so that the benchmark's CPU reference arm can generate its
+  workload without loading the trainer.
+
+A source/flag hash stamp per library skips rebuilds.
 """
 from __future__ import annotations
 
@@ -18,6 +23,8 @@ INCLUDE = os.path.join(ROOT, "include")
 OBJ_DIR = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libep_gb300.so")
+DATAGEN_PATH = os.path.join(LIB_DIR, "libep_datagen.so")
+DATAGEN_SOURCES = ("ep_datagen.cpp",)
 
 CU_SOURCES = ("ep_fwd.cu", "ep_sort.cu", "ep_red.cu", "ep_ctx.cu", "ep_knn.cu")
 CPP_SOURCES = ("ep_host.cpp",)
@@ -35,9 +42,9 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build cloverleaf_gb300")
 
 
-def _stamp() -> str:
+def _stamp(sources) -> str:
     h = hashlib.sha256()
-    for name in CU_SOURCES + CPP_SOURCES + HEADERS:
+    for name in sources:
         with open(os.path.join(CSRC, name), "rb") as f:
             h.update(name.encode() + f.read())
     for name in sorted(os.listdir(INCLUDE)):
@@ -48,14 +55,45 @@ def _stamp() -> str:
     return h.hexdigest()
 
 
+def _fresh(path: str, stamp: str) -> bool:
+    stamp_path = path + ".stamp"
+    if not (os.path.exists(path) and os.path.exists(stamp_path)):
+        return False
+    with open(stamp_path) as f:
+        return f.read().strip() == stamp
+
+
+def _run(cmd, verbose: bool):
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r
+
+
+def build_datagen(verbose: bool = False, force: bool = False) -> str:
+    """Compiles and links libep_datagen.so if its sources changed; returns its path."""
+    stamp = _stamp(DATAGEN_SOURCES)
+    if not force and _fresh(DATAGEN_PATH, stamp):
+        return DATAGEN_PATH
+    os.makedirs(LIB_DIR, exist_ok=True)
+    tmp = DATAGEN_PATH + ".tmp"
+    _run(["g++"] + CXX_FLAGS + ["-shared", "-o", tmp] + [os.path.join(CSRC, s) for s in DATAGEN_SOURCES] + ["-lgomp"],
+         verbose)
+    os.replace(tmp, DATAGEN_PATH)
+    with open(DATAGEN_PATH + ".stamp", "w") as f:
+        f.write(stamp)
+    return DATAGEN_PATH
+
+
 def build(verbose: bool = False, force: bool = False) -> str:
-    """Compiles and links the library if sources changed; returns its path."""
-    stamp_path = os.path.join(LIB_DIR, ".stamp")
-    stamp = _stamp()
-    if not force and os.path.exists(LIB_PATH) and os.path.exists(stamp_path):
-        with open(stamp_path) as f:
-            if f.read().strip() == stamp:
-                return LIB_PATH
+    """Compiles and links the trainer library (and the generator library) if
+    sources changed; returns the trainer library's path."""
+    build_datagen(verbose, force)
+    stamp = _stamp(CU_SOURCES + CPP_SOURCES + HEADERS)
+    if not force and _fresh(LIB_PATH, stamp):
+        return LIB_PATH
     os.makedirs(OBJ_DIR, exist_ok=True)
     os.makedirs(LIB_DIR, exist_ok=True)
     nvcc = _nvcc()
@@ -67,19 +105,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
         obj = os.path.join(OBJ_DIR, src.replace(".cpp", ".o"))
         jobs.append((["g++"] + CXX_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj], obj))
 
-    def run(cmd):
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
-        return r
-
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
-        list(ex.map(lambda j: run(j[0]), jobs))
+        list(ex.map(lambda j: _run(j[0], verbose), jobs))
     tmp = LIB_PATH + ".tmp"
-    run([nvcc, "-shared", ARCH, "-o", tmp] + [j[1] for j in jobs] + ["-Xcompiler", "-fopenmp", "-lgomp"])
+    _run([nvcc, "-shared", ARCH, "-o", tmp] + [j[1] for j in jobs] + ["-Xcompiler", "-fopenmp", "-lgomp"], verbose)
     os.replace(tmp, LIB_PATH)
-    with open(stamp_path, "w") as f:
+    with open(LIB_PATH + ".stamp", "w") as f:
         f.write(stamp)
     return LIB_PATH

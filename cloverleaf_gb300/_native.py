@@ -1,4 +1,4 @@
-"""ctypes binding of ``include/ep_gb300.h`` and ``include/ep_datagen.h``.
+"""ctypes binding of ``include/ep_gb300.h``.
 
 The shared library is the product path: every training call goes through it,
 and loading fails loudly (``NativeError``) when it cannot be built or loaded;
@@ -148,6 +148,8 @@ SIGNATURES = {
     "ep_knn_last_kernel_ms": (ctypes.c_float, []),
     "ep_ag_forward": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), ctypes.c_int, _P, _P, _P]),
     "ep_ag_backward": (ctypes.c_int, [_P, _P, _P, _P]),
+    "ep_get_split": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(_U32), ctypes.POINTER(_U32)]),
+    "ep_sample_validation": (ctypes.c_int, [_P, _U32, _U32, _U32, _P, _P, _P, _P, _P]),
     "ep_synchronize": (ctypes.c_int, [_P]),
     "ep_last_error": (ctypes.c_char_p, [_P]),
     "ep_destroy": (None, [_P]),
@@ -167,13 +169,6 @@ SIGNATURES = {
     "ep_vocab_export": (ctypes.c_int, [_P, _U64, _U64, _P, _P, _P, _P]),
     "ep_parse_edges": (ctypes.c_int64, [_P, _P, _U64, ctypes.c_int, _P, _P, _P, _U64, ctypes.POINTER(_U64)]),
     "ep_format_edges": (ctypes.c_int64, [_P, ctypes.c_char_p, _U64, _P, _P, _P, _U64, _U64, _P, _U64]),
-    "epg_sbm": (ctypes.c_int, [_U64, _U32, ctypes.c_double, ctypes.c_double, _U64, _P, _P, _P, _P, _P]),
-    "epg_sbm_tokens": (ctypes.c_int, [_U64, _P, _U32, _U32, _U32, _U32, ctypes.c_double, _U32, _U64, _P, _P,
-                                      _P, _P, _P]),
-    "epg_chung_lu": (ctypes.c_int, [_U64, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, _F32,
-                                    _F32, _U64, _P, _P, _P, _P]),
-    "epg_zipf_features": (ctypes.c_int, [_U64, ctypes.c_double, _U32, _U32, ctypes.c_double, _U32, _U64, _P,
-                                         _P, _P]),
 }
 
 
@@ -266,6 +261,30 @@ class Context:
         check(lib().ep_sample(self._h, ptr(anchors), n, int(step), int(stride), ptr(cnt), ptr(nbr), ptr(w), ptr(neg)),
               self._h, "ep_sample")
         return cnt, nbr, w, neg
+
+    def split(self):
+        """(train ids, validation ids in validation order) of this context's
+        seeded train/validation split."""
+        nt, nv = ctypes.c_uint32(), ctypes.c_uint32()
+        check(lib().ep_get_split(self._h, None, None, ctypes.byref(nt), ctypes.byref(nv)), self._h, "ep_get_split")
+        tr = np.zeros(max(nt.value, 1), np.uint32)
+        va = np.zeros(max(nv.value, 1), np.uint32)
+        check(lib().ep_get_split(self._h, ptr(tr), ptr(va), ctypes.byref(nt), ctypes.byref(nv)), self._h,
+              "ep_get_split")
+        return tr[: nt.value], va[: nv.value]
+
+    def sample_validation(self, first, n, stride):
+        """The validation pass's samples at validation positions [first,
+        first + n): (anchors, nbr_cnt, nbr[n, stride], nbr_w[n, stride],
+        neg[n, R])."""
+        anchors = np.zeros(n, np.uint32)
+        cnt = np.zeros(n, np.uint32)
+        nbr = np.zeros((n, stride), np.uint32)
+        w = np.zeros((n, stride), np.float32)
+        neg = np.zeros((n, self.cfg.negatives), np.uint32)
+        check(lib().ep_sample_validation(self._h, int(first), int(n), int(stride), ptr(anchors), ptr(cnt), ptr(nbr),
+                                         ptr(w), ptr(neg)), self._h, "ep_sample_validation")
+        return anchors, cnt, nbr, w, neg
 
     def tuning(self):
         """(tuned, chunk, fused_mode, graph_batches) of this context."""

@@ -870,6 +870,34 @@ static int autotune(ep_ctx* c, uint32_t& n) {
     return EP_OK;
 }
 
+// Captures and instantiates `batches` consecutive training batches as one
+// graph (nothing runs: the capture only records the launches).
+static int capture_batches(ep_ctx* c, uint32_t batches, cudaGraphExec_t* out) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+    const uint64_t before = c->launches;
+    for (uint32_t i = 0; i < batches; ++i) issue_train_batch(c, nullptr, true, i + 1 == batches);
+    c->launches = before;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return c->cuda_fail(e, "graph capture");
+    e = cudaGraphInstantiate(out, g, cudaGraphInstantiateFlagUseNodePriority);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { *out = nullptr; return c->cuda_fail(e, "graph instantiate"); }
+    return EP_OK;
+}
+
+// Builds, ahead of a run of n batches, the graphs that run will replay, so
+// that the one-time capture and instantiation stay outside its timing.
+static int prepare_graphs(ep_ctx* c, uint32_t n) {
+    if (!(c->cfg.use_graphs && c->cfg.form == EP_FORM_FUSED_BF16) || n == 0) return EP_OK;
+    if (c->cfg.autotune && !c->tuned) return EP_OK;   // the tuner rebuilds them per candidate
+    const uint32_t k = c->graph_batches;
+    int rc = EP_OK;
+    if (k > 1 && n >= k && !c->gexec_run) rc = capture_batches(c, k, &c->gexec_run);
+    if (!rc && (k == 1 || n % k) && !c->gexec) rc = capture_batches(c, 1, &c->gexec);
+    return rc;
+}
+
 static int launch_train_run(ep_ctx* c, uint32_t n) {
     if (c->cfg.autotune && !c->tuned) {
         int rc = autotune(c, n);
@@ -880,16 +908,8 @@ static int launch_train_run(ep_ctx* c, uint32_t n) {
     while (n) {
         if (use_graph && k > 1 && n >= k) {
             if (!c->gexec_run) {
-                cudaGraph_t g = nullptr;
-                CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
-                const uint64_t before = c->launches;
-                for (uint32_t i = 0; i < k; ++i) issue_train_batch(c, nullptr, true, i + 1 == k);
-                c->launches = before;
-                cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-                if (e != cudaSuccess) return c->cuda_fail(e, "graph capture");
-                e = cudaGraphInstantiate(&c->gexec_run, g, cudaGraphInstantiateFlagUseNodePriority);
-                cudaGraphDestroy(g);
-                if (e != cudaSuccess) { c->gexec_run = nullptr; return c->cuda_fail(e, "graph instantiate"); }
+                int rc = capture_batches(c, k, &c->gexec_run);
+                if (rc) return rc;
             }
             CK(cudaGraphLaunch(c->gexec_run, c->stream), "graph launch");
             c->launches += (uint64_t)k * kernels_per_batch(c, true);
@@ -908,16 +928,8 @@ static int launch_train_batch(ep_ctx* c) {
     const bool use_graph = c->cfg.use_graphs && c->cfg.form == EP_FORM_FUSED_BF16;
     if (use_graph) {
         if (!c->gexec) {
-            cudaGraph_t g = nullptr;
-            CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
-            const uint64_t before = c->launches;
-            issue_train_batch(c, nullptr, true);
-            c->launches = before;
-            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-            if (e != cudaSuccess) return c->cuda_fail(e, "graph capture");
-            e = cudaGraphInstantiate(&c->gexec, g, cudaGraphInstantiateFlagUseNodePriority);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) { c->gexec = nullptr; return c->cuda_fail(e, "graph instantiate"); }
+            int rc = capture_batches(c, 1, &c->gexec);
+            if (rc) return rc;
         }
         CK(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
         c->launches += kernels_per_batch(c, true);
@@ -1004,6 +1016,7 @@ extern "C" int ep_train(ep_ctx* c, ep_pass_stats* stats, uint32_t stats_len) {
     cudaEventCreate(&e1);
     for (uint32_t pass = 1; pass <= c->cfg.passes; ++pass) {
         if ((rc = clear_accumulators(c))) break;
+        if ((rc = prepare_graphs(c, c->steps_per_pass))) break;
         cudaEventRecord(e0, c->stream);
         if ((rc = launch_train_run(c, c->steps_per_pass))) break;
         cudaEventRecord(e1, c->stream);
@@ -1026,6 +1039,7 @@ extern "C" int ep_train_batches(ep_ctx* c, uint32_t n_batches, ep_pass_stats* st
     if (rc) return rc;
     if (!c->state_ok && (rc = reset_state(c))) return rc;
     if ((rc = clear_accumulators(c))) return rc;
+    if ((rc = prepare_graphs(c, n_batches))) return rc;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1190,6 +1204,67 @@ extern "C" int ep_sample(ep_ctx* c, const uint32_t* anchors, uint32_t n, uint32_
     CK(cudaMemcpyAsync(neg, c->neg.p, (size_t)n * c->R * 4, cudaMemcpyDeviceToHost, s), "read samples");
     CK(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s), "read state");
     CK(cudaStreamSynchronize(s), "sample");
+    if (h.error) return c->fail(EP_ERR_DEVICE, "device error flags 0x%x", h.error);
+    for (uint32_t a = 0; a < n; ++a) {
+        nbr_cnt[a] = hc[a];
+        for (uint32_t k = 0; k < hc[a]; ++k) {
+            nbr[(size_t)a * stride + k] = hn[(size_t)a * c->Kcap + k];
+            nbr_w[(size_t)a * stride + k] = hw[(size_t)a * c->Kcap + k];
+        }
+    }
+    return EP_OK;
+}
+
+extern "C" int ep_get_split(ep_ctx* c, uint32_t* train_ids, uint32_t* valid_ids, uint32_t* n_train,
+                            uint32_t* n_valid) {
+    if (!c) return EP_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    int rc = prepare_train(c);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream), "split");
+    if (train_ids)
+        CK(cudaMemcpy(train_ids, c->train_ids.p, (size_t)c->n_train * 4, cudaMemcpyDeviceToHost), "read split");
+    if (valid_ids && c->n_valid)
+        CK(cudaMemcpy(valid_ids, c->valid_ids.p, (size_t)c->n_valid * 4, cudaMemcpyDeviceToHost), "read split");
+    if (n_train) *n_train = c->n_train;
+    if (n_valid) *n_valid = c->n_valid;
+    return EP_OK;
+}
+
+extern "C" int ep_sample_validation(ep_ctx* c, uint32_t first, uint32_t n, uint32_t stride, uint32_t* anchors,
+                                    uint32_t* nbr_cnt, uint32_t* nbr, float* nbr_w, uint32_t* neg) {
+    if (!c) return EP_ERR_INVALID_ARG;
+    if (n && (!anchors || !nbr_cnt || !nbr || !nbr_w || !neg)) return c->fail(EP_ERR_INVALID_ARG, "null array");
+    cudaSetDevice(c->device);
+    int rc = prepare_train(c);
+    if (rc) return rc;
+    if (n > c->Bcap) return c->fail(EP_ERR_INVALID_ARG, "%u anchors exceed the batch size %u", n, c->Bcap);
+    if ((uint64_t)first + n > c->n_valid)
+        return c->fail(EP_ERR_INVALID_ARG, "positions [%u, %llu) beyond the %u validation ids", first,
+                       (unsigned long long)first + n, c->n_valid);
+    if (stride < c->Kcap)
+        return c->fail(EP_ERR_INVALID_ARG, "neighbour stride %u below the %u slots an anchor can fill", stride, c->Kcap);
+    if (!n) return EP_OK;
+    BatchState h{};
+    h.pass = 1;
+    h.step = 1;
+    h.b0 = first;
+    h.n_anchors = n;
+    if (!c->st_inj.ensure(sizeof(BatchState))) return c->fail(EP_ERR_OOM, "state allocation failed");
+    BatchState* st = c->st_inj.as<BatchState>();
+    cudaStream_t s = c->stream;
+    CK(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s), "validation state");
+    launch_sample(sample_params(c, st, true, 0), s);   // the validation pass's sampler, as run_validation launches it
+    CK(cudaGetLastError(), "sample launch");
+    std::vector<uint32_t> hn((size_t)n * c->Kcap), hc(n);
+    std::vector<float> hw((size_t)n * c->Kcap);
+    CK(cudaMemcpyAsync(anchors, c->anchors.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s), "read samples");
+    CK(cudaMemcpyAsync(hc.data(), c->nbr_cnt.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s), "read samples");
+    CK(cudaMemcpyAsync(hn.data(), c->nbr.p, hn.size() * 4, cudaMemcpyDeviceToHost, s), "read samples");
+    CK(cudaMemcpyAsync(hw.data(), c->nbr_w.p, hw.size() * 4, cudaMemcpyDeviceToHost, s), "read samples");
+    CK(cudaMemcpyAsync(neg, c->neg.p, (size_t)n * c->R * 4, cudaMemcpyDeviceToHost, s), "read samples");
+    CK(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s), "read state");
+    CK(cudaStreamSynchronize(s), "validation samples");
     if (h.error) return c->fail(EP_ERR_DEVICE, "device error flags 0x%x", h.error);
     for (uint32_t a = 0; a < n; ++a) {
         nbr_cnt[a] = hc[a];

@@ -23,11 +23,47 @@ Named workloads restate the five benchmark configurations as generators:
 from __future__ import annotations
 
 import ctypes
+import threading
 from typing import Dict
 
 import numpy as np
 
-from ._native import check, lib, ptr
+from . import _build
+
+_P, _U32, _U64, _F32, _D = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_float, ctypes.c_double
+# include/ep_datagen.h, exported by libep_datagen.so (host code only: loading
+# it loads none of the trainer's library)
+SIGNATURES = {
+    "epg_sbm": (ctypes.c_int, [_U64, _U32, _D, _D, _U64, _P, _P, _P, _P, _P]),
+    "epg_sbm_tokens": (ctypes.c_int, [_U64, _P, _U32, _U32, _U32, _U32, _D, _U32, _U64, _P, _P, _P, _P, _P]),
+    "epg_chung_lu": (ctypes.c_int, [_U64, _D, _D, _D, ctypes.c_int, _F32, _F32, _U64, _P, _P, _P, _P]),
+    "epg_zipf_features": (ctypes.c_int, [_U64, _D, _U32, _U32, _D, _U32, _U64, _P, _P, _P]),
+}
+_lib = None
+_lock = threading.Lock()
+
+
+def lib():
+    """Loads (building first when needed) libep_datagen.so."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            handle = ctypes.CDLL(_build.build_datagen())
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(handle, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = handle
+        return _lib
+
+
+def ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else ctypes.c_void_p(0)
+
+
+def check(rc: int, _ctx, what: str):
+    if rc != 0:
+        raise ValueError(f"{what}: invalid argument (status {rc})")
 
 
 def sbm(n: int, blocks: int, k_in: float, k_out: float, seed: int):

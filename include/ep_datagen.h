@@ -10,7 +10,11 @@
  *
  * Two-call protocol: call with NULL output pointers to get the sizes, then
  * again with buffers of those sizes (the second call regenerates the same
- * data from the seed).
+ * data from the seed).  Every function returns 0 on success and -1 for an
+ * invalid argument.
+ *
+ * Exported by libep_datagen.so, a host-only library separate from the
+ * trainer's libep_gb300.so.
  */
 #ifndef EP_DATAGEN_H
 #define EP_DATAGEN_H

@@ -206,6 +206,21 @@ int ep_batch_grad(ep_ctx* ctx, const ep_batch_samples* samples, ep_sparse_grad* 
 int ep_sample(ep_ctx* ctx, const uint32_t* anchors, uint32_t n, uint32_t step, uint32_t stride,
               uint32_t* nbr_cnt, uint32_t* nbr, float* nbr_w, uint32_t* neg);
 
+/* Inspection hook: the train/validation split of mod.rs:119-125 (a seeded
+ * permutation; the last floor(n * valid_pct) ids are validation ids).  Writes
+ * the n_train training ids (the pool uniform negatives are drawn from,
+ * node_sampler.rs:83-107) and the n_valid validation ids in their validation
+ * order; either pointer may be NULL.  *n_train / *n_valid receive the counts. */
+int ep_get_split(ep_ctx* ctx, uint32_t* train_ids, uint32_t* valid_ids, uint32_t* n_train, uint32_t* n_valid);
+
+/* Inspection hook: the samples the validation pass (mod.rs:267-283) draws for
+ * its anchors at positions [first, first + n) of the validation order
+ * (n <= batch_size): the anchors, their neighbours (stride as ep_sample) and
+ * their negatives, drawn from the validation ids.  Validation sampling uses
+ * one fixed random stream, so these are the samples of every pass. */
+int ep_sample_validation(ep_ctx* ctx, uint32_t first, uint32_t n, uint32_t stride, uint32_t* anchors,
+                         uint32_t* nbr_cnt, uint32_t* nbr, float* nbr_w, uint32_t* neg);
+
 /* Parity hook: one full optimizer step for explicit samples with learning
  * rate lr and Adam time pass+1 (optimizer.rs:43-81). */
 int ep_batch_step(ep_ctx* ctx, const ep_batch_samples* samples, float lr, uint32_t pass);

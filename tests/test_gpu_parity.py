@@ -73,6 +73,32 @@ def test_batch_grad_plain_fp32(oracle, loss, dims):
     check_parity(oracle, prob, smp, ctx, prob["table"], loss=loss, gamma=gamma)
 
 
+@pytest.mark.parametrize("name", ["margin", "starspace"])
+@pytest.mark.parametrize("form", [0, 1])
+def test_default_losses_known_answers(name, form):
+    # the hand-derived Margin and StarSpace answers of tests/test_oracle.py,
+    # straight through the C ABI (the tables are exact in BF16)
+    from tests.test_oracle import MARGIN_KAT, STARSPACE_KAT
+
+    k = MARGIN_KAT if name == "margin" else STARSPACE_KAT
+    n = len(k["fptr"]) - 1
+    prob = dict(rows=np.arange(n + 1, dtype=np.uint64), cols=((np.arange(n) + 1) % n).astype(np.uint32),
+                fptr=np.array(k["fptr"], np.uint64), fids=np.array(k["fids"], np.uint32),
+                table=np.array(k["table"], np.float32), n=n, n_feat=len(k["table"]), dims=2)
+    smp = dict(anchors=np.array([0], np.uint32), nbr_ptr=np.array(k["nbr_ptr"], np.uint32),
+               nbr=np.array(k["nbr"], np.uint32), nbr_w=np.array(k["nbr_w"], np.float32),
+               neg=np.array(k["neg"], np.uint32))
+    R = smp["neg"].shape[1]
+    ctx = make_ctx(prob, loss=0 if name == "margin" else 1, gamma=k["gamma"], R=R, form=form)
+    gl, gst, ids, rows = gpu_batch(ctx, prob, smp)
+    assert gst.tolist() == [0]
+    assert abs(gl[0] - k["loss"]) < 1e-6
+    assert sorted(ids.tolist()) == sorted(k["grad"])
+    tol = 1e-6 if form == 0 else TOL_GRAD_BF16       # fused form: BF16 directions
+    for f, row in zip(ids.tolist(), rows):
+        np.testing.assert_allclose(row, k["grad"][f], atol=tol, rtol=0)
+
+
 @pytest.mark.parametrize("grad_mode", [0, 1])
 @pytest.mark.parametrize("weighting", [0, 1, 2])
 def test_batch_grad_modes_and_weighting(oracle, grad_mode, weighting):

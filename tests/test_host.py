@@ -25,9 +25,26 @@ def declared_functions():
 def test_library_exports_every_declared_symbol(native):
     names = declared_functions()
     assert {"ep_create", "ep_train", "ep_batch_grad", "ep_destroy", "epg_chung_lu"} <= names
+    gen = datagen.lib()
     for n in names:
-        assert hasattr(native, n), n
-    assert names == set(_native.SIGNATURES), names ^ set(_native.SIGNATURES)
+        assert hasattr(gen if n.startswith("epg_") else native, n), n
+    bound = set(_native.SIGNATURES) | set(datagen.SIGNATURES)
+    assert names == bound, names ^ bound
+
+
+def test_generators_live_apart_from_the_trainer():
+    # the generator library exports no trainer entry point, and loading it
+    # does not load the trainer library
+    import subprocess
+    import sys
+
+    code = ("import sys; sys.path.insert(0, %r); from cloverleaf_gb300 import datagen; "
+            "w = datagen.workload('sbm1k'); "
+            "maps = open('/proc/self/maps').read(); "
+            "assert 'libep_datagen.so' in maps and 'libep_gb300.so' not in maps, 'trainer loaded'; "
+            "assert not hasattr(datagen.lib(), 'ep_create')" % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
 
 
 def test_config_defaults_match_reference(native):

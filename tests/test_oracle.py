@@ -97,6 +97,65 @@ def test_l2norm_known_answer(oracle):
     np.testing.assert_allclose(grad[2], gu, atol=1e-7)
 
 
+# Hand-derived known answers for the two default losses (loss.rs:59-105),
+# every role's gradient written out from the formulas, not from any
+# restatement.  Count weights (model.rs:257-278): an occurrence of a feature
+# of node u in a role counts w_u + 1 (w_u = 1 for the anchor and the
+# negatives, the given neighbour weight in the reconstruction); a feature's
+# leaf gradient is its count share of the role's gradient (model.rs:448-463).
+#
+# Margin, gamma = 1, R = 3:
+#   h = mean(E0, E1) = mean((0,2), (2,0)) = (1,1);   t = E2 = (4,5)
+#   u1 = E3 = (4,1): |t-u1| = 4, l1 = 1 + 5 - 4 = 2  (kept)
+#   u2 = E4 = (1,5): |t-u2| = 3, l2 = 1 + 5 - 3 = 3  (kept)
+#   u3 = E5 = (4,15): |t-u3| = 10, l3 = -4           (dropped: no gradient)
+#   L = (2 + 3) / 2 = 2.5
+#   dL/dh  = -(t-h)/|t-h| = (-0.6, -0.8)              -> E0, E1 get half each
+#   dL/dt  = [2 (t-h)/5 - (t-u1)/4 - (t-u2)/3] / 2 = (0.1, 0.3)
+#   dL/du1 = (t-u1)/4 / 2 = (0, 0.5);  dL/du2 = (t-u2)/3 / 2 = (0.5, 0)
+MARGIN_KAT = dict(
+    table=[[0, 2], [2, 0], [4, 5], [4, 1], [1, 5], [4, 15]],
+    fptr=[0, 2, 3, 4, 5, 6], fids=[0, 1, 2, 3, 4, 5],
+    nbr_ptr=[0, 1], nbr=[1], nbr_w=[1.0], neg=[[2, 3, 4]], gamma=1.0, loss=2.5,
+    grad={0: [-0.3, -0.4], 1: [-0.3, -0.4], 2: [0.1, 0.3], 3: [0.0, 0.5], 4: [0.5, 0.0]})
+# StarSpace, gamma = 0.5, R = 2, with x^ = x/|x| and d x^ = (I - x^ x^T)/|x|:
+#   h = E0 = (2,0): h^ = (1,0)
+#   t = (2 E1 + 4 E2) / 6 with neighbour weights 1 and 3 (counts 2 and 4),
+#       E1 = (-2,1), E2 = (1,1): t = (0,1) = t^
+#   u1 = E3 = (3,4): u1^ = (.6,.8); l1 = .5 - (t^.h^ - h^.u1^) = 1.1  (kept)
+#   u2 = E4 = (-1,0): l2 = .5 - (0 - (-1)) = -.5 -> max(0, .) = 0     (dropped)
+#   L = 1.1
+#   dL/dh  = (I - h^h^T)/2 (u1^ - t^) = (0, -0.1)
+#   dL/dt  = (I - t^t^T)/1 (-h^)      = (-1, 0)  -> E1 gets 2/6, E2 4/6
+#   dL/du1 = (I - u1^u1^T)/5 h^       = (0.128, -0.096)
+STARSPACE_KAT = dict(
+    table=[[2, 0], [-2, 1], [1, 1], [3, 4], [-1, 0]],
+    fptr=[0, 1, 2, 3, 4, 5], fids=[0, 1, 2, 3, 4],
+    nbr_ptr=[0, 2], nbr=[1, 2], nbr_w=[1.0, 3.0], neg=[[3, 4]], gamma=0.5, loss=1.1,
+    grad={0: [0.0, -0.1], 1: [-1 / 3, 0.0], 2: [-2 / 3, 0.0], 3: [0.128, -0.096]})
+
+
+def kat_args(k):
+    n = len(k["fptr"]) - 1
+    rows = np.arange(n + 1, dtype=np.uint64)          # one (unused) edge per node
+    return (np.array(k["fptr"], np.uint64), np.array(k["fids"], np.uint32), len(k["table"]),
+            np.array(k["table"], np.float32), rows, [0], k["nbr_ptr"], k["nbr"], k["nbr_w"], k["neg"])
+
+
+@pytest.mark.parametrize("name", ["margin", "starspace"])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_default_losses_known_answers(oracle, name, prec):
+    k = MARGIN_KAT if name == "margin" else STARSPACE_KAT
+    lid = oracle.LOSS_MARGIN if name == "margin" else oracle.LOSS_STARSPACE
+    loss, st, g, t = oracle.batch(*kat_args(k), oracle.loss_cfg(loss=lid, gamma=k["gamma"]), prec)
+    tol = 1e-12 if prec == "f64" else 1e-6
+    assert st.tolist() == [0]
+    assert abs(loss[0] - k["loss"]) < tol * 10
+    assert sorted(np.nonzero(t)[0].tolist()) == sorted(k["grad"])
+    for f, row in k["grad"].items():
+        np.testing.assert_allclose(g[f], row, atol=tol * 10, rtol=0)
+
+
 @pytest.mark.parametrize("loss", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("grad_mode", [0, 1])
 @pytest.mark.parametrize("weighting", [0, 1, 2])
