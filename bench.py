@@ -89,6 +89,10 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-knn", action="store_true")
+    p.add_argument("--no-recall", action="store_true", help="skip the held-out-edge recall@10 leg")
+    p.add_argument("--recall-queries", type=int, default=20000)
+    p.add_argument("--no-large", action="store_true", help="skip the 50M-node leg")
+    p.add_argument("--large-steps", type=int, default=100)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--profile-steps", type=int, default=100)
     return p.parse_args()
@@ -287,6 +291,79 @@ def gpu_leg(w, form, loss, steps, warmup, world, sampler_device=None):
     return ctx, st, wall, clocks
 
 
+def recall_leg(w, loss, queries):
+    """Held-out-edge recall@10 (scripts/evaluate.py:29-61) after the
+    workload's passes, for the fused and plain GPU forms and the CPU
+    restatement, all trained on the same graph with 1% of its undirected
+    edges held out (seeded)."""
+    from cloverleaf_gb300 import _native, evaluate
+    from oracle import ep_oracle as O
+
+    ep = w["ep"]
+    t0 = time.time()
+    rows, cols, wts, test = evaluate.holdout_edges(w["rows"], w["cols"], w["weights"], 0.01, seed=5,
+                                                   max_test=queries)
+    out = {"k": 10, "test_edges": int(len(test)), "held_out_fraction": 0.01, "passes": ep["passes"],
+           "metric": "share of held-out edges (u, v) with v among the 10 nearest node embeddings of u (cosine); "
+                     "auc: share with cos(u, v) > cos(u, random node)"}
+    for form in ("fused", "plain"):
+        ctx = _native.Context(make_config(ep, form, loss, passes=ep["passes"]))
+        ctx.upload_graph(rows, cols, None)
+        ctx.upload_features(w["fptr"], w["fids"], w["n_feat"])
+        ctx.set_table(None)
+        ctx.train(ep["passes"])
+        table = ctx.get_table(w["n_feat"], ep["dims"])
+        ctx.close()
+        out[form] = evaluate.heldout_recall(w["fptr"], w["fids"], table, test)
+        out[form]["table_checksum"] = float(table.sum(dtype=np.float64))
+        del table
+        log(f"[bench] recall {form}: {out[form]}")
+    t1 = time.time()
+    table, st = O.train(rows, cols, wts, w["fptr"], w["fids"], w["n_feat"], dims=ep["dims"], alpha=ep["alpha"],
+                        loss=O.LOSS_STARSPACE if loss == "starspace" else O.LOSS_MARGIN, gamma=ep["gamma"],
+                        negatives=ep["negatives"], batch_size=ep["batch_size"], passes=ep["passes"],
+                        max_nodes=(O.SAMPLE_FIXED, float(ep["max_nodes"])), threads=0)
+    out["cpu_train_seconds"] = round(time.time() - t1, 1)
+    out["cpu"] = evaluate.heldout_recall(w["fptr"], w["fids"], table, test)
+    del table
+    for form in ("fused", "plain"):
+        out[f"{form}_minus_cpu"] = out[form]["recall"] - out["cpu"]["recall"]
+    out["seconds"] = round(time.time() - t0, 1)
+    log(f"[bench] recall cpu: {out['cpu']} ({out['cpu_train_seconds']} s of CPU training)")
+    return out
+
+
+def large_leg(loss, steps, warmup, world):
+    """The 50M-node / ~1B-edge Chung-Lu workload (dims 256, max_neighbors 32,
+    16 negatives, batch 32768): fused and plain nodes/s over `steps` batches,
+    and the fused form's per-stage profile."""
+    from cloverleaf_gb300 import datagen
+
+    t0 = time.time()
+    w = datagen.workload("cl50m")
+    gen_s = time.time() - t0
+    ep = w["ep"]
+    n = len(w["rows"]) - 1
+    out = {"workload": f"cl50m: Chung-Lu {n} nodes / {len(w['cols'])} directed edges, dims {ep['dims']}, "
+                       f"max_neighbors {ep['max_nodes']}, {ep['negatives']} negatives, batch {ep['batch_size']}",
+           "generate_seconds": round(gen_s, 1), "steps": steps, "warmup": warmup}
+    log(f"[bench] cl50m generated in {gen_s:.1f}s: {n} nodes, {len(w['cols'])} edges")
+    for form in ("fused", "plain"):
+        ctx, st, wall, _ = gpu_leg(w, form, loss, steps, warmup, world)
+        ms = allmax(st["ms"], world)
+        rec = {"value": allsum(st["anchors"], world) / (ms / 1e3), "unit": UNIT,
+               "ms_per_step": ms / max(st["batches"], 1),
+               "step_gbs": st["alg_bytes"] / (st["ms"] / 1e3) / 1e9}
+        if form == "fused":
+            stage_ms, pst = ctx.profile_batches(20)
+            rec["stage_ms"] = stage_ms
+        ctx.close()
+        out[form] = rec
+        log(f"[bench] cl50m {form}: {rec['value'] / 1e6:.2f} M nodes/s ({rec['ms_per_step']:.3f} ms/batch)")
+    out["fused_speedup"] = out["fused"]["value"] / out["plain"]["value"]
+    return out
+
+
 def cpu_reference(w, loss, seconds, threads=0, max_batches=None):
     """The oracle's restatement of the reference loop on host cores, on a
     bounded number of batches sized to take about `seconds`."""
@@ -459,6 +536,14 @@ def main():
             knn = knn_leg(pk_bf16)
             log(f"[bench] knn: {knn['tflops']:.1f} TFLOP/s ({knn['kernel_ms']:.2f} ms) = "
                 f"{100 * knn['frac']:.1f}% of {pk_bf16:.0f}")
+        recall = None
+        if not args.no_recall:
+            recall = recall_leg(w, args.loss, args.recall_queries)
+        large = None
+        if not args.no_large and args.workload == "cl10m" and args.scale == 1.0 and world == 1:
+            del w
+            _PINNED.clear()
+            large = large_leg(args.loss, args.large_steps, max(args.warmup, 3), world)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / max(st["batches"], 1), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "bf16 table storage, f32 accumulation and Adam moments",
@@ -466,6 +551,7 @@ def main():
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(st["launches"]),
                 "clocks": clocks, "plain_fp32": plain,
                 "speedup_vs_cpu": (value / cpu["value"]) if cpu else None,
+                "recall_at_10": recall, "largest": large,
                 "eval_knn": knn}
         print(json.dumps(line), flush=True)
     return 0

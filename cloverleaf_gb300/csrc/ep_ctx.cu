@@ -97,6 +97,11 @@ struct ep_ctx {
     // closes; 1 = gradient rows, then a separate Adam kernel; 2 = queued in
     // the reducing warp's shared memory and updated four rows at a time
     int fused_mode = 2;
+    // mode 3's warp-specialised reduction: reducing warps, Adam warps and
+    // ring slots per CTA
+    uint32_t ring_pw = 12, ring_cw = 4, ring_slots = 32;
+    // persistent staged gather: CTAs of its grid (0 = one warp per anchor)
+    uint32_t gather_ctas = 0;
     bool tuned = false;         // autotuner has chosen chunk / fused_mode
     bool prepared = false;
     cudaGraphExec_t gexec = nullptr;
@@ -248,8 +253,12 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     }
     if (const char* fm = getenv("EP_FUSED_MODE")) {   // (tuning)
         const int v = atoi(fm);
-        if (v >= 0 && v <= 2) c->fused_mode = v;
+        if (v >= 0 && v <= 3) c->fused_mode = v;
     }
+    if (const char* e = getenv("EP_RING_PW")) { const long v = atol(e); if (v >= 1 && v <= 15) c->ring_pw = (uint32_t)v; }
+    if (const char* e = getenv("EP_RING_CW")) { const long v = atol(e); if (v >= 1 && v <= 15) c->ring_cw = (uint32_t)v; }
+    if (const char* e = getenv("EP_RING_SLOTS")) { const long v = atol(e); if (v >= 2 && v <= 64) c->ring_slots = (uint32_t)v; }
+    if (const char* e = getenv("EP_GATHER_CTAS")) { const long v = atol(e); if (v >= 0 && v <= 65536) c->gather_ctas = (uint32_t)v; }
     if (const char* ch = getenv("EP_REDUCE_CHUNK")) {   // reducer items per warp (tuning)
         const long v = atol(ch);
         if (v >= 32 && v <= (1l << 20)) c->chunk = (uint32_t)v;
@@ -682,6 +691,7 @@ static ForwardParams forward_params(ep_ctx* c, BatchState* st, const void* table
     fp.item_src = c->item_src.as<uint32_t>();
     fp.item_c = c->item_c.as<float>();
     fp.deferred = c->deferred.as<uint8_t>();
+    fp.gather_ctas = c->gather_ctas;
     return fp;
 }
 
@@ -711,6 +721,9 @@ static ReduceParams reduce_params(ep_ctx* c, BatchState* st, int out_mode, void*
     rp.carry_f = c->carry_f.as<uint32_t>();
     rp.carry_flags = c->carry_flags.as<uint32_t>();
     rp.long_list = c->long_list.as<uint32_t>();
+    rp.ring_pw = c->ring_pw;
+    rp.ring_cw = c->ring_cw;
+    rp.ring_slots = c->ring_slots;
     return rp;
 }
 
@@ -723,6 +736,15 @@ static void sort_and_reduce(ep_ctx* c, BatchState* st, int tt, int out_mode, voi
     ReduceParams rp = reduce_params(c, st, out_mode, table);
     launch_reduce(tt, (int)c->vpl, rp, c->items_cap, s);
     launch_fixup(tt, (int)c->vpl, rp, c->items_cap, s);
+}
+
+// The FUSED form's reduction output for its Adam placement (fused_mode 0,
+// 2, 3); the ring falls back to the per-warp queue for row shapes it cannot
+// bulk-copy.
+static int fused_out_mode(const ep_ctx* c) {
+    if (c->fused_mode == 3)
+        return ring_supported(c->tt, c->dpad, c->ring_pw, c->ring_cw, c->ring_slots) ? OUT_RING : OUT_QUEUE;
+    return c->fused_mode == 2 ? OUT_QUEUE : OUT_ADAM;
 }
 
 // Kernels launched per training batch.
@@ -788,7 +810,7 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = 
     }
     const bool plain = c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_mode == 1;
     if (plain) cudaMemsetAsync(c->n_touched.p, 0, 4, s);
-    ReduceParams rp = reduce_params(c, st, plain ? OUT_DENSE : (c->fused_mode == 2 ? OUT_QUEUE : OUT_ADAM), c->table.p);
+    ReduceParams rp = reduce_params(c, st, plain ? OUT_DENSE : fused_out_mode(c), c->table.p);
     launch_reduce(c->tt, (int)c->vpl, rp, c->items_cap, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_REDUCE], s);
     if (fork && !plain) {

@@ -326,14 +326,21 @@ extern "C" int epg_chung_lu(uint64_t n, double exponent, double mean_degree, dou
         }
         std::vector<double> wexp(n);
         for (uint64_t i = 0; i < n; ++i) wexp[i] = std::min(std::max(hi * base[i], 1.0), max_degree);
-        // random node labels, so that high-degree nodes are spread over the id range
+        // random node labels, so that high-degree nodes are spread over the id
+        // range (bipartite: over each side's range, users [0, n/2) and items
+        // [n/2, n))
+        const uint64_t half = n / 2;
         std::vector<uint32_t> label(n);
         std::iota(label.begin(), label.end(), 0u);
         {
             Rng r(seed, 4, 0);
-            for (uint64_t i = n; i > 1; --i) std::swap(label[i - 1], label[r.below(i)]);
+            if (bipartite) {
+                for (uint64_t i = half; i > 1; --i) std::swap(label[i - 1], label[r.below(i)]);
+                for (uint64_t i = n - half; i > 1; --i) std::swap(label[half + i - 1], label[half + r.below(i)]);
+            } else {
+                for (uint64_t i = n; i > 1; --i) std::swap(label[i - 1], label[r.below(i)]);
+            }
         }
-        const uint64_t half = n / 2;
         std::vector<double> w_all(wexp);
         std::vector<double> wa, wb;
         if (bipartite) {

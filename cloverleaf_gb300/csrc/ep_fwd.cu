@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "ep_device.cuh"
@@ -177,6 +178,7 @@ __global__ void k_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, ui
     st->bc1 = 1.f - powf(0.9f, t);
     st->bc2 = 1.f - powf(0.999f, t);
     st->n_items = 0;
+    st->fwd_next = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1022,13 +1024,51 @@ __device__ __forceinline__ bool warp_all_finite(const A (&x)[VPL]) {
 // p.deferred and skipped.  STAGED = false: the direct path, run afterwards for
 // the flagged anchors only (every anchor when p.deferred is null).  Both
 // produce identical items, means and totals.
+// The staged gather of anchor a (phases A-C) by one warp; anchors that do not
+// fit the tables are flagged for the direct path.
+template <typename T, typename A, int VPL>
+__device__ __forceinline__ void gather_staged(const ForwardParams& p, WarpTables& W, uint32_t a, int lane) {
+    const uint32_t NR = p.R + 2;
+    const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
+    const uint32_t v = p.anchors[a];
+    const bool emit = p.emit && p.st->n_items > 0;
+    const uint64_t pos = emit ? p.occ_off[a] : 0;
+    const uint64_t sbase = (uint64_t)a * NR;
+    const uint32_t cnt = p.nbr_cnt[a];
+    const uint32_t salt = p.eval ? 0xffffffffu : (uint32_t)p.st->step;   // as k_sample
+    const bool staged = stage_anchor<A>(p, W, a, v, cnt, pos, emit, (uint32_t)sbase, salt, lane);
+    if (lane == 0) p.deferred[a] = staged ? 0 : 1;
+    if (staged) roles_from_table<T, A, VPL>(p, (const T*)p.table, W, NR, sbase, lane, lane_on);
+    __syncwarp();
+}
+
 template <typename T, typename A, int VPL, bool STAGED>
 __global__ void __launch_bounds__(256, STAGED ? (VPL <= 8 ? 4 : 3) : 1) k_fwd_gather(ForwardParams p) {
     pdl_wait();
     pdl_trigger();
     const int lane = threadIdx.x & 31;
-    const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t n = p.st->n_anchors;
+    if constexpr (STAGED) {
+        extern __shared__ __align__(16) unsigned char fwd_smem[];
+        WarpTables& W = reinterpret_cast<WarpTables*>(fwd_smem)[threadIdx.x >> 5];
+        // persistent (gather_ctas > 0): each warp takes the next anchor from
+        // the batch's work queue until none is left, so a warp that drew
+        // short anchors takes more of them and no wave waits on the slowest;
+        // otherwise one anchor per warp
+        const bool queue = p.gather_ctas != 0;
+        uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        for (;;) {
+            if (queue) {
+                if (lane == 0) a = atomicAdd(&p.st->fwd_next, 1u);
+                a = __shfl_sync(FULL, a, 0);
+            }
+            if (a >= n) break;
+            gather_staged<T, A, VPL>(p, W, a, lane);
+            if (!queue) break;
+        }
+        return;
+    }
+    const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (a >= n) return;
     const uint32_t R = p.R, NR = R + 2, dpad = p.dpad;
     const bool lane_on = (uint32_t)(lane * VPL) < dpad;
@@ -1039,14 +1079,7 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 8 ? 4 : 3) : 1) k_fwd_ga
     const uint64_t sbase = (uint64_t)a * NR;
     const uint32_t cnt = p.nbr_cnt[a];
     const uint32_t salt = p.eval ? 0xffffffffu : (uint32_t)p.st->step;   // as k_sample
-    if constexpr (STAGED) {
-        extern __shared__ __align__(16) unsigned char fwd_smem[];
-        WarpTables& W = reinterpret_cast<WarpTables*>(fwd_smem)[threadIdx.x >> 5];
-        const bool staged = stage_anchor<A>(p, W, a, v, cnt, pos, emit, (uint32_t)sbase, salt, lane);
-        if (lane == 0) p.deferred[a] = staged ? 0 : 1;
-        if (!staged) return;
-        roles_from_table<T, A, VPL>(p, table, W, NR, sbase, lane, lane_on);
-    } else {
+    {
         if (p.deferred && !p.deferred[a]) return;
         A* dir = (A*)p.dir;
         A* scale = (A*)p.scale;
@@ -1613,7 +1646,8 @@ static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s, int
         return;
     }
     if (part != FWD_LOSS) {
-        launch_chain(k_fwd_gather<T, A, VPL, true>, blocks, 32 * FWD_WARPS, smem, s, p);
+        const uint32_t gblocks = p.gather_ctas ? std::min(p.gather_ctas, blocks) : blocks;
+        launch_chain(k_fwd_gather<T, A, VPL, true>, gblocks, 32 * FWD_WARPS, smem, s, p);
         launch_chain(k_fwd_gather<T, A, VPL, false>, blocks, 32 * FWD_WARPS, 0, s, p);
     }
     if (part != FWD_GATHER) launch_chain(k_fwd_loss<T, A, VPL>, (cap + 3) / 4, 128, 0, s, p);

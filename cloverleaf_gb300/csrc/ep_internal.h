@@ -28,13 +28,17 @@ enum : uint32_t {
     ERR_ITEMS_OVERFLOW = 1u << 0,   // a batch emitted more items than allocated
     ERR_FEISTEL = 1u << 1,          // permutation cycle walk exceeded its cap
     ERR_NBR_OVERFLOW = 1u << 2,     // sampled neighbours exceeded capacity
+    ERR_RING_TIMEOUT = 1u << 3,     // a wait of the reducer's row ring gave up (bounded polls)
 };
 
 // OUT_ADAM: each finished feature row is updated in place by the warp that
 // finished it.  OUT_DENSE: rows go to a dense gradient buffer plus a touched
 // list (a separate Adam kernel, or the caller, consumes them).  OUT_QUEUE:
 // rows are queued in the warp's shared memory and updated four at a time.
-enum OutMode : int { OUT_ADAM = 0, OUT_DENSE = 1, OUT_QUEUE = 2 };
+// OUT_RING: warp-specialised CTAs; reducing warps push finished rows into a
+// CTA-wide shared-memory ring whose slots bulk-copy (TMA) the row's Adam
+// state, and Adam warps pop and update them.
+enum OutMode : int { OUT_ADAM = 0, OUT_DENSE = 1, OUT_QUEUE = 2, OUT_RING = 3 };
 enum TableType : int { TT_F32 = 0, TT_BF16 = 1, TT_F64 = 2 };
 
 struct BatchState {
@@ -49,6 +53,7 @@ struct BatchState {
     float bc1, bc2;         // 1 - beta^t with t = pass + 1 (optimizer.rs:50)
     uint32_t error;         // ERR_* bits, sticky
     uint32_t n_items;       // items emitted by this batch
+    uint32_t fwd_next;      // work queue of the persistent gather: next anchor to take (k_batch_begin zeroes it)
     float noise_sigma;      // gradient-noise scale of this step (0 = off)
     // per-batch outputs of k_batch_end
     float batch_err;        // sum(loss kept) / n_anchors (0 when none kept)
@@ -141,6 +146,8 @@ struct ForwardParams {
     int emit;                 // 0: forward only (validation)
     uint64_t items_cap;
     uint8_t* deferred;        // [n_anchors]: 1 = anchor left to the direct path
+    uint32_t gather_ctas;     // staged gather: 0 = a warp per anchor; else this many persistent CTAs
+                              // whose warps take anchors from BatchState::fwd_next
     // outputs
     void* dir;              // A[n_anchors * NR * dpad]: role means, then (D == A) directions
     void* dir16;            // BF16 tables: directions as BF16 (D = bf16)
@@ -179,6 +186,8 @@ struct ReduceParams {
     uint32_t* carry_f;
     uint32_t* carry_flags;
     uint32_t* long_list;    // long spans: (owner chunk, last chunk) pairs [n_chunks][2]
+    // OUT_RING shape: reducing warps, Adam warps and ring slots per CTA
+    uint32_t ring_pw, ring_cw, ring_slots;
 };
 
 // ---- launchers (defined in the kernel translation units) -----------------
@@ -218,5 +227,10 @@ void launch_pack_rows(size_t es, const void* dense, const uint32_t* rows, const 
 size_t radix_hist_entries(uint64_t cap);
 uint32_t reduce_chunks(uint64_t cap, uint32_t chunk);
 cudaError_t reduce_kernels_setup();
+// Whether OUT_RING serves this row shape (whole rows of m, v and the table are
+// 16-byte multiples, and the ring's shared memory fits), and the ring's
+// shared memory per CTA.
+bool ring_supported(int tt, uint32_t dpad, uint32_t pw, uint32_t cw, uint32_t slots);
+size_t ring_smem_bytes(int tt, uint32_t dpad, uint32_t slots);
 
 }  // namespace ep

@@ -324,11 +324,188 @@ __device__ __forceinline__ void queue_flush(const ReduceParams& p, WarpQueue& q,
     while (q.n) queue_pop<T, VPL>(p, q, lane, lane_on, as);
 }
 
+// ---------------------------------------------------------------------------
+// OUT_RING: warp-specialised reduction.  A CTA runs pw reducing warps and cw
+// Adam warps around a ring of `slots` shared-memory slots, each holding one
+// finished feature row: its gradient (stored by the reducing warp), and the
+// feature's m, v and table rows, which one lane of the reducing warp fetches
+// with three bulk copies (cp.async.bulk, the TMA's linear form) counted on
+// the slot's `full` mbarrier.  Adam warp k takes tickets k, k + cw, ... in
+// order, waits for the slot's copies, updates the row in place in HBM and
+// releases the slot on its `empty` mbarrier.  The reducing warps thus never
+// wait for HBM (only for a free slot), and the Adam warps never wait for the
+// reduction's L2 traffic: the two latency chains overlap.
+//
+// Tickets are handed out by a shared-memory counter, so the slot of ticket t
+// is t % slots in round t / slots.  A reducing warp takes its ticket without
+// waiting, so it may hold a round of its slot several rounds ahead of the
+// consumer; it therefore waits on the slot's count of consumed rounds (a
+// word that only grows), not on an mbarrier parity, which only tells the
+// current phase from the one before.  Adam warp k owns the slots congruent
+// to k modulo cw (slots is a multiple of cw) and takes their rounds in
+// order, so when it waits on a slot's `full` parity for round r it has itself
+// seen round r - 1 complete, and no producer can have completed round r + 1
+// (that producer waits for round r to be consumed): the parity is exact.
+// No wait can close a cycle: the smallest unfilled ticket's producer only
+// waits for earlier rounds of its slot, and every ticket before it is filled.
+// Every poll loop is bounded (RING_WAIT_LIMIT); a loop that gives up sets
+// ERR_RING_TIMEOUT and the CTA's abort word, so all warps stop waiting, and
+// the CTA waits (bounded) for the bulk copies it issued before it exits.  The
+// host reports the error bit.
+// ---------------------------------------------------------------------------
+constexpr uint32_t RING_WAIT_LIMIT = 1u << 21;   // polls of about 32 ns each
+constexpr uint32_t RING_MAX_WARPS = 16;
+
+struct RingHdr {
+    unsigned long long full[64];              // mbarrier per slot: the row and its bulk copies landed
+    uint32_t consumed[64];                    // rounds of the slot the Adam warp has finished
+    uint32_t f[64];                           // feature of the row in the slot
+    uint32_t issued[64];                      // rounds whose copies were issued, per slot
+    uint32_t tail;                            // next ticket
+    uint32_t done;                            // reducing warps finished
+    uint32_t abort;
+};
+constexpr uint32_t RING_MAX_SLOTS = 64;
+
+template <typename T>
+__host__ __device__ constexpr size_t ring_slot_bytes(uint32_t dpad) {
+    return (size_t)dpad * (3 * sizeof(float) + sizeof(T));   // g, m, v (FP32) + table row; 16-byte multiples
+}
+__host__ __device__ constexpr size_t ring_hdr_bytes() { return (sizeof(RingHdr) + 127) & ~(size_t)127; }
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint32_t ring_test(unsigned long long* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done;
+}
+
+__device__ __forceinline__ void ring_set_abort(const ReduceParams& p, RingHdr* rh) {
+    atomicExch(&rh->abort, 1u);
+    atomicOr(&p.st->error, ERR_RING_TIMEOUT);
+}
+
+// Waits (whole warp, lane 0 polling) until the Adam warp has finished
+// `rounds` rounds of the slot.  Returns false when the CTA aborts or the wait
+// gives up (then the abort is raised).
+__device__ __forceinline__ bool ring_wait_consumed(const ReduceParams& p, RingHdr* rh, uint32_t slot,
+                                                   uint32_t rounds) {
+    uint32_t ok = 0;
+    if ((threadIdx.x & 31) == 0) {
+        volatile RingHdr* vh = rh;
+        for (uint32_t it = 0; it < RING_WAIT_LIMIT; ++it) {
+            if (vh->consumed[slot] >= rounds) { ok = 1; break; }
+            if (vh->abort) break;
+            __nanosleep(32);
+        }
+        if (!ok && !vh->abort) ring_set_abort(p, rh);
+        __threadfence_block();   // the consumer's reads of the slot happen before our writes
+    }
+    return __shfl_sync(FULL, ok, 0) != 0;
+}
+
+// Reducing warp: queue a finished NaN-free row for the Adam warps.
+template <typename T, typename A, int VPL>
+__device__ __forceinline__ void ring_push(const ReduceParams& p, RingHdr* rh, unsigned char* slots, uint32_t f,
+                                          const A (&acc)[VPL], int lane, bool lane_on) {
+    const uint32_t S = p.ring_slots, dpad = p.dpad;
+    uint32_t t = 0;
+    if (lane == 0) t = atomicAdd(&rh->tail, 1u);
+    t = __shfl_sync(FULL, t, 0);
+    const uint32_t slot = t % S, round = t / S;
+    if (round > 0 && !ring_wait_consumed(p, rh, slot, round)) return;   // row dropped: aborting
+    unsigned char* base = slots + (size_t)slot * ring_slot_bytes<T>(dpad);
+    float* g = reinterpret_cast<float*>(base);
+    if (lane_on) store_row<float, VPL, A>(g, lane, acc);
+    __threadfence_block();
+    __syncwarp();
+    if (lane == 0) {
+        rh->f[slot] = f;
+        rh->issued[slot] = round + 1;
+        const uint32_t mb = dpad * 4u, tb = dpad * (uint32_t)sizeof(T);
+        const uint32_t bar = smem_addr(&rh->full[slot]);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(2 * mb + tb) : "memory");
+        const char* src[3] = {reinterpret_cast<const char*>(p.m) + (uint64_t)f * mb,
+                              reinterpret_cast<const char*>(p.v) + (uint64_t)f * mb,
+                              reinterpret_cast<const char*>(p.table) + (uint64_t)f * tb};
+        const uint32_t dst[3] = {smem_addr(base + mb), smem_addr(base + 2 * mb), smem_addr(base + 3 * mb)};
+        const uint32_t len[3] = {mb, mb, tb};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         ::"r"(dst[i]), "l"(src[i]), "r"(len[i]), "r"(bar)
+                         : "memory");
+    }
+    __syncwarp();
+}
+
+// Adam warp `k` of the CTA: tickets k, k + cw, ... (its slots' rounds in
+// order) until every reducing warp has finished and no later ticket was taken.
+template <typename T, int VPL>
+__device__ void ring_consume(const ReduceParams& p, RingHdr* rh, unsigned char* slots, uint32_t k, int lane,
+                             bool lane_on, const AdamStep& as) {
+    const uint32_t S = p.ring_slots, dpad = p.dpad;
+    for (uint32_t h = k;; h += p.ring_cw) {
+        const uint32_t slot = h % S, round = h / S;
+        uint32_t mine = 0, got = 0;
+        for (uint32_t it = 0;; ++it) {
+            if (!mine) mine = ring_test(&rh->full[slot], round & 1u);
+            if (__all_sync(FULL, mine)) { got = 1; break; }
+            uint32_t stop = 0;
+            if (lane == 0) {
+                // `done` before `tail`: a reducing warp takes its last ticket
+                // before it counts itself done, so once all are done the
+                // ticket count read after the fence is final
+                volatile RingHdr* vh = rh;
+                const uint32_t d = vh->done;
+                __threadfence_block();
+                const uint32_t tl = vh->tail;
+                stop = vh->abort || (d == p.ring_pw && tl <= h);
+            }
+            if (__shfl_sync(FULL, stop, 0) && !__any_sync(FULL, mine)) break;
+            if (it >= RING_WAIT_LIMIT) {
+                if (lane == 0) ring_set_abort(p, rh);
+                break;
+            }
+            __nanosleep(32);
+        }
+        if (!got) return;
+        const unsigned char* base = slots + (size_t)slot * ring_slot_bytes<T>(dpad);
+        const uint32_t f = rh->f[slot];
+        if (lane_on) {
+            float gg[VPL], mm[VPL], vv[VPL], ee[VPL];
+            const float* g = reinterpret_cast<const float*>(base);
+            RowIO<float, VPL>::load_generic(g, lane, gg);
+            RowIO<float, VPL>::load_generic(g + dpad, lane, mm);
+            RowIO<float, VPL>::load_generic(g + 2 * dpad, lane, vv);
+            RowIO<T, VPL>::load_generic(reinterpret_cast<const T*>(g + 3 * dpad), lane, ee);
+            adam_apply<T, VPL>((T*)p.table, p.m, p.v, f, dpad, gg, mm, vv, ee, as, p.seed, lane);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();   // our reads of the slot before the producer's reuse
+            *(volatile uint32_t*)&rh->consumed[slot] = round + 1;
+        }
+    }
+}
+
 template <typename T, typename A, int VPL, int MODE>
 __device__ __forceinline__ void finish_row(const ReduceParams& p, uint32_t f, const A (&acc)[VPL], int lane,
                                            bool lane_on, const AdamStep& as, uint32_t* fin, uint32_t& n_fin,
-                                           WarpQueue* q = nullptr) {
-    if constexpr (MODE == OUT_QUEUE) {
+                                           WarpQueue* q = nullptr, RingHdr* rh = nullptr,
+                                           unsigned char* ring_slots = nullptr) {
+    if constexpr (MODE == OUT_RING) {
+        // rows containing NaN get no Adam step (optimizer.rs:56): not queued
+        bool bad = false;
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) bad = bad || (acc[k] != acc[k]);
+        if (!__any_sync(FULL, bad)) ring_push<T, A, VPL>(p, rh, ring_slots, f, acc, lane, lane_on);
+    } else if constexpr (MODE == OUT_QUEUE) {
         // rows containing NaN get no Adam step (optimizer.rs:56): not queued
         bool bad = false;
 #pragma unroll
@@ -386,9 +563,25 @@ __device__ __forceinline__ void prefetch_segment_state(const ReduceParams& p, ui
 // passes the start of the next one.  Item metadata is software-pipelined:
 // while batch b is reduced, the role flags and scales of batch b+1 and the
 // keys of batch b+2 are in flight.
+// End of an OUT_RING CTA (every warp of both roles): once all warps are
+// here, the bulk copies of each slot's last issued round must have landed
+// before the CTA's shared memory is released.
+__device__ __forceinline__ void ring_finish(const ReduceParams& p, RingHdr* rh) {
+    asm volatile("bar.sync 1, %0;" ::"r"(blockDim.x) : "memory");
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < p.ring_slots; ++s) {
+            const uint32_t r = rh->issued[s];
+            if (!r) continue;
+            uint32_t it = 0;
+            while (!ring_test(&rh->full[s], (r - 1) & 1u) && ++it < RING_WAIT_LIMIT) __nanosleep(32);
+            if (it >= RING_WAIT_LIMIT) atomicOr(&p.st->error, ERR_RING_TIMEOUT);
+        }
+    }
+}
+
 template <typename T, typename A, int VPL, int MODE>
-__global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREADS,
-                                  VPL >= 16 ? 1 : (MODE == OUT_DENSE ? 3 : (MODE == OUT_QUEUE ? 4 : 2)))
+__global__ void __launch_bounds__(MODE == OUT_RING ? RING_MAX_WARPS * 32 : (MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREADS),
+                                  MODE == OUT_RING ? 1 : (VPL >= 16 ? 1 : (MODE == OUT_DENSE ? 3 : (MODE == OUT_QUEUE ? 4 : 2))))
     k_reduce(ReduceParams p) {
     pdl_wait();
     pdl_trigger();
@@ -408,6 +601,23 @@ __global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREAD
     q.f = reinterpret_cast<uint32_t*>(red_queue + (size_t)(blockDim.x >> 5) * QN * q.sb) + (threadIdx.x >> 5) * QN;
     q.head = 0;
     q.n = 0;
+    RingHdr* rh = reinterpret_cast<RingHdr*>(red_queue);
+    unsigned char* ring_slots = red_queue + ring_hdr_bytes();
+    const uint32_t warp = threadIdx.x >> 5;
+    if constexpr (MODE == OUT_RING) {
+        if (threadIdx.x == 0) {
+            for (uint32_t i = 0; i < p.ring_slots; ++i) {
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&rh->full[i])) : "memory");
+                rh->issued[i] = 0;
+                rh->consumed[i] = 0;
+            }
+            rh->tail = 0;
+            rh->done = 0;
+            rh->abort = 0;
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {   // read by k_fixup / k_fixup_long / k_adam_dense
         BatchState* st = p.st;
         st->n_long = 0;
@@ -419,14 +629,22 @@ __global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREAD
         st->fx_sigma = st->noise_sigma;
     }
     const unsigned lt_mask = (1u << lane) - 1u;
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    // OUT_RING: warps [0, ring_pw) reduce, the others run Adam
+    const uint32_t gw = MODE == OUT_RING ? blockIdx.x * p.ring_pw + warp : (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = MODE == OUT_RING ? gridDim.x * p.ring_pw : (gridDim.x * blockDim.x) >> 5;
     const uint32_t M = p.st->n_items;
     const uint32_t C = p.chunk;
     const uint32_t nchunks = (M + C - 1) / C;
     const uint32_t NR = p.NR;
     const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
     const AdamStep as = AdamStep::load(p.st);
+    if constexpr (MODE == OUT_RING) {
+        if (warp >= p.ring_pw) {
+            ring_consume<T, VPL>(p, rh, ring_slots, warp - p.ring_pw, lane, lane_on, as);
+            ring_finish(p, rh);
+            return;
+        }
+    }
     const D* dir = std::is_same<D, A>::value ? (const D*)p.dir : (const D*)p.dir16;
     const A* scale = (const A*)p.scale;
     unsigned long long g_cnt = 0, u_cnt = 0;
@@ -562,7 +780,7 @@ __global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREAD
             auto close_open = [&](int lo) {
                 if (started_here) {
                     if (any_kept) {
-                        finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, as, fin, n_fin, &q);
+                        finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, as, fin, n_fin, &q, rh, ring_slots);
                         ++u_cnt;
                     }
                 } else {
@@ -619,7 +837,7 @@ __global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREAD
         const bool cont = i1 < M && p.skey[i1] == cur_f;
         if (started_here && !cont) {
             if (any_kept) {
-                finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, as, fin, n_fin, &q);
+                finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, as, fin, n_fin, &q, rh, ring_slots);
                 ++u_cnt;
             }
         } else if (!started_here) {
@@ -634,11 +852,19 @@ __global__ void __launch_bounds__(MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREAD
     }
     if constexpr (MODE == OUT_DENSE) fin_flush(p, fin, n_fin, lane);
     if constexpr (MODE == OUT_QUEUE) queue_flush<T, VPL>(p, q, lane, lane_on, as);
+    if constexpr (MODE == OUT_RING) {
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            atomicAdd(&rh->done, 1u);
+        }
+    }
     g_cnt = warp_sum<unsigned long long>(g_cnt);
     if (lane == 0) {
         if (g_cnt) atomicAdd(&p.st->gathered, g_cnt);
         if (u_cnt) atomicAdd(&p.st->unique_rows, u_cnt);
     }
+    if constexpr (MODE == OUT_RING) ring_finish(p, rh);
 }
 
 // Chunk holding the last item of feature f, whose segment starts in chunk c
@@ -872,6 +1098,19 @@ static void red_launch(const ReduceParams& p, uint64_t cap, cudaStream_t s, int 
             uint32_t qctas = (warps + QUEUE_THREADS / 32 - 1) / (QUEUE_THREADS / 32);
             if (qctas > 2 * RED_MAX_CTAS) qctas = 2 * RED_MAX_CTAS;
             launch_chain(k_reduce<T, A, VPL, OUT_QUEUE>, qctas, QUEUE_THREADS, queue_smem<T>(p.dpad), s, p);
+        } else if (p.out_mode == OUT_RING) {
+            if constexpr (sizeof(T) != 8) {
+                // persistent: every CTA resident at once (one per SM at 16 warps)
+                const uint32_t threads = 32 * (p.ring_pw + p.ring_cw);
+                const size_t smem = ring_hdr_bytes() + (size_t)p.ring_slots * ring_slot_bytes<T>(p.dpad);
+                uint32_t per_sm = 65536u / (threads * 128u);
+                const uint32_t by_smem = (uint32_t)((227u * 1024u) / (smem + 1024u));
+                if (by_smem < per_sm) per_sm = by_smem;
+                if (per_sm < 1) per_sm = 1;
+                uint32_t rctas = (warps + p.ring_pw - 1) / p.ring_pw;
+                if (rctas > 152 * per_sm) rctas = 152 * per_sm;
+                launch_chain(k_reduce<T, A, VPL, OUT_RING>, rctas, threads, smem, s, p);
+            }
         }
         else launch_chain(k_reduce<T, A, VPL, OUT_ADAM>, ctas, RED_THREADS, 0, s, p);
     } else {
@@ -898,7 +1137,26 @@ static cudaError_t fixl_setup() {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_reduce<T, A, VPL, OUT_QUEUE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)queue_smem<T>(VPL * 32));
+    if constexpr (sizeof(T) != 8) {
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_reduce<T, A, VPL, OUT_RING>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     227 * 1024);
+    }
     return e;
+}
+
+bool ring_supported(int tt, uint32_t dpad, uint32_t pw, uint32_t cw, uint32_t slots) {
+    if (tt == TT_F64 || pw < 1 || cw < 1 || pw + cw > RING_MAX_WARPS || slots < 2 || slots > RING_MAX_SLOTS)
+        return false;
+    if (slots % cw) return false;   // each Adam warp owns whole slots (exact parity waits)
+    const uint32_t es = tt == TT_BF16 ? 2u : 4u;
+    if ((dpad * 4u) % 16u || (dpad * es) % 16u) return false;   // bulk copies move 16-byte multiples
+    return ring_smem_bytes(tt, dpad, slots) <= 227u * 1024u;
+}
+
+size_t ring_smem_bytes(int tt, uint32_t dpad, uint32_t slots) {
+    return ring_hdr_bytes() + (size_t)slots * (tt == TT_BF16 ? ring_slot_bytes<__nv_bfloat16>(dpad)
+                                                              : ring_slot_bytes<float>(dpad));
 }
 
 template <typename T, typename A>

@@ -17,7 +17,7 @@ def gpu_train(w, rows, cols, form, passes):
     ep = w["ep"]
     cfg = _native.default_config()
     cfg.dims, cfg.negatives, cfg.loss, cfg.gamma = ep["dims"], ep["negatives"], _native.LOSS_STARSPACE, ep["gamma"]
-    cfg.batch_size, cfg.alpha, cfg.passes, cfg.valid_pct = ep["batch_size"], ep["alpha"], passes, 0.0
+    cfg.batch_size, cfg.alpha, cfg.passes, cfg.valid_pct = w["batch"], ep["alpha"], passes, 0.0
     cfg.max_nodes_kind, cfg.max_nodes = _native.SAMPLE_FIXED, float(ep["max_nodes"])
     cfg.form = form
     ctx = _native.Context(cfg)
@@ -34,26 +34,37 @@ def cpu_train(oracle, w, rows, cols, weights, passes):
     ep = w["ep"]
     table, st = oracle.train(rows, cols, weights, w["fptr"], w["fids"], w["n_feat"], dims=ep["dims"],
                              alpha=ep["alpha"], loss=oracle.LOSS_STARSPACE, gamma=ep["gamma"],
-                             negatives=ep["negatives"], batch_size=ep["batch_size"], passes=passes,
+                             negatives=ep["negatives"], batch_size=w["batch"], passes=passes,
                              max_nodes=(oracle.SAMPLE_FIXED, float(ep["max_nodes"])), threads=0)
     return table
 
 
 @pytest.mark.parametrize("name,scale", [("cl10m", 0.05), ("cl1m", 0.2)])
 def test_heldout_recall_matches_cpu_reference(oracle, name, scale):
+    # A shrunken workload keeps the full one's batches per pass with a batch
+    # shrunk in proportion (next power of two): the CPU restatement runs its
+    # batches concurrently on every host core with hogwild writes, as the
+    # reference does, and with the full batch size a 5% graph has so few
+    # batches per pass that most of them would read a stale table.
     w = datagen.workload(name, scale=scale)
+    w["batch"] = 1 << int(np.ceil(np.log2(w["ep"]["batch_size"] * scale)))
     passes = w["ep"]["passes"]
     rows, cols, wts, test = evaluate.holdout_edges(w["rows"], w["cols"], w["weights"], 0.01, seed=5, max_test=5000)
     assert len(test) >= 2000
-    res = {}
+    res, tables = {}, {}
     for form, fid in (("fused", _native.FORM_FUSED_BF16), ("plain", _native.FORM_PLAIN_FP32)):
         table, stats = gpu_train(w, rows, cols, fid, passes)
         assert np.isfinite(table).all() and stats[-1]["kept_anchors"] > 0
+        tables[form] = table
         res[form] = evaluate.heldout_recall(w["fptr"], w["fids"], table, test)
+    assert not np.array_equal(tables["fused"], tables["plain"])
     res["cpu"] = evaluate.heldout_recall(w["fptr"], w["fids"], cpu_train(oracle, w, rows, cols, wts, passes), test)
-    print(name, {k: (round(v["recall"], 4), round(v["auc"], 4)) for k, v in res.items()})
+    print(name, {k: (round(v["recall"], 4), round(v["auc"], 4)) for k, v in res.items()},
+          "max |fused - plain|", float(np.abs(tables["fused"] - tables["plain"]).max()))
     for form in ("fused", "plain"):
         assert abs(res[form]["recall"] - res["cpu"]["recall"]) <= 0.01, res
+        # held-out edges vs random pairs: the CPU restatement's own spread
+        # over seeds is about 0.003 at these sizes
         assert abs(res[form]["auc"] - res["cpu"]["auc"]) <= 0.02, res
 
 

@@ -175,6 +175,58 @@ def test_multi_batch_graph_matches_single_batch_graphs(monkeypatch):
     assert np.array_equal(tables[0], tables[1])
 
 
+@pytest.mark.parametrize("mode", ["0", "1", "3"])
+def test_adam_placements_give_the_same_table(monkeypatch, mode):
+    # the fused form's Adam placements -- per row as each feature closes (0),
+    # a separate kernel over dense gradient rows (1), the per-warp queue (2,
+    # the reference point) and the warp-specialised ring with bulk copies (3)
+    # -- apply the same update to the same reduced rows: equal tables, bit for bit
+    w = datagen.workload("cl10m", scale=0.005)
+    tables = []
+    for m in ("2", mode):
+        monkeypatch.setenv("EP_FUSED_MODE", m)
+        ctx = _cl_ctx(w)
+        assert ctx.tuning()[2] == int(m)
+        st = ctx.train_batches(37)
+        assert st["kept_anchors"] > 0
+        tables.append(ctx.get_table(w["n_feat"], w["ep"]["dims"]))
+    assert np.array_equal(tables[0], tables[1])
+
+
+@pytest.mark.parametrize("ctas", ["1", "152", "608"])
+def test_persistent_gather_gives_the_same_table(monkeypatch, ctas):
+    # the staged gather as a persistent grid whose warps take anchors from a
+    # work queue (any grid size, down to one CTA) computes every anchor as
+    # the one-warp-per-anchor grid does
+    w = datagen.workload("cl10m", scale=0.005)
+    tables = []
+    for g in ("0", ctas):
+        monkeypatch.setenv("EP_GATHER_CTAS", g)
+        for graphs in (1, 0):
+            ctx = _cl_ctx_cfg(w, use_graphs=graphs)
+            ctx.train_batches(19)
+            tables.append(ctx.get_table(w["n_feat"], w["ep"]["dims"]))
+    assert all(np.array_equal(tables[0], t) for t in tables[1:])
+
+
+@pytest.mark.parametrize("shape", [("12", "4", "32"), ("6", "2", "4"), ("2", "14", "56"), ("1", "1", "2"),
+                                   ("15", "1", "3")])
+def test_ring_shapes_give_the_same_table(monkeypatch, shape):
+    # reducing warps, Adam warps and slots per CTA of the ring change the
+    # schedule only; tiny rings make every slot wrap many times
+    w = datagen.workload("cl10m", scale=0.005)
+    monkeypatch.setenv("EP_FUSED_MODE", "2")
+    ref = _cl_ctx(w)
+    ref.train_batches(21)
+    want = ref.get_table(w["n_feat"], w["ep"]["dims"])
+    monkeypatch.setenv("EP_FUSED_MODE", "3")
+    for k, v in zip(("EP_RING_PW", "EP_RING_CW", "EP_RING_SLOTS"), shape):
+        monkeypatch.setenv(k, v)
+    ctx = _cl_ctx(w)
+    ctx.train_batches(21)
+    assert np.array_equal(ctx.get_table(w["n_feat"], w["ep"]["dims"]), want)
+
+
 def test_graph_replays_match_stream_launches():
     # captured batches run k_batch_end on a side branch beside the sort and
     # reduction; the table and the pass statistics must equal those of the
