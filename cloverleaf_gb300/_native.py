@@ -98,6 +98,16 @@ class EpPassStats(ctypes.Structure):
         return d
 
 
+class EpLaunchShape(ctypes.Structure):
+    _fields_ = [("chunk", ctypes.c_uint32), ("fused_mode", ctypes.c_int32), ("graph_batches", ctypes.c_uint32),
+                ("gather_ctas", ctypes.c_uint32), ("ring_reduce_warps", ctypes.c_uint32),
+                ("ring_adam_warps", ctypes.c_uint32), ("ring_slots", ctypes.c_uint32), ("ring_active", ctypes.c_int32),
+                ("tuned", ctypes.c_int32), ("autotune", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class EpBatchSamples(ctypes.Structure):
     _fields_ = [
         ("n_anchors", ctypes.c_uint32),
@@ -149,6 +159,7 @@ SIGNATURES = {
     "ep_ag_forward": (ctypes.c_int, [_P, ctypes.POINTER(EpBatchSamples), ctypes.c_int, _P, _P, _P]),
     "ep_ag_backward": (ctypes.c_int, [_P, _P, _P, _P]),
     "ep_get_split": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(_U32), ctypes.POINTER(_U32)]),
+    "ep_get_launch_shape": (ctypes.c_int, [_P, _P]),
     "ep_sample_validation": (ctypes.c_int, [_P, _U32, _U32, _U32, _P, _P, _P, _P, _P]),
     "ep_synchronize": (ctypes.c_int, [_P]),
     "ep_last_error": (ctypes.c_char_p, [_P]),
@@ -285,6 +296,12 @@ class Context:
         check(lib().ep_sample_validation(self._h, int(first), int(n), int(stride), ptr(anchors), ptr(cnt), ptr(nbr),
                                          ptr(w), ptr(neg)), self._h, "ep_sample_validation")
         return anchors, cnt, nbr, w, neg
+
+    def launch_shape(self):
+        """Every launch shape in use (ep_get_launch_shape) as a dict."""
+        out = EpLaunchShape()
+        check(lib().ep_get_launch_shape(self._h, ctypes.byref(out)), self._h, "ep_get_launch_shape")
+        return out.as_dict()
 
     def tuning(self):
         """(tuned, chunk, fused_mode, graph_batches) of this context."""

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -185,6 +186,7 @@ extern "C" void ep_config_default(ep_config* cfg) {
     cfg->form = EP_FORM_PLAIN_FP32;
     cfg->grad_mode = EP_GRAD_REFERENCE;
     cfg->use_graphs = 1;
+    cfg->autotune = 1;
     cfg->ppr_restart_p = 0.5f;
 }
 
@@ -259,6 +261,9 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     if (const char* e = getenv("EP_RING_CW")) { const long v = atol(e); if (v >= 1 && v <= 15) c->ring_cw = (uint32_t)v; }
     if (const char* e = getenv("EP_RING_SLOTS")) { const long v = atol(e); if (v >= 2 && v <= 64) c->ring_slots = (uint32_t)v; }
     if (const char* e = getenv("EP_GATHER_CTAS")) { const long v = atol(e); if (v >= 0 && v <= 65536) c->gather_ctas = (uint32_t)v; }
+    // a launch shape set by hand is used as given: no tuning
+    for (const char* k : {"EP_FUSED_MODE", "EP_REDUCE_CHUNK", "EP_GATHER_CTAS", "EP_RING_PW", "EP_RING_CW", "EP_RING_SLOTS"})
+        if (getenv(k)) c->cfg.autotune = 0;
     if (const char* ch = getenv("EP_REDUCE_CHUNK")) {   // reducer items per warp (tuning)
         const long v = atol(ch);
         if (v >= 32 && v <= (1l << 20)) c->chunk = (uint32_t)v;
@@ -588,8 +593,9 @@ static int prepare_train(ep_ctx* c) {
     // with the autotuner, size the reducer carries for its smallest chunk and
     // keep the dense gradient buffers for the split Adam placement
     const uint32_t chunk = c->chunk;
-    if (c->cfg.autotune) c->chunk = std::min<uint32_t>(c->chunk, kTuneChunks[0]);
-    int rc = ensure_bufs(c, B, K, items, 4, c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_mode == 1 || c->cfg.autotune);
+    if (c->cfg.autotune >= 2) c->chunk = std::min<uint32_t>(c->chunk, kTuneChunks[0]);
+    int rc = ensure_bufs(c, B, K, items, 4,
+                         c->cfg.form == EP_FORM_PLAIN_FP32 || c->fused_mode == 1 || c->cfg.autotune >= 2);
     c->chunk = chunk;
     if (rc) return rc;
     c->Bcap = B;
@@ -845,32 +851,61 @@ static int launch_train_batch(ep_ctx* c);
 // batches replay one graph holding that many copies of the batch (the
 // device-resident BatchState moves each copy to the next batch, crossing pass
 // boundaries as the device would); the remainder replays the one-batch graph.
-// The autotuner (config.autotune): times kTuneTimed batches after kTuneWarm
+//
+// The autotuner (config.autotune) times kTuneTimed batches after kTuneWarm
 // warm-up batches under each candidate launch shape and keeps the fastest.
-// The batches it runs are ordinary training batches of the pass (they update
-// the table); it runs once per context, when at least all candidates' batches
-// are requested in one call.  Chosen values: ep_get_tuning.
-static int autotune(ep_ctx* c, uint32_t& n) {
-    struct Cand { uint32_t chunk; int mode; };
-    Cand cands[6];
-    int nc = 0;
-    const bool fused = c->cfg.form == EP_FORM_FUSED_BF16;
-    for (uint32_t ch : kTuneChunks) {
-        cands[nc++] = {ch, fused ? 2 : c->fused_mode};
-        if (fused) cands[nc++] = {ch, 1};
+// Level 1 tries only shapes that leave every result bit-identical (tested):
+// the FUSED form's Adam placement -- queued in the reducing warp, or the
+// warp-specialised ring with two splits of a CTA into reducing and Adam
+// warps -- and the staged gather's grid: one warp per anchor, or a persistent
+// grid of 2 or 3 CTAs per SM taking anchors from a work queue.  Level 2 also
+// tries reducer chunk sizes and the split-off Adam kernel; chunk sizes change
+// the floating-point summation order, so level 2 trades reproducibility for
+// speed.  The batches it runs are ordinary training batches of the pass (they
+// update the table); it runs once per context, when at least all candidates'
+// batches are requested in one call, and its choice is remembered per
+// workload shape and device, so later contexts on the same shape start with
+// it.  Chosen values: ep_get_tuning, ep_get_launch_shape.
+struct TuneChoice {
+    uint32_t chunk;
+    int mode;
+    uint32_t gather_ctas, pw, cw, slots;
+};
+
+namespace {
+std::mutex g_tune_mu;
+std::map<std::vector<uint64_t>, TuneChoice> g_tune_cache;
+
+std::vector<uint64_t> tune_key(const ep_ctx* c) {
+    return {(uint64_t)c->cfg.form, (uint64_t)c->cfg.autotune, c->dims, c->Bcap, c->R, c->Kcap, c->n_feat, c->n_nodes,
+            c->n_edges, (uint64_t)c->cfg.loss, (uint64_t)c->device, (uint64_t)c->cfg.max_features_kind};
+}
+
+void apply_choice(ep_ctx* c, const TuneChoice& t) {
+    c->chunk = t.chunk;
+    c->fused_mode = t.mode;
+    c->gather_ctas = t.gather_ctas;
+    c->ring_pw = t.pw;
+    c->ring_cw = t.cw;
+    c->ring_slots = t.slots;
+    c->drop_graph();
+}
+}  // namespace
+
+// Times each candidate on real batches; returns the fastest (or the current
+// shape when a launch fails, with rc set).
+static int tune_stage(ep_ctx* c, const std::vector<TuneChoice>& cands, TuneChoice* pick) {
+    if (cands.size() < 2) {
+        if (!cands.empty()) *pick = cands[0];
+        return EP_OK;
     }
-    const uint32_t need = (uint32_t)nc * (kTuneWarm + kTuneTimed);
-    if (n < need) return EP_OK;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0), "tuning events");
     CK(cudaEventCreate(&e1), "tuning events");
     float best = 0.f;
-    Cand pick = {c->chunk, c->fused_mode};
     int rc = EP_OK;
-    for (int i = 0; i < nc && !rc; ++i) {
-        c->chunk = cands[i].chunk;
-        c->fused_mode = cands[i].mode;
-        c->drop_graph();
+    for (size_t i = 0; i < cands.size() && !rc; ++i) {
+        apply_choice(c, cands[i]);
         for (uint32_t b = 0; b < kTuneWarm && !rc; ++b) rc = launch_train_batch(c);
         cudaEventRecord(e0, c->stream);
         for (uint32_t b = 0; b < kTuneTimed && !rc; ++b) rc = launch_train_batch(c);
@@ -879,16 +914,77 @@ static int autotune(ep_ctx* c, uint32_t& n) {
         if (cudaEventSynchronize(e1) != cudaSuccess) { rc = c->cuda_fail(cudaGetLastError(), "tuning"); break; }
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
-        if (i == 0 || ms < best) { best = ms; pick = cands[i]; }
+        if (i == 0 || ms < best) { best = ms; *pick = cands[i]; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (rc) return rc;
-    n -= need;
-    c->chunk = pick.chunk;
-    c->fused_mode = pick.mode;
-    c->drop_graph();
+    return rc;
+}
+
+// A choice remembered for this workload shape, applied without timing.
+static bool tune_from_cache(ep_ctx* c) {
+    if (!c->cfg.autotune || c->tuned) return c->tuned;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(tune_key(c));
+    if (it == g_tune_cache.end()) return false;
+    apply_choice(c, it->second);
     c->tuned = true;
+    return true;
+}
+
+// Candidates of the two tuning stages; `need` receives the batches they take.
+static void tune_candidates(const ep_ctx* c, std::vector<TuneChoice>& s1, uint32_t& need) {
+    const TuneChoice cur = {c->chunk, c->fused_mode, c->gather_ctas, c->ring_pw, c->ring_cw, c->ring_slots};
+    const bool fused = c->cfg.form == EP_FORM_FUSED_BF16;
+    const int level = c->cfg.autotune;
+    // stage 1: reducer chunk (level 2) x Adam placement (FUSED form)
+    const std::vector<uint32_t> chunks = level >= 2 ? std::vector<uint32_t>(kTuneChunks, kTuneChunks + 3)
+                                                    : std::vector<uint32_t>{c->chunk};
+    for (uint32_t ch : chunks) {
+        TuneChoice t = cur;
+        t.chunk = ch;
+        if (!fused) { s1.push_back(t); continue; }
+        t.mode = 2;
+        s1.push_back(t);
+        if (level >= 2) { t.mode = 1; s1.push_back(t); }
+        const uint32_t rings[2][3] = {{12, 4, 32}, {10, 6, 36}};
+        for (const auto& r : rings)
+            if (ring_supported(c->tt, c->dpad, r[0], r[1], r[2])) {
+                t.mode = 3; t.pw = r[0]; t.cw = r[1]; t.slots = r[2];
+                s1.push_back(t);
+            }
+    }
+    // stage 2 times three gather grids
+    need = (uint32_t)((s1.size() > 1 ? s1.size() : 0) + 3) * (kTuneWarm + kTuneTimed);
+}
+
+static int autotune(ep_ctx* c, uint32_t& n) {
+    if (tune_from_cache(c)) return EP_OK;
+    const TuneChoice cur = {c->chunk, c->fused_mode, c->gather_ctas, c->ring_pw, c->ring_cw, c->ring_slots};
+    std::vector<TuneChoice> s1;
+    uint32_t need = 0;
+    tune_candidates(c, s1, need);
+    if (n < need) return EP_OK;
+    // stage 2: the staged gather's grid, with the stage-1 choice
+    const uint32_t gathers[3] = {0, 2 * 152, 3 * 152};
+    TuneChoice pick = cur;
+    int rc = tune_stage(c, s1, &pick);
+    std::vector<TuneChoice> s2;
+    for (uint32_t g : gathers) {
+        TuneChoice t = pick;
+        t.gather_ctas = g;
+        s2.push_back(t);
+    }
+    if (!rc) rc = tune_stage(c, s2, &pick);
+    if (rc) {
+        apply_choice(c, cur);
+        return rc;
+    }
+    n -= need;
+    apply_choice(c, pick);
+    c->tuned = true;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[tune_key(c)] = pick;
     return EP_OK;
 }
 
@@ -912,7 +1008,12 @@ static int capture_batches(ep_ctx* c, uint32_t batches, cudaGraphExec_t* out) {
 // that the one-time capture and instantiation stay outside its timing.
 static int prepare_graphs(ep_ctx* c, uint32_t n) {
     if (!(c->cfg.use_graphs && c->cfg.form == EP_FORM_FUSED_BF16) || n == 0) return EP_OK;
-    if (c->cfg.autotune && !c->tuned) return EP_OK;   // the tuner rebuilds them per candidate
+    if (c->cfg.autotune && !tune_from_cache(c)) {
+        std::vector<TuneChoice> s1;
+        uint32_t need = 0;
+        tune_candidates(c, s1, need);
+        if (n >= need) return EP_OK;   // this run starts with the tuner, which rebuilds them per candidate
+    }
     const uint32_t k = c->graph_batches;
     int rc = EP_OK;
     if (k > 1 && n >= k && !c->gexec_run) rc = capture_batches(c, k, &c->gexec_run);
@@ -1391,6 +1492,21 @@ extern "C" int ep_ag_backward(ep_ctx* c, const void* dloss_dev, void* grad_dev, 
                      (uint32_t)std::min<uint64_t>(c->n_feat, c->items_cap), s);
     CK(cudaGetLastError(), "gradient scatter");
     CK(cudaStreamSynchronize(s), "autograd backward");
+    return EP_OK;
+}
+
+extern "C" int ep_get_launch_shape(ep_ctx* c, ep_launch_shape* out) {
+    if (!c || !out) return EP_ERR_INVALID_ARG;
+    out->chunk = c->chunk;
+    out->fused_mode = c->fused_mode;
+    out->graph_batches = c->graph_batches;
+    out->gather_ctas = c->gather_ctas;
+    out->ring_reduce_warps = c->ring_pw;
+    out->ring_adam_warps = c->ring_cw;
+    out->ring_slots = c->ring_slots;
+    out->ring_active = c->cfg.form == EP_FORM_FUSED_BF16 && fused_out_mode(c) == OUT_RING;
+    out->tuned = c->tuned;
+    out->autotune = c->cfg.autotune;
     return EP_OK;
 }
 

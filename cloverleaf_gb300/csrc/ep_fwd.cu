@@ -1050,22 +1050,8 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 8 ? 4 : 3) : 1) k_fwd_ga
     const uint32_t n = p.st->n_anchors;
     if constexpr (STAGED) {
         extern __shared__ __align__(16) unsigned char fwd_smem[];
-        WarpTables& W = reinterpret_cast<WarpTables*>(fwd_smem)[threadIdx.x >> 5];
-        // persistent (gather_ctas > 0): each warp takes the next anchor from
-        // the batch's work queue until none is left, so a warp that drew
-        // short anchors takes more of them and no wave waits on the slowest;
-        // otherwise one anchor per warp
-        const bool queue = p.gather_ctas != 0;
-        uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-        for (;;) {
-            if (queue) {
-                if (lane == 0) a = atomicAdd(&p.st->fwd_next, 1u);
-                a = __shfl_sync(FULL, a, 0);
-            }
-            if (a >= n) break;
-            gather_staged<T, A, VPL>(p, W, a, lane);
-            if (!queue) break;
-        }
+        const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        if (a < n) gather_staged<T, A, VPL>(p, reinterpret_cast<WarpTables*>(fwd_smem)[threadIdx.x >> 5], a, lane);
         return;
     }
     const uint32_t a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1102,6 +1088,30 @@ __global__ void __launch_bounds__(256, STAGED ? (VPL <= 8 ? 4 : 3) : 1) k_fwd_ga
             }
             if (lane == 0) scale[sbase + r] = nr;
         }
+    }
+}
+
+// k_fwd_gather_queue: the staged gather as a persistent grid (gather_ctas
+// CTAs).  Each warp takes the next anchor from the batch's work queue
+// (BatchState::fwd_next, zeroed by k_batch_begin) until none is left, so a
+// warp that drew short anchors takes more of them and no wave waits on its
+// slowest warp.  MINB CTAs per SM (2 or 3, from the grid size) set the
+// register budget of the loop (the one-shot kernel is at its 64-register
+// limit at 4).
+template <typename T, typename A, int VPL, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_fwd_gather_queue(ForwardParams p) {
+    pdl_wait();
+    pdl_trigger();
+    extern __shared__ __align__(16) unsigned char fwd_smem[];
+    WarpTables& W = reinterpret_cast<WarpTables*>(fwd_smem)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const uint32_t n = p.st->n_anchors;
+    for (;;) {
+        uint32_t a = 0;
+        if (lane == 0) a = atomicAdd(&p.st->fwd_next, 1u);
+        a = __shfl_sync(FULL, a, 0);
+        if (a >= n) break;
+        gather_staged<T, A, VPL>(p, W, a, lane);
     }
 }
 
@@ -1639,6 +1649,8 @@ static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s, int
     static bool attr = false;   // opt in to > 48 KB of dynamic shared memory once
     if (!attr) {
         cudaFuncSetAttribute(k_fwd_gather<T, A, VPL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_fwd_gather_queue<T, A, VPL, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_fwd_gather_queue<T, A, VPL, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
     }
     if (part == FWD_EMIT) {
@@ -1646,8 +1658,12 @@ static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s, int
         return;
     }
     if (part != FWD_LOSS) {
-        const uint32_t gblocks = p.gather_ctas ? std::min(p.gather_ctas, blocks) : blocks;
-        launch_chain(k_fwd_gather<T, A, VPL, true>, gblocks, 32 * FWD_WARPS, smem, s, p);
+        if (p.gather_ctas > 2 * 152)
+            launch_chain(k_fwd_gather_queue<T, A, VPL, 3>, std::min(p.gather_ctas, blocks), 32 * FWD_WARPS, smem, s, p);
+        else if (p.gather_ctas)
+            launch_chain(k_fwd_gather_queue<T, A, VPL, 2>, std::min(p.gather_ctas, blocks), 32 * FWD_WARPS, smem, s, p);
+        else
+            launch_chain(k_fwd_gather<T, A, VPL, true>, blocks, 32 * FWD_WARPS, smem, s, p);
         launch_chain(k_fwd_gather<T, A, VPL, false>, blocks, 32 * FWD_WARPS, 0, s, p);
     }
     if (part != FWD_GATHER) launch_chain(k_fwd_loss<T, A, VPL>, (cap + 3) / 4, 128, 0, s, p);

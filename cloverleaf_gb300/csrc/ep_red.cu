@@ -881,7 +881,9 @@ __device__ __forceinline__ uint32_t owner_last(const ReduceParams& p, uint32_t c
         const bool in = probe < hi && p.skey[probe] == f;
         const uint32_t k = __popc(__ballot_sync(FULL, in));
         const uint32_t nlo = lo + k * stepw;
-        hi = min(hi, nlo + stepw);
+        // probe k + 1 (outside f, or past hi) bounds the span; when all 32
+        // probes are inside, nothing new is known above the last one
+        if (k < 32) hi = min(hi, nlo + stepw);
         lo = nlo;
     }
     return lo / C;

@@ -94,8 +94,13 @@ typedef struct ep_config {
     int32_t device;              /* CUDA device ordinal */
     int32_t use_graphs;          /* replay each batch as a CUDA graph */
     int32_t autotune;            /* pick launch shapes by timing candidates on the
-                                    first training batches (see ep_get_tuning);
-                                    results then depend on timing: default 0 */
+                                    first training batches (see ep_get_launch_shape):
+                                    0 off; 1 (default) only shapes that leave results
+                                    bit-identical; 2 also reducer chunk sizes, whose
+                                    summation order then depends on timing.  Setting a
+                                    shape through EP_FUSED_MODE, EP_REDUCE_CHUNK,
+                                    EP_GATHER_CTAS or EP_RING_* in the environment
+                                    turns tuning off */
     float ppr_restart_p;         /* EP_LOSS_PPR walk restart probability in [0, 1] */
 } ep_config;
 
@@ -231,12 +236,29 @@ int ep_get_table(ep_ctx* ctx, float* out);
 
 /* Launch shapes in use (no counterpart in the reference): the reducer's items
  * per warp, the FUSED form's Adam placement (2 = queued in the reducer, 1 = a
- * separate kernel, 0 = per row as each feature closes) and the batches per
- * replayed CUDA graph.  With config.autotune the first training call that
- * asks for enough batches times the candidates on real batches and keeps the
- * fastest; returns EP_OK once that choice is made, 1 before (the values are
- * then the defaults).  Any pointer may be NULL. */
+ * separate kernel, 0 = per row as each feature closes, 3 = the
+ * warp-specialised ring) and the batches per replayed CUDA graph.  With
+ * config.autotune the first training call that asks for enough batches times
+ * the candidates on real batches and keeps the fastest; returns EP_OK once
+ * that choice is made, 1 before (the values are then the defaults).  Any
+ * pointer may be NULL. */
 int ep_get_tuning(ep_ctx* ctx, uint32_t* chunk, int32_t* fused_mode, uint32_t* graph_batches);
+
+/* Every launch shape in use (no counterpart in the reference), including
+ * those ep_get_tuning does not report: the staged gather's grid (0 = one
+ * warp per anchor, else persistent CTAs taking anchors from a work queue)
+ * and the ring's reducing warps, Adam warps and slots per CTA. */
+typedef struct ep_launch_shape {
+    uint32_t chunk;
+    int32_t fused_mode;
+    uint32_t graph_batches;
+    uint32_t gather_ctas;
+    uint32_t ring_reduce_warps, ring_adam_warps, ring_slots;
+    int32_t ring_active;         /* the FUSED form reduces through the ring */
+    int32_t tuned;               /* the autotuner has made its choice */
+    int32_t autotune;            /* the tuning level in effect */
+} ep_launch_shape;
+int ep_get_launch_shape(ep_ctx* ctx, ep_launch_shape* out);
 
 /* Row download without device allocation (no counterpart in the reference).
  * Writes rows [first_row, first_row + n_rows) of the table to out (host

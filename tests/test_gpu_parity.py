@@ -73,6 +73,31 @@ def test_batch_grad_plain_fp32(oracle, loss, dims):
     check_parity(oracle, prob, smp, ctx, prob["table"], loss=loss, gamma=gamma)
 
 
+def zipf_problem(seed):
+    """Zipf(1.1) feature ids over 2,000 slots: many features whose items span
+    several reducer chunks, ending at every offset within a chunk."""
+    prob = random_problem(seed, n=3000, n_feat=2000, dims=16, deg=(1, 12), feats=(1, 16))
+    rng = np.random.default_rng(seed + 1)
+    p = 1.0 / np.arange(1, prob["n_feat"] + 1) ** 1.1
+    prob["fids"] = rng.choice(prob["n_feat"], len(prob["fids"]), p=p / p.sum()).astype(np.uint32)
+    return prob
+
+
+@pytest.mark.parametrize("chunk", ["32", "64", "128"])
+@pytest.mark.parametrize("form", [0, 1])
+def test_batch_grad_multi_chunk_spans(oracle, monkeypatch, chunk, form):
+    # the fix-ups locate the last chunk of each feature spanning three or more
+    # chunks by a 32-ary search; every such feature's last partial sum must
+    # be included (about ten features per case here end where a search
+    # that clipped its bound after 32 inside probes would stop one chunk early)
+    monkeypatch.setenv("EP_REDUCE_CHUNK", chunk)
+    prob = zipf_problem(3)
+    smp = sample_batch(3, prob, B=1024, K=10, R=5)
+    ctx = make_ctx(prob, loss=1, gamma=0.5, R=5, form=form)
+    table = ctx.get_table(prob["n_feat"], prob["dims"]) if form else prob["table"]   # BF16-rounded when fused
+    check_parity(oracle, prob, smp, ctx, table, grad_tol=TOL if form == 0 else TOL_GRAD_BF16, loss=1, gamma=0.5)
+
+
 @pytest.mark.parametrize("name", ["margin", "starspace"])
 @pytest.mark.parametrize("form", [0, 1])
 def test_default_losses_known_answers(name, form):

@@ -75,8 +75,9 @@ def cl1m():
     return w
 
 
-@pytest.mark.parametrize("weighted", [False, True])
-def test_cl1m_batches_plain_fp32_parity(oracle, cl1m, weighted):
+@pytest.mark.parametrize("weighted,chunk", [(False, "128"), (True, "128"), (False, "32")])
+def test_cl1m_batches_plain_fp32_parity(oracle, monkeypatch, cl1m, weighted, chunk):
+    monkeypatch.setenv("EP_REDUCE_CHUNK", chunk)
     w = cl1m
     ep = w["ep"]
     n = len(w["rows"]) - 1

@@ -266,15 +266,35 @@ def test_graph_replays_match_stream_launches_with_direct_gathers():
 
 
 @pytest.mark.parametrize("form", [_native.FORM_FUSED_BF16, _native.FORM_PLAIN_FP32])
-def test_autotune_picks_a_candidate_and_trains(form):
+@pytest.mark.parametrize("level", [1, 2])
+def test_autotune_picks_a_candidate_and_trains(form, level):
     w = datagen.workload("cl10m", scale=0.01)
-    ctx = _cl_ctx(w, form=form, autotune=1)
+    ctx = _cl_ctx(w, form=form, autotune=level)
     assert ctx.tuning()[0] is False
-    s1 = ctx.train_batches(70)          # the candidates' batches, then 10 more
+    s1 = ctx.train_batches(130)          # the candidates' batches, then more
+    shape = ctx.launch_shape()
     tuned, chunk, mode, _ = ctx.tuning()
-    assert tuned and chunk in (64, 128, 256)
-    assert mode in ((1, 2) if form == _native.FORM_FUSED_BF16 else (2,))
+    assert tuned and shape["tuned"] and shape["autotune"] == level
+    assert chunk == 128 if level == 1 else chunk in (64, 128, 256)
+    if form == _native.FORM_FUSED_BF16:
+        assert mode in ((2, 3) if level == 1 else (1, 2, 3))
+    assert shape["gather_ctas"] in (0, 304, 456)
     ctx.train_batches(120)
     s2 = ctx.train_batches(10)
     assert s2["train_loss"] < s1["train_loss"]
     assert np.isfinite(ctx.get_table(w["n_feat"], w["ep"]["dims"])).all()
+    # a second context on the same workload starts with the remembered choice
+    again = _cl_ctx(w, form=form, autotune=level)
+    again.train_batches(1)
+    assert again.launch_shape() == shape
+
+
+def test_level_one_tuning_keeps_results_identical():
+    # level 1 only chooses between launch shapes that give the same bits
+    w = datagen.workload("cl10m", scale=0.01)
+    tables = []
+    for level in (0, 1):
+        ctx = _cl_ctx(w, autotune=level)
+        ctx.train_batches(110)
+        tables.append(ctx.get_table(w["n_feat"], w["ep"]["dims"]))
+    assert np.array_equal(tables[0], tables[1])
