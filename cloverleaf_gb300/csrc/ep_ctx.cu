@@ -103,10 +103,13 @@ struct ep_ctx {
     uint32_t ring_pw = 12, ring_cw = 4, ring_slots = 32;
     // persistent staged gather: CTAs of its grid (0 = one warp per anchor)
     uint32_t gather_ctas = 0;
+    // the queue reducer's resident CTAs per SM (4, or 5 with fewer registers)
+    uint32_t queue_ctas = 4;
     bool tuned = false;         // autotuner has chosen chunk / fused_mode
     bool prepared = false;
     cudaGraphExec_t gexec = nullptr;
     cudaGraphExec_t gexec_run = nullptr;   // graph_batches consecutive batches
+    std::map<uint32_t, cudaGraphExec_t> gexec_rem;   // 2 .. graph_batches - 1 consecutive batches (a run's remainder)
     uint32_t graph_batches = 16;
     uint32_t* sorted_keys = nullptr;
     uint2* sorted_vals = nullptr;
@@ -126,6 +129,7 @@ struct ep_ctx {
     ~ep_ctx() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (gexec_run) cudaGraphExecDestroy(gexec_run);
+        for (auto& kv : gexec_rem) cudaGraphExecDestroy(kv.second);
         if (h_st) cudaFreeHost(h_st);
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_join) cudaEventDestroy(ev_join);
@@ -155,6 +159,8 @@ struct ep_ctx {
     void drop_graph() {
         if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
         if (gexec_run) { cudaGraphExecDestroy(gexec_run); gexec_run = nullptr; }
+        for (auto& kv : gexec_rem) cudaGraphExecDestroy(kv.second);
+        gexec_rem.clear();
     }
 };
 
@@ -261,8 +267,10 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     if (const char* e = getenv("EP_RING_CW")) { const long v = atol(e); if (v >= 1 && v <= 15) c->ring_cw = (uint32_t)v; }
     if (const char* e = getenv("EP_RING_SLOTS")) { const long v = atol(e); if (v >= 2 && v <= 64) c->ring_slots = (uint32_t)v; }
     if (const char* e = getenv("EP_GATHER_CTAS")) { const long v = atol(e); if (v >= 0 && v <= 65536) c->gather_ctas = (uint32_t)v; }
+    if (const char* e = getenv("EP_QUEUE_CTAS")) { const long v = atol(e); if (v == 4 || v == 5) c->queue_ctas = (uint32_t)v; }
     // a launch shape set by hand is used as given: no tuning
-    for (const char* k : {"EP_FUSED_MODE", "EP_REDUCE_CHUNK", "EP_GATHER_CTAS", "EP_RING_PW", "EP_RING_CW", "EP_RING_SLOTS"})
+    for (const char* k : {"EP_FUSED_MODE", "EP_REDUCE_CHUNK", "EP_GATHER_CTAS", "EP_QUEUE_CTAS", "EP_RING_PW", "EP_RING_CW",
+                          "EP_RING_SLOTS"})
         if (getenv(k)) c->cfg.autotune = 0;
     if (const char* ch = getenv("EP_REDUCE_CHUNK")) {   // reducer items per warp (tuning)
         const long v = atol(ch);
@@ -730,6 +738,7 @@ static ReduceParams reduce_params(ep_ctx* c, BatchState* st, int out_mode, void*
     rp.ring_pw = c->ring_pw;
     rp.ring_cw = c->ring_cw;
     rp.ring_slots = c->ring_slots;
+    rp.queue_ctas_per_sm = c->queue_ctas;
     return rp;
 }
 
@@ -850,7 +859,8 @@ static int launch_train_batch(ep_ctx* c);
 // Issues n consecutive training batches.  With graphs, runs of graph_batches
 // batches replay one graph holding that many copies of the batch (the
 // device-resident BatchState moves each copy to the next batch, crossing pass
-// boundaries as the device would); the remainder replays the one-batch graph.
+// boundaries as the device would); a remainder of r >= 2 batches replays a
+// graph of r batches, a single batch the one-batch graph.
 //
 // The autotuner (config.autotune) times kTuneTimed batches after kTuneWarm
 // warm-up batches under each candidate launch shape and keeps the fastest.
@@ -869,7 +879,7 @@ static int launch_train_batch(ep_ctx* c);
 struct TuneChoice {
     uint32_t chunk;
     int mode;
-    uint32_t gather_ctas, pw, cw, slots;
+    uint32_t gather_ctas, pw, cw, slots, qctas;
 };
 
 namespace {
@@ -888,6 +898,7 @@ void apply_choice(ep_ctx* c, const TuneChoice& t) {
     c->ring_pw = t.pw;
     c->ring_cw = t.cw;
     c->ring_slots = t.slots;
+    c->queue_ctas = t.qctas;
     c->drop_graph();
 }
 }  // namespace
@@ -934,7 +945,7 @@ static bool tune_from_cache(ep_ctx* c) {
 
 // Candidates of the two tuning stages; `need` receives the batches they take.
 static void tune_candidates(const ep_ctx* c, std::vector<TuneChoice>& s1, uint32_t& need) {
-    const TuneChoice cur = {c->chunk, c->fused_mode, c->gather_ctas, c->ring_pw, c->ring_cw, c->ring_slots};
+    const TuneChoice cur = {c->chunk, c->fused_mode, c->gather_ctas, c->ring_pw, c->ring_cw, c->ring_slots, c->queue_ctas};
     const bool fused = c->cfg.form == EP_FORM_FUSED_BF16;
     const int level = c->cfg.autotune;
     // stage 1: reducer chunk (level 2) x Adam placement (FUSED form)
@@ -945,7 +956,9 @@ static void tune_candidates(const ep_ctx* c, std::vector<TuneChoice>& s1, uint32
         t.chunk = ch;
         if (!fused) { s1.push_back(t); continue; }
         t.mode = 2;
+        t.qctas = 4;
         s1.push_back(t);
+        if (c->vpl <= 8) { t.qctas = 5; s1.push_back(t); t.qctas = 4; }
         if (level >= 2) { t.mode = 1; s1.push_back(t); }
         const uint32_t rings[2][3] = {{12, 4, 32}, {10, 6, 36}};
         for (const auto& r : rings)
@@ -960,7 +973,7 @@ static void tune_candidates(const ep_ctx* c, std::vector<TuneChoice>& s1, uint32
 
 static int autotune(ep_ctx* c, uint32_t& n) {
     if (tune_from_cache(c)) return EP_OK;
-    const TuneChoice cur = {c->chunk, c->fused_mode, c->gather_ctas, c->ring_pw, c->ring_cw, c->ring_slots};
+    const TuneChoice cur = {c->chunk, c->fused_mode, c->gather_ctas, c->ring_pw, c->ring_cw, c->ring_slots, c->queue_ctas};
     std::vector<TuneChoice> s1;
     uint32_t need = 0;
     tune_candidates(c, s1, need);
@@ -1017,7 +1030,13 @@ static int prepare_graphs(ep_ctx* c, uint32_t n) {
     const uint32_t k = c->graph_batches;
     int rc = EP_OK;
     if (k > 1 && n >= k && !c->gexec_run) rc = capture_batches(c, k, &c->gexec_run);
-    if (!rc && (k == 1 || n % k) && !c->gexec) rc = capture_batches(c, 1, &c->gexec);
+    const uint32_t r = k > 1 ? n % k : 1;
+    if (!rc && r == 1 && !c->gexec) rc = capture_batches(c, 1, &c->gexec);
+    if (!rc && r >= 2 && !c->gexec_rem.count(r)) {
+        cudaGraphExec_t g = nullptr;
+        rc = capture_batches(c, r, &g);
+        if (!rc) c->gexec_rem[r] = g;
+    }
     return rc;
 }
 
@@ -1038,6 +1057,20 @@ static int launch_train_run(ep_ctx* c, uint32_t n) {
             c->launches += (uint64_t)k * kernels_per_batch(c, true);
             for (uint32_t i = 0; i < k; ++i) advance_host_batch(c);
             n -= k;
+        } else if (use_graph && n >= 2) {
+            // the run's remainder as one graph of n batches: their fix-ups
+            // overlap the next batch's sampling as in the full-size graph
+            auto it = c->gexec_rem.find(n);
+            if (it == c->gexec_rem.end()) {
+                cudaGraphExec_t g = nullptr;
+                int rc = capture_batches(c, n, &g);
+                if (rc) return rc;
+                it = c->gexec_rem.emplace(n, g).first;
+            }
+            CK(cudaGraphLaunch(it->second, c->stream), "graph launch");
+            c->launches += (uint64_t)n * kernels_per_batch(c, true);
+            for (uint32_t i = 0; i < n; ++i) advance_host_batch(c);
+            n = 0;
         } else {
             int rc = launch_train_batch(c);
             if (rc) return rc;
@@ -1504,6 +1537,7 @@ extern "C" int ep_get_launch_shape(ep_ctx* c, ep_launch_shape* out) {
     out->ring_reduce_warps = c->ring_pw;
     out->ring_adam_warps = c->ring_cw;
     out->ring_slots = c->ring_slots;
+    out->queue_ctas_per_sm = c->queue_ctas;
     out->ring_active = c->cfg.form == EP_FORM_FUSED_BF16 && fused_out_mode(c) == OUT_RING;
     out->tuned = c->tuned;
     out->autotune = c->cfg.autotune;

@@ -188,6 +188,8 @@ struct ReduceParams {
     uint32_t* long_list;    // long spans: (owner chunk, last chunk) pairs [n_chunks][2]
     // OUT_RING shape: reducing warps, Adam warps and ring slots per CTA
     uint32_t ring_pw, ring_cw, ring_slots;
+    // OUT_QUEUE: resident CTAs per SM the reducer is compiled for (4 or 5)
+    uint32_t queue_ctas_per_sm;
 };
 
 // ---- launchers (defined in the kernel translation units) -----------------

@@ -175,6 +175,18 @@ def test_multi_batch_graph_matches_single_batch_graphs(monkeypatch):
     assert np.array_equal(tables[0], tables[1])
 
 
+def test_five_cta_queue_reducer_gives_the_same_table(monkeypatch):
+    w = datagen.workload("cl10m", scale=0.005)
+    tables = []
+    for q in ("4", "5"):
+        monkeypatch.setenv("EP_QUEUE_CTAS", q)
+        ctx = _cl_ctx(w)
+        assert ctx.launch_shape()["queue_ctas_per_sm"] == int(q)
+        ctx.train_batches(29)
+        tables.append(ctx.get_table(w["n_feat"], w["ep"]["dims"]))
+    assert np.array_equal(tables[0], tables[1])
+
+
 @pytest.mark.parametrize("mode", ["0", "1", "3"])
 def test_adam_placements_give_the_same_table(monkeypatch, mode):
     # the fused form's Adam placements -- per row as each feature closes (0),
@@ -271,7 +283,7 @@ def test_autotune_picks_a_candidate_and_trains(form, level):
     w = datagen.workload("cl10m", scale=0.01)
     ctx = _cl_ctx(w, form=form, autotune=level)
     assert ctx.tuning()[0] is False
-    s1 = ctx.train_batches(170)          # the candidates' batches (150 at most), then more
+    s1 = ctx.train_batches(250)          # the candidates' batches (180 at most), then more
     shape = ctx.launch_shape()
     tuned, chunk, mode, _ = ctx.tuning()
     assert tuned and shape["tuned"] and shape["autotune"] == level
