@@ -226,12 +226,16 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
-def load_traffic(workload):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
-    summary (profiles/), or None."""
+def load_traffic(unique_rows):
+    """DRAM bytes per launch of the dominant kernel (the fused reducer) from
+    the committed ncu summary (profiles/traffic.json): the bytes measured on
+    a reduced workload of the same batch shape, plus each further unique row
+    of this batch at its Adam-state bytes (table row read and written, m and
+    v read and written).  None when there is no summary."""
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            return json.load(f).get(workload)
+            t = json.load(f)["k_reduce"]
+        return t["bytes_per_launch"] + (unique_rows - t["unique_rows"]) * t["bytes_per_extra_row"]
     except Exception:
         return None
 
@@ -462,7 +466,7 @@ def main():
     roofline = {"bound": "hbm", "kernel": kernel_of[rf_stage],
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)",
-                "traffic": load_traffic(args.workload), "alg_bytes_per_launch": stage_bytes[rf_stage],
+                "traffic": load_traffic(U) if split is False else None, "alg_bytes_per_launch": stage_bytes[rf_stage],
                 "stage_ms": stage_ms, "dominant_stage": dom,
                 "stage_gbs": {k: stage_bytes[k] / (stage_ms[k] / 1e3) / 1e9 for k in stage_bytes if stage_bytes[k]},
                 "step": {"achieved": step_bytes / (step_ms / 1e3) / 1e9, "alg_bytes_per_step": step_bytes,
