@@ -18,6 +18,11 @@ Legs in one run (rank 0, N=1):
                such passes)
   roofline     algorithmic bytes of the dominant stage / its mean CUDA-event
                duration from a stage-by-stage profile of the same batches
+  recall_at_10 held-out-edge recall@10 (scripts/evaluate.py:29-61) of the
+               fused, plain and CPU-restatement forms after one pass on the
+               same graph with 1% of its edges held out
+  largest      the 50M-node / ~1B-edge workload: fused and plain nodes/s
+               over a bounded run of batches
 
 ``--impl reference`` times only the CPU reference restatement (the Rust
 reference cannot be built here) and prints its own line.
