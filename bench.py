@@ -23,6 +23,8 @@ Legs in one run (rank 0, N=1):
                same graph with 1% of its edges held out
   largest      the 50M-node / ~1B-edge workload: fused and plain nodes/s
                over a bounded run of batches
+  plain_drop_in_cl1m  the 1M-node bipartite workload: plain FP32 and fused
+               nodes/s and the CPU restatement on the same graph
 
 ``--impl reference`` times only the CPU reference restatement (the Rust
 reference cannot be built here) and prints its own line.
@@ -98,7 +100,8 @@ def parse():
     p.add_argument("--recall-queries", type=int, default=20000)
     p.add_argument("--no-large", action="store_true", help="skip the 50M-node leg")
     p.add_argument("--large-steps", type=int, default=100)
-    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cl1m", action="store_true", help="skip the 1M-node bipartite leg")
     p.add_argument("--profile-steps", type=int, default=100)
     return p.parse_args()
 
@@ -342,6 +345,34 @@ def recall_leg(w, loss, queries):
     return out
 
 
+def cl1m_leg(loss, steps, warmup, world, cpu_seconds):
+    """The 1M-node bipartite Chung-Lu workload (weights U[1,5], dims 128, 25
+    neighbours, 10 negatives, batch 1024): PLAIN FP32 and FUSED nodes/s, and
+    the CPU restatement on a bounded sample, all on this graph."""
+    from cloverleaf_gb300 import datagen
+
+    w = datagen.workload("cl1m")
+    ep = w["ep"]
+    n = len(w["rows"]) - 1
+    out = {"workload": f"cl1m: bipartite Chung-Lu {n} nodes / {len(w['cols'])} directed edges, weights U[1,5], "
+                       f"dims {ep['dims']}, max_neighbors {ep['max_nodes']}, {ep['negatives']} negatives, "
+                       f"batch {ep['batch_size']}", "steps": steps, "warmup": warmup}
+    for form in ("plain", "fused"):
+        ctx, st, wall, _ = gpu_leg(w, form, loss, steps, warmup, world)
+        ctx.close()
+        ms = allmax(st["ms"], world)
+        out[form] = {"value": allsum(st["anchors"], world) / (ms / 1e3), "unit": UNIT,
+                     "ms_per_step": ms / max(st["batches"], 1)}
+    cv, cst, cores, nb = cpu_reference(w, loss, cpu_seconds)
+    out["cpu"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
+                  "sample": f"{cst.batches} batches of {ep['batch_size']} anchors, {cst.seconds:.1f}s"}
+    out["plain_vs_cpu"] = out["plain"]["value"] / cv
+    out["fused_vs_plain"] = out["fused"]["value"] / out["plain"]["value"]
+    log(f"[bench] cl1m: plain {out['plain']['value'] / 1e6:.2f} M, fused {out['fused']['value'] / 1e6:.2f} M, "
+        f"cpu {cv / 1e3:.1f} k nodes/s")
+    return out
+
+
 def large_leg(loss, steps, warmup, world):
     """The 50M-node / ~1B-edge Chung-Lu workload (dims 256, max_neighbors 32,
     16 negatives, batch 32768): fused and plain nodes/s over `steps` batches,
@@ -385,7 +416,9 @@ def cpu_reference(w, loss, seconds, threads=0, max_batches=None):
     args = (w["rows"], w["cols"], w["weights"], w["fptr"], w["fids"], w["n_feat"])
     cores = threads if threads > 0 else (os.cpu_count() or 1)
     if max_batches is None:
-        _, st = O.train(*args, max_batches=max(2, cores // 4), **kw)
+        # one batch per thread: the restatement runs batches concurrently, so
+        # fewer would leave threads idle and underestimate the rate
+        _, st = O.train(*args, max_batches=max(2, cores), **kw)
         rate = st.anchors / max(st.seconds, 1e-9)
         max_batches = max(cores, int(seconds * rate / ep["batch_size"]))
     _, st = O.train(*args, max_batches=max_batches, **kw)
@@ -546,10 +579,14 @@ def main():
             log(f"[bench] knn: {knn['tflops']:.1f} TFLOP/s ({knn['kernel_ms']:.2f} ms) = "
                 f"{100 * knn['frac']:.1f}% of {pk_bf16:.0f}")
         recall = None
-        if not args.no_recall:
+        single = args.workload == "cl10m" and args.scale == 1.0 and world == 1
+        if not args.no_recall and world == 1:
             recall = recall_leg(w, args.loss, args.recall_queries)
+        drop_in = None
+        if not args.no_cl1m and single:
+            drop_in = cl1m_leg(args.loss, 300, max(args.warmup, 3), world, 8.0)
         large = None
-        if not args.no_large and args.workload == "cl10m" and args.scale == 1.0 and world == 1:
+        if not args.no_large and single:
             del w
             _PINNED.clear()
             large = large_leg(args.loss, args.large_steps, max(args.warmup, 3), world)
@@ -560,7 +597,7 @@ def main():
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(st["launches"]),
                 "clocks": clocks, "plain_fp32": plain,
                 "speedup_vs_cpu": (value / cpu["value"]) if cpu else None,
-                "recall_at_10": recall, "largest": large,
+                "recall_at_10": recall, "largest": large, "plain_drop_in_cl1m": drop_in,
                 "eval_knn": knn}
         print(json.dumps(line), flush=True)
     return 0

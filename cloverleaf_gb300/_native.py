@@ -102,7 +102,7 @@ class EpLaunchShape(ctypes.Structure):
     _fields_ = [("chunk", ctypes.c_uint32), ("fused_mode", ctypes.c_int32), ("graph_batches", ctypes.c_uint32),
                 ("gather_ctas", ctypes.c_uint32), ("ring_reduce_warps", ctypes.c_uint32),
                 ("ring_adam_warps", ctypes.c_uint32), ("ring_slots", ctypes.c_uint32), ("ring_active", ctypes.c_int32),
-                ("queue_ctas_per_sm", ctypes.c_uint32), ("tuned", ctypes.c_int32), ("autotune", ctypes.c_int32)]
+                ("queue_ctas_per_sm", ctypes.c_uint32), ("gather_warps", ctypes.c_uint32), ("tuned", ctypes.c_int32), ("autotune", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -179,6 +179,7 @@ __global__ void k_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, ui
     st->bc2 = 1.f - powf(0.999f, t);
     st->n_items = 0;
     st->fwd_next = 0;
+    st->red_next = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1653,8 +1654,13 @@ static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s, int
         cudaFuncSetAttribute(k_fwd_gather_queue<T, A, VPL, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
     }
+    // the one-warp-per-anchor kernels in CTAs of gather_warps warps (1-8):
+    // smaller CTAs free their slots sooner when anchors differ in work
+    const uint32_t gw = p.gather_warps >= 1 && p.gather_warps <= (uint32_t)FWD_WARPS ? p.gather_warps : FWD_WARPS;
+    const uint32_t gblocks = (cap + gw - 1) / gw;
+    const size_t gsmem = sizeof(WarpTables) * gw;
     if (part == FWD_EMIT) {
-        launch_chain(k_fwd_emit<T, A, VPL>, blocks, 32 * FWD_WARPS, smem, s, p);
+        launch_chain(k_fwd_emit<T, A, VPL>, gblocks, 32 * gw, gsmem, s, p);
         return;
     }
     if (part != FWD_LOSS) {
@@ -1663,7 +1669,7 @@ static void fwd_launch(const ForwardParams& p, uint32_t cap, cudaStream_t s, int
         else if (p.gather_ctas)
             launch_chain(k_fwd_gather_queue<T, A, VPL, 2>, std::min(p.gather_ctas, blocks), 32 * FWD_WARPS, smem, s, p);
         else
-            launch_chain(k_fwd_gather<T, A, VPL, true>, blocks, 32 * FWD_WARPS, smem, s, p);
+            launch_chain(k_fwd_gather<T, A, VPL, true>, gblocks, 32 * gw, gsmem, s, p);
         launch_chain(k_fwd_gather<T, A, VPL, false>, blocks, 32 * FWD_WARPS, 0, s, p);
     }
     if (part != FWD_GATHER) launch_chain(k_fwd_loss<T, A, VPL>, (cap + 3) / 4, 128, 0, s, p);

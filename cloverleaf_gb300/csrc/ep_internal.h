@@ -54,6 +54,7 @@ struct BatchState {
     uint32_t error;         // ERR_* bits, sticky
     uint32_t n_items;       // items emitted by this batch
     uint32_t fwd_next;      // work queue of the persistent gather: next anchor to take (k_batch_begin zeroes it)
+    uint32_t red_next;      // work queue of the persistent reducer: next chunk to take (k_batch_begin zeroes it)
     float noise_sigma;      // gradient-noise scale of this step (0 = off)
     // per-batch outputs of k_batch_end
     float batch_err;        // sum(loss kept) / n_anchors (0 when none kept)
@@ -146,6 +147,7 @@ struct ForwardParams {
     int emit;                 // 0: forward only (validation)
     uint64_t items_cap;
     uint8_t* deferred;        // [n_anchors]: 1 = anchor left to the direct path
+    uint32_t gather_warps;    // warps per CTA of the one-warp-per-anchor gather and item emission (1-8; 0 = 8)
     uint32_t gather_ctas;     // staged gather: 0 = a warp per anchor; else this many persistent CTAs
                               // whose warps take anchors from BatchState::fwd_next
     // outputs
@@ -190,6 +192,9 @@ struct ReduceParams {
     uint32_t ring_pw, ring_cw, ring_slots;
     // OUT_QUEUE: resident CTAs per SM the reducer is compiled for (4 or 5)
     uint32_t queue_ctas_per_sm;
+    // 0: one warp per chunk (static stride); else a persistent grid of this
+    // many CTAs whose warps take chunks from BatchState::red_next
+    uint32_t red_ctas;
 };
 
 // ---- launchers (defined in the kernel translation units) -----------------

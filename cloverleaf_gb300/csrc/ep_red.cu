@@ -664,7 +664,18 @@ __device__ __forceinline__ void reduce_body(const ReduceParams& p) {
     const D* dir = std::is_same<D, A>::value ? (const D*)p.dir : (const D*)p.dir16;
     const A* scale = (const A*)p.scale;
     unsigned long long g_cnt = 0, u_cnt = 0;
-    for (uint32_t c = gw; c < nchunks; c += nw) {
+    // chunks: a static stride over the grid's warps, or, with a persistent
+    // grid (red_ctas > 0), the next chunk from the batch's work counter, so
+    // that a warp whose chunk finishes early takes another at once instead
+    // of idling until its CTA's other warps finish (the result is the same:
+    // every chunk is reduced alone, and the fix-ups combine them in order)
+    const bool take = MODE != OUT_RING && p.red_ctas != 0;
+    auto next_chunk = [&]() {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(&p.st->red_next, 1u);
+        return __shfl_sync(FULL, t, 0);
+    };
+    for (uint32_t c = take ? next_chunk() : gw; c < nchunks; c = take ? next_chunk() : c + nw) {
         const uint32_t i0 = c * C, i1 = min(i0 + C, M);
         uint32_t cur_f = p.skey[i0];
         const bool head_partial = i0 > 0 && p.skey[i0 - 1] == cur_f;
@@ -1111,10 +1122,12 @@ static void red_launch(const ReduceParams& p, uint64_t cap, cudaStream_t s, int 
     if (which == 0) {
         uint32_t ctas = (warps + RED_THREADS / 32 - 1) / (RED_THREADS / 32);
         if (ctas > RED_MAX_CTAS) ctas = RED_MAX_CTAS;
+        if (p.red_ctas) ctas = std::min<uint32_t>(ctas, p.red_ctas);
         if (p.out_mode == OUT_DENSE) launch_chain(k_reduce<T, A, VPL, OUT_DENSE>, ctas, RED_THREADS, 0, s, p);
         else if (p.out_mode == OUT_QUEUE) {
             uint32_t qctas = (warps + QUEUE_THREADS / 32 - 1) / (QUEUE_THREADS / 32);
             if (qctas > 2 * RED_MAX_CTAS) qctas = 2 * RED_MAX_CTAS;
+            if (p.red_ctas) qctas = std::min(qctas, p.red_ctas);
             bool q5 = false;
             if constexpr (VPL <= 8) {
                 if (p.queue_ctas_per_sm >= 5) {

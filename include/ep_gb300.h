@@ -256,6 +256,7 @@ typedef struct ep_launch_shape {
     uint32_t ring_reduce_warps, ring_adam_warps, ring_slots;
     int32_t ring_active;         /* the FUSED form reduces through the ring */
     uint32_t queue_ctas_per_sm;  /* the queue reducer's resident CTAs per SM (4 or 5) */
+    uint32_t gather_warps;       /* warps per CTA of the one-warp-per-anchor gather */
     int32_t tuned;               /* the autotuner has made its choice */
     int32_t autotune;            /* the tuning level in effect */
 } ep_launch_shape;

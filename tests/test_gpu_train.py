@@ -175,6 +175,35 @@ def test_multi_batch_graph_matches_single_batch_graphs(monkeypatch):
     assert np.array_equal(tables[0], tables[1])
 
 
+@pytest.mark.parametrize("form", [_native.FORM_FUSED_BF16, _native.FORM_PLAIN_FP32])
+@pytest.mark.parametrize("ctas", ["1", "608"])
+def test_persistent_reducer_gives_the_same_table(monkeypatch, form, ctas):
+    # warps taking reducer chunks from a work counter (down to a single CTA)
+    # reduce every chunk as the one-warp-per-chunk grid does
+    w = datagen.workload("cl10m", scale=0.005)
+    tables = []
+    for r in ("0", ctas):
+        monkeypatch.setenv("EP_RED_CTAS", r)
+        ctx = _cl_ctx(w, form=form)
+        st = ctx.train_batches(23)
+        assert st["kept_anchors"] > 0
+        tables.append(ctx.get_table(w["n_feat"], w["ep"]["dims"]))
+    assert np.array_equal(tables[0], tables[1])
+
+
+@pytest.mark.parametrize("warps", ["1", "2", "4"])
+def test_gather_cta_size_gives_the_same_table(monkeypatch, warps):
+    w = datagen.workload("cl10m", scale=0.005)
+    tables = []
+    for g in ("8", warps):
+        monkeypatch.setenv("EP_GATHER_WARPS", g)
+        for graphs in (1, 0):
+            ctx = _cl_ctx_cfg(w, use_graphs=graphs)
+            ctx.train_batches(19)
+            tables.append(ctx.get_table(w["n_feat"], w["ep"]["dims"]))
+    assert all(np.array_equal(tables[0], t) for t in tables[1:])
+
+
 def test_five_cta_queue_reducer_gives_the_same_table(monkeypatch):
     w = datagen.workload("cl10m", scale=0.005)
     tables = []
@@ -283,14 +312,14 @@ def test_autotune_picks_a_candidate_and_trains(form, level):
     w = datagen.workload("cl10m", scale=0.01)
     ctx = _cl_ctx(w, form=form, autotune=level)
     assert ctx.tuning()[0] is False
-    s1 = ctx.train_batches(250)          # the candidates' batches (180 at most), then more
+    s1 = ctx.train_batches(260)          # the candidates' batches (200 at most), then more
     shape = ctx.launch_shape()
     tuned, chunk, mode, _ = ctx.tuning()
     assert tuned and shape["tuned"] and shape["autotune"] == level
     assert chunk == 128 if level == 1 else chunk in (64, 128, 256)
     if form == _native.FORM_FUSED_BF16:
         assert mode in ((2, 3) if level == 1 else (1, 2, 3))
-    assert shape["gather_ctas"] in (0, 304, 456)
+    assert shape["gather_ctas"] in (0, 304, 456) and shape["gather_warps"] in (2, 4, 8)
     ctx.train_batches(120)
     s2 = ctx.train_batches(10)
     assert s2["train_loss"] < s1["train_loss"]
