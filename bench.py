@@ -59,6 +59,21 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+def loaded_libraries():
+    """Base names of this repository's shared libraries mapped into the
+    process (the trainer, the workload generators, the oracle)."""
+    names = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if len(line.split()) >= 6 else ""
+                if path.startswith(ROOT) and path.endswith(".so"):
+                    names.add(os.path.relpath(path, ROOT))
+    except OSError:
+        pass
+    return sorted(names)
+
+
 def cpu_model() -> str:
     """The host CPU's model name (lscpu, else /proc/cpuinfo, else platform)."""
     try:
@@ -459,7 +474,8 @@ def main():
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": "port",
                                  "sample": f"{st.batches} batches of {ep['batch_size']} anchors "
                                            f"({st.anchors} anchors) of the {args.workload} workload"},
-                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "loaded_libraries": loaded_libraries()}
         print(json.dumps(line), flush=True)
         return 0
 
@@ -598,6 +614,7 @@ def main():
                 "clocks": clocks, "plain_fp32": plain,
                 "speedup_vs_cpu": (value / cpu["value"]) if cpu else None,
                 "recall_at_10": recall, "largest": large, "plain_drop_in_cl1m": drop_in,
+                "loaded_libraries": loaded_libraries(),
                 "eval_knn": knn}
         print(json.dumps(line), flush=True)
     return 0
