@@ -112,6 +112,8 @@ struct ep_ctx {
     // their slots sooner when anchors differ in work (2: forward 0.164 ->
     // 0.150 ms per batch on the 10M-node graph)
     uint32_t gather_warps = 2;
+    // warps per CTA of the sampler (1-8)
+    uint32_t sample_warps = 8;
     bool tuned = false;         // autotuner has chosen chunk / fused_mode
     bool prepared = false;
     cudaGraphExec_t gexec = nullptr;
@@ -277,6 +279,7 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
     if (const char* e = getenv("EP_QUEUE_CTAS")) { const long v = atol(e); if (v == 4 || v == 5) c->queue_ctas = (uint32_t)v; }
     if (const char* e = getenv("EP_RED_CTAS")) { const long v = atol(e); if (v >= 0 && v <= 65536) c->red_ctas = (uint32_t)v; }
     if (const char* e = getenv("EP_GATHER_WARPS")) { const long v = atol(e); if (v >= 1 && v <= 8) c->gather_warps = (uint32_t)v; }
+    if (const char* e = getenv("EP_SAMPLE_WARPS")) { const long v = atol(e); if (v >= 1 && v <= 8) c->sample_warps = (uint32_t)v; }
     // a launch shape set by hand is used as given: no tuning
     for (const char* k : {"EP_FUSED_MODE", "EP_REDUCE_CHUNK", "EP_GATHER_CTAS", "EP_QUEUE_CTAS", "EP_RED_CTAS", "EP_GATHER_WARPS", "EP_RING_PW",
                           "EP_RING_CW", "EP_RING_SLOTS"})
@@ -666,6 +669,7 @@ static SampleParams sample_params(ep_ctx* c, BatchState* st, bool eval, int inje
     sp.pool = sp.order;
     sp.n_pool = sp.n_order;
     sp.batch_cap = injected ? c->buf_B : c->Bcap;
+    sp.sample_warps = c->sample_warps;
     sp.injected = injected;
     sp.eval = eval;
     sp.feistel_half = feistel_half(sp.n_order);

@@ -1634,8 +1634,10 @@ void launch_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, uint32_t
 }
 
 void launch_sample(const SampleParams& p, cudaStream_t s) {
-    const uint32_t blocks = (p.batch_cap + 7) / 8;
-    launch_chain(k_sample, blocks, 256, 0, s, p);
+    // warp per anchor in CTAs of sample_warps warps (1-8; 0 = 8)
+    const uint32_t w = p.sample_warps >= 1 && p.sample_warps <= 8 ? p.sample_warps : 8;
+    const uint32_t blocks = (p.batch_cap + w - 1) / w;
+    launch_chain(k_sample, blocks, 32 * w, 0, s, p);
 }
 
 void launch_scan_occ(BatchState* st, uint32_t* occ, uint32_t cap, uint64_t items_cap, cudaStream_t s) {

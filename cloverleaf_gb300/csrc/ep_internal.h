@@ -109,6 +109,7 @@ struct SampleParams {
     const uint32_t* pool;   // negative pool (train or valid ids)
     uint32_t n_pool;
     uint32_t batch_cap;     // anchors per batch
+    uint32_t sample_warps;  // warps per CTA (1-8; 0 = 8)
     int injected;           // 1: samples provided by the host (only count);
                             // 2: anchors provided, neighbours and negatives sampled
     int eval;               // validation: fixed sampling stream, no shuffle
