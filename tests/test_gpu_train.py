@@ -191,6 +191,18 @@ def test_persistent_reducer_gives_the_same_table(monkeypatch, form, ctas):
     assert np.array_equal(tables[0], tables[1])
 
 
+@pytest.mark.parametrize("warps", ["1", "2"])
+def test_sampler_cta_size_gives_the_same_table(monkeypatch, warps):
+    w = datagen.workload("cl10m", scale=0.005)
+    tables = []
+    for g in ("8", warps):
+        monkeypatch.setenv("EP_SAMPLE_WARPS", g)
+        ctx = _cl_ctx(w)
+        ctx.train_batches(19)
+        tables.append(ctx.get_table(w["n_feat"], w["ep"]["dims"]))
+    assert np.array_equal(tables[0], tables[1])
+
+
 @pytest.mark.parametrize("warps", ["1", "2", "4"])
 def test_gather_cta_size_gives_the_same_table(monkeypatch, warps):
     w = datagen.workload("cl10m", scale=0.005)
