@@ -549,11 +549,13 @@ def main():
             est = ectx.train(1)[0]
             t.append(time.perf_counter())
             table = ectx.get_table(w["n_feat"], d, out=out)
+            t.append(time.perf_counter())
             ectx.close()
             t.append(time.perf_counter())
             secs.append(allmax(t[-1] - t[0], world))
             phases.append({"setup": round(t[1] - t[0], 4), "train": round(t[2] - t[1], 4),
-                           "download_close": round(t[3] - t[2], 4), "train_device_ms": round(est["ms"], 2)})
+                           "download": round(t[3] - t[2], 4), "close": round(t[4] - t[3], 4),
+                           "train_device_ms": round(est["ms"], 2)})
         e_sec = float(np.median(secs))
         h2d = sum(w[k].nbytes for k in ("rows", "cols", "weights", "fptr", "fids"))
         nb = max(est["batches"], 1)
