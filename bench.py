@@ -351,6 +351,10 @@ def recall_leg(w, loss, queries):
                         negatives=ep["negatives"], batch_size=ep["batch_size"], passes=ep["passes"],
                         max_nodes=(O.SAMPLE_FIXED, float(ep["max_nodes"])), threads=0)
     out["cpu_train_seconds"] = round(time.time() - t1, 1)
+    # the CPU restatement over one whole pass (all host threads): its rate
+    # over the pass's timed region, next to the bounded sample of cpu_baseline
+    out["cpu_full_pass"] = {"value": st.anchors / max(st.seconds, 1e-9), "unit": UNIT, "anchors": int(st.anchors),
+                            "seconds": round(st.seconds, 2)}
     out["cpu"] = evaluate.heldout_recall(w["fptr"], w["fids"], table, test)
     del table
     for form in ("fused", "plain"):

@@ -23,6 +23,7 @@
 // (no Adam step), as in mod.rs:223-233.
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
 
 #include "ep_device.cuh"
@@ -1214,11 +1215,21 @@ static cudaError_t fixl_setup_all() {
 
 // Opts the long-span fixup kernels in to their dynamic shared memory (one row
 // per warp, up to 64 KB); called at context creation, outside any capture.
+// Once per device (the current one): later contexts on it skip the calls.
 cudaError_t reduce_kernels_setup() {
-    cudaError_t e = fixl_setup_all<float, float>();
+    static std::mutex mu;
+    static bool done[256] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 256 && done[dev]) return cudaSuccess;
+    e = fixl_setup_all<float, float>();
     const cudaError_t b = fixl_setup_all<__nv_bfloat16, float>();
     const cudaError_t d = fixl_setup_all<double, double>();
-    return e != cudaSuccess ? e : (b != cudaSuccess ? b : d);
+    e = e != cudaSuccess ? e : (b != cudaSuccess ? b : d);
+    if (e == cudaSuccess && dev >= 0 && dev < 256) done[dev] = true;
+    return e;
 }
 
 template <typename T, typename A>
