@@ -30,6 +30,10 @@ def _check_line(d: dict, n_gpus: int):
     e = d["e2e"]
     assert e["value"] == d["value"] and e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
     assert d["config"]["workload"].startswith("sbm10k: SBM")
+    # the reference arm runs none of the trainer's code: it loads the
+    # workload generators and the oracle only
+    libs = d["loaded_libraries"]
+    assert "oracle/_build/libep_oracle.so" in libs and not any("libep_gb300" in x for x in libs), libs
 
 
 def test_reference_arm_line():
