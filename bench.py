@@ -438,10 +438,19 @@ def cpu_reference(w, loss, seconds, threads=0, max_batches=None):
         # one batch per thread: the restatement runs batches concurrently, so
         # fewer would leave threads idle and underestimate the rate
         _, st = O.train(*args, max_batches=max(2, cores), **kw)
-        rate = st.anchors / max(st.seconds, 1e-9)
+        rate = cpu_rate(st)
         max_batches = max(cores, int(seconds * rate / ep["batch_size"]))
     _, st = O.train(*args, max_batches=max_batches, **kw)
-    return st.anchors / st.seconds, st, cores, max_batches
+    return cpu_rate(st), st, cores, max_batches
+
+
+def cpu_rate(st):
+    """Anchors per second of a run of the CPU restatement.  A bounded sample
+    of b batches stands for b / steps_per_pass of a pass, so it carries that
+    share of the pass's one shuffle of the anchor order (mod.rs:173), not all
+    of it."""
+    share = min(1.0, st.batches / max(st.steps_per_pass, 1))
+    return st.anchors / max(st.seconds - st.shuffle_seconds * (1.0 - share), 1e-9)
 
 
 def main():
@@ -472,7 +481,7 @@ def main():
         _, stw, _, _ = cpu_reference(w, args.loss, 0, max_batches=max(args.warmup, 1))
         value, st, cores, nb = cpu_reference(w, args.loss, 0, max_batches=max(args.steps, 1))
         line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": nb, "warmup": args.warmup, "ms_per_step": 1e3 * st.seconds / max(st.batches, 1),
+                "steps": nb, "warmup": args.warmup, "ms_per_step": 1e3 * st.anchors / value / max(st.batches, 1),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic", "config": dict(config, table_dtype="f32"),
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": "port",

@@ -530,9 +530,12 @@ int orc_train(const uint64_t* rows, const uint32_t* cols, const float* wcdf,
 #else
     nthreads = 1;
 #endif
+    double shuffle_s = 0.0;
     double t0 = now_s();
     for (uint32_t pass = 1; pass <= cfg->passes && batches_left > 0; ++pass) {
+        const double ts0 = now_s();
         shuffle_u32(train, n_train, &master);
+        shuffle_s += now_s() - ts0;
         uint64_t nb = steps < batches_left ? steps : batches_left;
         double err_sum = 0.0;
         uint64_t err_cnt = 0;
@@ -626,6 +629,8 @@ int orc_train(const uint64_t* rows, const uint32_t* cols, const float* wcdf,
     double t1 = now_s();
     if (stats) {
         stats->seconds = t1 - t0;
+        stats->shuffle_seconds = shuffle_s;
+        stats->steps_per_pass = steps;
         stats->anchors = anchors_done;
         stats->batches = batches_done;
         stats->last_train_loss = last_err;

@@ -125,6 +125,8 @@ typedef struct orc_train_stats {
     uint64_t batches;
     float last_train_loss;
     float last_valid_loss;
+    double shuffle_seconds;  /* of `seconds`, spent shuffling the pass order (once per pass) */
+    uint64_t steps_per_pass; /* batches of a full pass */
 } orc_train_stats;
 
 /* The whole learn_feature_embeddings loop (mod.rs:92-287): seeded init,

@@ -90,6 +90,8 @@ class TrainStats(ctypes.Structure):
         ("batches", ctypes.c_uint64),
         ("last_train_loss", ctypes.c_float),
         ("last_valid_loss", ctypes.c_float),
+        ("shuffle_seconds", ctypes.c_double),
+        ("steps_per_pass", ctypes.c_uint64),
     ]
 
 
