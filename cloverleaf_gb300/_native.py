@@ -161,6 +161,7 @@ SIGNATURES = {
     "ep_get_split": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(_U32), ctypes.POINTER(_U32)]),
     "ep_get_launch_shape": (ctypes.c_int, [_P, _P]),
     "ep_sample_validation": (ctypes.c_int, [_P, _U32, _U32, _U32, _P, _P, _P, _P, _P]),
+    "ep_selftest_stochastic_rounding": (ctypes.c_int, [ctypes.c_int, _U64, _U64, ctypes.POINTER(_U64)]),
     "ep_synchronize": (ctypes.c_int, [_P]),
     "ep_last_error": (ctypes.c_char_p, [_P]),
     "ep_destroy": (None, [_P]),
@@ -589,6 +590,15 @@ def _line(buf: bytes, k: int) -> bytes:
             if k == 0:
                 return line.rstrip(b"\r")
     return b""
+
+
+def selftest_stochastic_rounding(n=1 << 24, seed=1, device=0) -> int:
+    """Pairs (of n) whose hardware stochastic rounding to BF16 differs from
+    the bit rule it stands for (ep_selftest_stochastic_rounding); 0 expected."""
+    out = _U64(0)
+    check(lib().ep_selftest_stochastic_rounding(int(device), int(n), int(seed), ctypes.byref(out)), None,
+          "ep_selftest_stochastic_rounding")
+    return int(out.value)
 
 
 def _knn_check(rc, what):

@@ -235,4 +235,17 @@ __device__ __forceinline__ __nv_bfloat16 bf16_stochastic(float x, uint32_t r16) 
     return __ushort_as_bfloat16((unsigned short)(b >> 16));
 }
 
+// The same rounding of an element pair in one instruction: sm_100-family
+// stochastic-rounding conversion (PTX cvt.rs.bf16x2.f32).  Returns the pair
+// packed as stored (lo in the low half); lo takes rbits[15:0] and hi
+// rbits[31:16] as its 16 random bits, so the result equals
+// {bf16_stochastic(hi, rbits >> 16), bf16_stochastic(lo, rbits & 0xffff)}
+// bit for bit, NaN, infinities and subnormals included
+// (ep_selftest_stochastic_rounding checks this on the device).
+__device__ __forceinline__ uint32_t bf16x2_stochastic(float lo, float hi, uint32_t rbits) {
+    uint32_t d;
+    asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+    return d;
+}
+
 }  // namespace ep

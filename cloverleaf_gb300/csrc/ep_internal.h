@@ -239,6 +239,6 @@ cudaError_t reduce_kernels_setup();
 // 16-byte multiples, and the ring's shared memory fits), and the ring's
 // shared memory per CTA.
 bool ring_supported(int tt, uint32_t dpad, uint32_t pw, uint32_t cw, uint32_t slots);
-size_t ring_smem_bytes(int tt, uint32_t dpad, uint32_t slots);
+size_t ring_smem_bytes(int tt, uint32_t dpad, uint32_t pw, uint32_t slots);
 
 }  // namespace ep

@@ -29,6 +29,7 @@
 #include "ep_device.cuh"
 #include "ep_internal.h"
 #include "ep_launch.cuh"
+#include "ep_gb300.h"
 
 namespace ep {
 
@@ -71,11 +72,18 @@ struct AdamStep {
 
 // Square root of Adam's second-moment estimate on the SFU (PTX sqrt.approx:
 // relative error within a few units of 2^-23); the denominator sqrt(v) + eps
-// tolerates that, as it tolerates the fast divide.
+// tolerates that, as it tolerates the fast divide.  Both flush subnormal
+// inputs to zero (.ftz): a subnormal second moment (below 1.2e-38) then gives
+// the denominator eps, as its square root (below 1.1e-19) added to eps would.
 __device__ __forceinline__ float sqrt_sfu(float x) {
     float y;
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
+}
+__device__ __forceinline__ float div_sfu(float x, float y) {
+    float q;
+    asm("div.approx.ftz.f32 %0, %1, %2;" : "=f"(q) : "f"(x), "f"(y));
+    return q;
 }
 
 // Adam on one row (optimizer.rs:43-81): t = pass + 1, beta1 0.9, beta2 0.999,
@@ -123,8 +131,8 @@ __device__ __forceinline__ void adam_apply(T* __restrict__ table, float* __restr
             const float2 v2 = __ffma2_rn(B2, make_float2(vv[k], vv[k + 1]), __fmul2_rn(C2, __fmul2_rn(g, g)));
             const float2 mh = __fmul2_rn(m2, R1), vh = __fmul2_rn(v2, R2);
             const float2 den = __fadd2_rn(make_float2(sqrt_sfu(vh.x), sqrt_sfu(vh.y)), E);
-            // the denominator is >= eps = 1e-8, inside __fdividef's full-accuracy range
-            const float2 q = make_float2(__fdividef(mh.x, den.x), __fdividef(mh.y, den.y));
+            // the denominator is >= eps = 1e-8, inside the fast divide's full-accuracy range
+            const float2 q = make_float2(div_sfu(mh.x, den.x), div_sfu(mh.y, den.y));
             const float2 e2 = __ffma2_rn(NL, q, make_float2(ee[k], ee[k + 1]));
             mm[k] = m2.x; mm[k + 1] = m2.y;
             vv[k] = v2.x; vv[k + 1] = v2.y;
@@ -138,7 +146,7 @@ __device__ __forceinline__ void adam_apply(T* __restrict__ table, float* __restr
             vv[k] = fmaf(b2, vv[k], (1.f - b2) * (gk * gk));
             const float mh = mm[k] * rb1;
             const float vh = vv[k] * rb2;
-            ee[k] = fmaf(-lr, __fdividef(mh, sqrt_sfu(vh) + eps), ee[k]);
+            ee[k] = fmaf(-lr, div_sfu(mh, sqrt_sfu(vh) + eps), ee[k]);
         }
     }
     RowIO<float, VPL>::store_raw(m + o, lane, mm);
@@ -148,16 +156,20 @@ __device__ __forceinline__ void adam_apply(T* __restrict__ table, float* __restr
     } else {
         // BF16 table: stochastic rounding, 16 random bits per element; one
         // 32-bit hash (murmur3 finalizer of the element pair's coordinates
-        // row, step, column) per pair of elements.
-        __nv_bfloat16 out[VPL];
+        // row, step, column) per pair of elements, rounded by one
+        // stochastic-rounding conversion per pair.
+        union {
+            uint32_t w[(VPL + 1) / 2];
+            __nv_bfloat16 b[VPL];
+        } out;
         const uint32_t key = (uint32_t)seed ^ (uint32_t)(seed >> 32) ^ (f * 0x9E3779B1u) ^ (step * 0x85EBCA77u);
 #pragma unroll
         for (int k = 0; k < VPL; k += 2) {
             const uint32_t h = mix32(key ^ ((uint32_t)(lane * VPL + k) * 0xC2B2AE3Du));
-            out[k] = bf16_stochastic(ee[k], h & 0xffffu);
-            if (k + 1 < VPL) out[k + 1] = bf16_stochastic(ee[k + 1], h >> 16);
+            if (k + 1 < VPL) out.w[k / 2] = bf16x2_stochastic(ee[k], ee[k + 1], h);
+            else out.b[k] = bf16_stochastic(ee[k], h & 0xffffu);
         }
-        RowIO<__nv_bfloat16, VPL>::store_raw(table + o, lane, out);
+        RowIO<__nv_bfloat16, VPL>::store_raw(table + o, lane, out.b);
     }
 }
 
@@ -205,7 +217,7 @@ __device__ __forceinline__ void fin_flush(const ReduceParams& p, uint32_t* fin, 
 // flight when the oldest slot is updated, so the update reads everything from
 // shared memory and rarely waits.  Each lane copies and later reads only its
 // own slices, so the per-thread cp.async groups order everything it needs.
-constexpr uint32_t QN = 3;
+constexpr uint32_t QN = 2;
 constexpr int QUEUE_THREADS = 128;
 
 template <typename T>
@@ -580,6 +592,33 @@ __device__ __forceinline__ void ring_finish(const ReduceParams& p, RingHdr* rh) 
     }
 }
 
+// Per-warp lists of one window of RW sorted items, built by the warp's lanes
+// in parallel and then walked in order: the kept items (direction row and
+// weight) and the feature segments that start in the window (feature id and
+// the number of kept items before it).  Walking the list costs one broadcast
+// shared-memory load per kept item instead of a search of the batch's masks
+// and two shuffles, and the direction rows of NF consecutive kept items are
+// in flight together across feature boundaries.
+constexpr uint32_t RW = 128;
+
+template <typename A>
+struct RedEntry {
+    uint32_t src;   // role row of the direction buffer
+    A w;            // count weight x role scale
+};
+
+template <typename A>
+__host__ __device__ constexpr size_t list_bytes() {
+    return RW * (sizeof(RedEntry<A>) + sizeof(uint2));
+}
+
+// Offset of the lists in the reducer's dynamic shared memory (after the
+// OUT_QUEUE slots and their ids, or the OUT_RING header and slots).
+template <typename T>
+__host__ __device__ constexpr size_t queue_list_offset(uint32_t dpad, uint32_t warps) {
+    return ((size_t)warps * QN * (queue_slot_bytes<T>(dpad) + sizeof(uint32_t)) + 15) & ~(size_t)15;
+}
+
 template <typename T, typename A, int VPL, int MODE>
 __device__ __forceinline__ void reduce_body(const ReduceParams& p);
 
@@ -606,7 +645,7 @@ __device__ __forceinline__ void reduce_body(const ReduceParams& p) {
     using IO = RowIO<D, VPL>;
     // rows in flight: about 24-32 registers of raw data in the rows-only mode,
     // fewer where a finished row is updated in place while others are in flight
-    constexpr int NF = MODE == OUT_DENSE ? (sizeof(D) == 2 ? 4 : 3) : 2;
+    constexpr int NF = MODE == OUT_DENSE ? (sizeof(D) == 2 ? 4 : 3) : (MODE == OUT_QUEUE ? 3 : 2);
     __shared__ uint32_t fin_all[MODE == OUT_DENSE ? RED_THREADS / 32 : 1][FIN_CAP];
     extern __shared__ __align__(16) unsigned char red_queue[];   // OUT_QUEUE: [warps][QN] slots, then ids
     const int lane = threadIdx.x & 31;
@@ -621,6 +660,16 @@ __device__ __forceinline__ void reduce_body(const ReduceParams& p) {
     RingHdr* rh = reinterpret_cast<RingHdr*>(red_queue);
     unsigned char* ring_slots = red_queue + ring_hdr_bytes();
     const uint32_t warp = threadIdx.x >> 5;
+    RedEntry<A>* ents;
+    uint2* segs;
+    {
+        size_t off = 0;
+        if constexpr (MODE == OUT_QUEUE) off = queue_list_offset<T>(p.dpad, blockDim.x >> 5);
+        if constexpr (MODE == OUT_RING) off = ring_hdr_bytes() + (size_t)p.ring_slots * ring_slot_bytes<T>(p.dpad);
+        unsigned char* lb = red_queue + off + (size_t)warp * list_bytes<A>();
+        ents = reinterpret_cast<RedEntry<A>*>(lb);
+        segs = reinterpret_cast<uint2*>(lb + RW * sizeof(RedEntry<A>));
+    }
     if constexpr (MODE == OUT_RING) {
         if (threadIdx.x == 0) {
             for (uint32_t i = 0; i < p.ring_slots; ++i) {
@@ -654,6 +703,9 @@ __device__ __forceinline__ void reduce_body(const ReduceParams& p) {
     const uint32_t nchunks = (M + C - 1) / C;
     const uint32_t NR = p.NR;
     const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
+    // lanes past the row (dims < 32 x VPL) read its last slice and accumulate
+    // what no store uses, so that the item loop has no lane-dependent branch
+    const int lane_ld = lane_on ? lane : (int)(p.dpad / VPL) - 1;
     const AdamStep as = AdamStep::load(p.st);
     if constexpr (MODE == OUT_RING) {
         if (warp >= p.ring_pw) {
@@ -744,123 +796,142 @@ __device__ __forceinline__ void reduce_body(const ReduceParams& p) {
                 sc0 = scale[s0];
             }
         }
-        for (uint32_t ib = i0; ib < i1; ib += 32) {
-            const uint32_t i = ib + lane;
-            const bool act = i < i1;
-            const uint32_t f = f0, s = s0;
-            const float cf = c0;
-            const bool v = v0;
-            const A sc = sc0;
-            // next batch's role flags and scales; the batch after's keys
-            bool v1 = false;
-            A sc1 = 0;
-            uint32_t f2 = NONE, s2 = 0;
-            float c2 = 0.f;
-            if (ib + 32 + lane < i1) {
-                v1 = p.valid[s1] != 0;
-                sc1 = scale[s1];
-            }
-            if (ib + 64 + lane < i1) {
-                const uint32_t j = ib + 64 + lane;
-                f2 = p.skey[j];
-                const uint2 sv = p.sval[j];
-                s2 = sv.x;
-                c2 = __uint_as_float(sv.y);
-            }
-            if constexpr (MODE == OUT_ADAM) prefetch_segment_state<T>(p, ib + 32, i1, lane);
-            const uint32_t anchor = s / NR;
-            // predecessor of each lane (lane 0: the carried item before the batch)
-            uint32_t pf = __shfl_up_sync(FULL, f, 1), pa = __shfl_up_sync(FULL, anchor, 1);
-            uint32_t ps = __shfl_up_sync(FULL, s, 1);
-            if (lane == 0) { pf = prev_f; pa = prev_anchor; ps = prev_src; }
-            const bool seg_start = act && f != pf;
-            const bool grp_start = act && (seg_start || anchor != pa);
-            if (act) g_cnt += (seg_start || s != ps);
-            const unsigned SS = __ballot_sync(FULL, seg_start);
-            const unsigned GS = __ballot_sync(FULL, grp_start);
-            const unsigned V = __ballot_sync(FULL, act && v);
-            bool keep;
-            if (p.grad_true) {
-                keep = act && v;
-            } else {
-                // lanes of this item's group up to and including itself
-                const unsigned gs_le = GS & (lt_mask | (1u << lane));
-                const int gstart = gs_le ? 31 - __clz(gs_le) : -1;
-                const unsigned grp = (lt_mask | (1u << lane)) & (gstart >= 0 ? ~((1u << gstart) - 1u) : FULL);
-                const unsigned vg = V & grp;
-                const int fv = vg ? __ffs(vg) - 1 : 0;
-                const uint32_t src_fv = __shfl_sync(FULL, s, fv);
-                uint32_t ch = NONE;
-                if (gstart < 0 && chosen != NONE) ch = chosen;      // group began before this batch
-                else if (vg) ch = src_fv;
-                keep = act && v && s == ch;
-                // carry the group state of the batch's last item
-                const int lastl = 31 - __clz(__ballot_sync(FULL, act));
-                chosen = __shfl_sync(FULL, ch, lastl);
-            }
-            const A w = keep ? (A)cf * sc : (A)0;
-            unsigned pend = __ballot_sync(FULL, keep);
-            unsigned starts = SS;
-            const int last = 31 - __clz(__ballot_sync(FULL, act));
-
-            // closes the open feature (finished here, or a head partial for
-            // the fix-up) and opens the one starting at lane lo
-            auto close_open = [&](int lo) {
-                if (started_here) {
-                    if (any_kept) {
-                        finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, as, fin, n_fin, &q, rh, ring_slots);
-                        ++u_cnt;
-                    }
-                } else {
-                    if (lane_on) store_row<A, VPL, A>((A*)p.carry_head + (uint64_t)c * p.dpad, lane, acc);
-                    flags |= CF_HEAD | (any_kept ? CF_HEAD_KEPT : 0u);
+        // closes the open feature (finished here, or a head partial for the
+        // fix-up) and opens feature fnew
+        auto close_open = [&](uint32_t fnew) {
+            if (started_here) {
+                if (any_kept) {
+                    finish_row<T, A, VPL, MODE>(p, cur_f, acc, lane, lane_on, as, fin, n_fin, &q, rh, ring_slots);
+                    ++u_cnt;
                 }
+            } else {
+                if (lane_on) store_row<A, VPL, A>((A*)p.carry_head + (uint64_t)c * p.dpad, lane, acc);
+                flags |= CF_HEAD | (any_kept ? CF_HEAD_KEPT : 0u);
+            }
 #pragma unroll
-                for (int k = 0; k < VPL; ++k) acc[k] = 0;
-                started_here = true;
-                any_kept = false;
-                cur_f = __shfl_sync(FULL, f, lo);
-            };
-            while (pend) {
+            for (int k = 0; k < VPL; ++k) acc[k] = 0;
+            started_here = true;
+            any_kept = false;
+            cur_f = fnew;
+        };
+        for (uint32_t wb = i0; wb < i1; wb += RW) {
+            const uint32_t we = min(wb + RW, i1);
+            // phase 1, 32 items per step with the lanes in parallel: which
+            // items are kept, their weights, where features start; appended
+            // to the window's lists
+            uint32_t nk = 0, ns = 0;
+            for (uint32_t ib = wb; ib < we; ib += 32) {
+                const uint32_t i = ib + lane;
+                const bool act = i < i1;
+                const uint32_t f = f0, s = s0;
+                const float cf = c0;
+                const bool v = v0;
+                const A sc = sc0;
+                // next batch's role flags and scales; the batch after's keys
+                bool v1 = false;
+                A sc1 = 0;
+                uint32_t f2 = NONE, s2 = 0;
+                float c2 = 0.f;
+                if (ib + 32 + lane < i1) {
+                    v1 = p.valid[s1] != 0;
+                    sc1 = scale[s1];
+                }
+                if (ib + 64 + lane < i1) {
+                    const uint32_t j = ib + 64 + lane;
+                    f2 = p.skey[j];
+                    const uint2 sv = p.sval[j];
+                    s2 = sv.x;
+                    c2 = __uint_as_float(sv.y);
+                }
+                if constexpr (MODE == OUT_ADAM) prefetch_segment_state<T>(p, ib + 32, i1, lane);
+                const uint32_t anchor = s / NR;
+                // predecessor of each lane (lane 0: the carried item before the batch)
+                uint32_t pf = __shfl_up_sync(FULL, f, 1), pa = __shfl_up_sync(FULL, anchor, 1);
+                uint32_t ps = __shfl_up_sync(FULL, s, 1);
+                if (lane == 0) { pf = prev_f; pa = prev_anchor; ps = prev_src; }
+                const bool seg_start = act && f != pf;
+                const bool grp_start = act && (seg_start || anchor != pa);
+                if (act) g_cnt += (seg_start || s != ps);
+                const unsigned GS = __ballot_sync(FULL, grp_start);
+                const unsigned V = __ballot_sync(FULL, act && v);
+                bool keep;
+                if (p.grad_true) {
+                    keep = act && v;
+                } else {
+                    // lanes of this item's group up to and including itself
+                    const unsigned gs_le = GS & (lt_mask | (1u << lane));
+                    const int gstart = gs_le ? 31 - __clz(gs_le) : -1;
+                    const unsigned grp = (lt_mask | (1u << lane)) & (gstart >= 0 ? ~((1u << gstart) - 1u) : FULL);
+                    const unsigned vg = V & grp;
+                    const int fv = vg ? __ffs(vg) - 1 : 0;
+                    const uint32_t src_fv = __shfl_sync(FULL, s, fv);
+                    uint32_t ch = NONE;
+                    if (gstart < 0 && chosen != NONE) ch = chosen;      // group began before this batch
+                    else if (vg) ch = src_fv;
+                    keep = act && v && s == ch;
+                    // carry the group state of the batch's last item
+                    const int lastl = 31 - __clz(__ballot_sync(FULL, act));
+                    chosen = __shfl_sync(FULL, ch, lastl);
+                }
+                const unsigned KM = __ballot_sync(FULL, keep);
+                const uint32_t kr = nk + __popc(KM & lt_mask);
+                if (keep) {
+                    RedEntry<A> e;
+                    e.src = s;
+                    e.w = (A)cf * sc;
+                    ents[kr] = e;
+                }
+                // the chunk's first item belongs to the feature opened above
+                const bool opens = seg_start && i != i0;
+                const unsigned SS = __ballot_sync(FULL, opens);
+                if (opens) segs[ns + __popc(SS & lt_mask)] = make_uint2(f, kr);
+                nk += __popc(KM);
+                ns += __popc(SS);
+                const int last = 31 - __clz(__ballot_sync(FULL, act));
+                prev_f = __shfl_sync(FULL, f, last);
+                prev_anchor = __shfl_sync(FULL, anchor, last);
+                prev_src = __shfl_sync(FULL, s, last);
+                f0 = f1; s0 = s1; c0 = c1; v0 = v1; sc0 = sc1;
+                f1 = f2; s1 = s2; c1 = c2;
+            }
+            __syncwarp();
+            // phase 2: the kept items in order, NF direction rows in flight;
+            // features close where the next one's first kept item comes
+            uint32_t j = 0;
+            uint32_t next_b = ns ? segs[0].y : 0xffffffffu;
+            for (uint32_t k = 0; k < nk; k += NF) {
                 uint32_t src[NF];
                 A wv[NF];
-                int ln[NF];
-                int n = 0;
 #pragma unroll
                 for (int u = 0; u < NF; ++u) {
-                    const int j = pend ? __ffs(pend) - 1 : 0;
-                    ln[u] = pend ? j : 32;
-                    src[u] = __shfl_sync(FULL, s, j);
-                    wv[u] = __shfl_sync(FULL, w, j);
-                    if (pend) { pend &= pend - 1; n = u + 1; }
+                    src[u] = 0;
+                    wv[u] = 0;
+                    if (k + u < nk) {
+                        const RedEntry<A> e = ents[k + u];
+                        src[u] = e.src;
+                        wv[u] = e.w;
+                    }
                 }
                 typename IO::Raw r[NF];
-                if (lane_on) {
 #pragma unroll
-                    for (int u = 0; u < NF; ++u)
-                        if (u < n) r[u] = IO::load_raw(dir + (uint64_t)src[u] * p.dpad, lane);
-                }
+                for (int u = 0; u < NF; ++u)
+                    if (k + u < nk) r[u] = IO::load_raw(dir + (uint64_t)src[u] * p.dpad, lane_ld);
 #pragma unroll
                 for (int u = 0; u < NF; ++u) {
-                    if (u < n) {
-                        while (starts && __ffs(starts) - 1 <= ln[u]) {
-                            close_open(__ffs(starts) - 1);
-                            starts &= starts - 1;
+                    if (k + u < nk) {
+                        while (k + u >= next_b) {
+                            close_open(segs[j].x);
+                            ++j;
+                            next_b = j < ns ? segs[j].y : 0xffffffffu;
                         }
-                        if (lane_on) IO::template fma<A>(acc, wv[u], r[u]);
+                        IO::template fma<A>(acc, wv[u], r[u]);
                         any_kept = true;
                     }
                 }
             }
-            while (starts) {
-                close_open(__ffs(starts) - 1);
-                starts &= starts - 1;
-            }
-            prev_f = __shfl_sync(FULL, f, last);
-            prev_anchor = __shfl_sync(FULL, anchor, last);
-            prev_src = __shfl_sync(FULL, s, last);
-            f0 = f1; s0 = s1; c0 = c1; v0 = v1; sc0 = sc1;
-            f1 = f2; s1 = s2; c1 = c2;
+            // features of the window with no kept item after their start
+            for (; j < ns; ++j) close_open(segs[j].x);
+            __syncwarp();
         }
         const bool cont = i1 < M && p.skey[i1] == cur_f;
         if (started_here && !cont) {
@@ -1111,9 +1182,55 @@ __global__ void __launch_bounds__(RED_THREADS) k_adam_dense(BatchState* st, T* t
     }
 }
 
-template <typename T>
+// Self-check of the stochastic-rounding conversion against the bit rule it
+// replaces: element pairs from a hash of (seed, i), with exponents across the
+// whole FP32 range and every 16th pair drawn from special values (zeros,
+// infinities, NaNs, subnormals, the largest finite values, values one ulp
+// below a BF16 carry), rounded both ways with the same random bits.
+__global__ void k_sr_selftest(uint64_t n, uint64_t seed, unsigned long long* mismatches) {
+    const uint32_t specials[12] = {0x00000000u, 0x80000000u, 0x7f800000u, 0xff800000u, 0x7fc00000u, 0xffc00001u,
+                                   0x00000001u, 0x807fffffu, 0x7f7fffffu, 0xff7fffffu, 0x3f80ffffu, 0xbf7fffffu};
+    unsigned long long bad = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = (uint32_t)seed ^ (uint32_t)(seed >> 32);
+        const uint32_t h0 = mix32(k ^ mix32((uint32_t)i * 3u + 0x9E3779B1u) ^ (uint32_t)(i >> 32));
+        const uint32_t h1 = mix32(h0 ^ 0x85EBCA77u), h2 = mix32(h1 ^ 0xC2B2AE3Du), r = mix32(h2 ^ 0x27D4EB2Fu);
+        uint32_t a = h1, b = h2;
+        if ((i & 15u) == 0) {
+            a = specials[h1 % 12u];
+            b = specials[h2 % 12u];
+        }
+        const float lo = __uint_as_float(a), hi = __uint_as_float(b);
+        const uint32_t hw = bf16x2_stochastic(lo, hi, r);
+        const uint32_t sw = (uint32_t)__bfloat16_as_ushort(bf16_stochastic(lo, r & 0xffffu)) |
+                            ((uint32_t)__bfloat16_as_ushort(bf16_stochastic(hi, r >> 16)) << 16);
+        bad += hw != sw;
+    }
+    bad = warp_sum<unsigned long long>(bad);
+    if ((threadIdx.x & 31) == 0 && bad) atomicAdd(mismatches, bad);
+}
+
+extern "C" int ep_selftest_stochastic_rounding(int device, uint64_t n, uint64_t seed, uint64_t* mismatches) {
+    if (!mismatches) return EP_ERR_INVALID_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return EP_ERR_CUDA;
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, sizeof(*d)) != cudaSuccess) return EP_ERR_OOM;
+    cudaError_t e = cudaMemset(d, 0, sizeof(*d));
+    if (e == cudaSuccess) {
+        k_sr_selftest<<<152 * 4, 256>>>(n, seed, d);
+        e = cudaGetLastError();
+    }
+    unsigned long long h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    *mismatches = h;
+    return e == cudaSuccess ? EP_OK : EP_ERR_CUDA;
+}
+
+// OUT_QUEUE: the slots and their feature ids, then the per-warp item lists.
+template <typename T, typename A>
 static size_t queue_smem(uint32_t dpad) {
-    return (size_t)(QUEUE_THREADS / 32) * QN * (queue_slot_bytes<T>(dpad) + sizeof(uint32_t));
+    return queue_list_offset<T>(dpad, QUEUE_THREADS / 32) + (size_t)(QUEUE_THREADS / 32) * list_bytes<A>();
 }
 
 template <typename T, typename A, int VPL>
@@ -1124,7 +1241,8 @@ static void red_launch(const ReduceParams& p, uint64_t cap, cudaStream_t s, int 
         uint32_t ctas = (warps + RED_THREADS / 32 - 1) / (RED_THREADS / 32);
         if (ctas > RED_MAX_CTAS) ctas = RED_MAX_CTAS;
         if (p.red_ctas) ctas = std::min<uint32_t>(ctas, p.red_ctas);
-        if (p.out_mode == OUT_DENSE) launch_chain(k_reduce<T, A, VPL, OUT_DENSE>, ctas, RED_THREADS, 0, s, p);
+        const size_t lists = (size_t)(RED_THREADS / 32) * list_bytes<A>();
+        if (p.out_mode == OUT_DENSE) launch_chain(k_reduce<T, A, VPL, OUT_DENSE>, ctas, RED_THREADS, lists, s, p);
         else if (p.out_mode == OUT_QUEUE) {
             uint32_t qctas = (warps + QUEUE_THREADS / 32 - 1) / (QUEUE_THREADS / 32);
             if (qctas > 2 * RED_MAX_CTAS) qctas = 2 * RED_MAX_CTAS;
@@ -1132,16 +1250,17 @@ static void red_launch(const ReduceParams& p, uint64_t cap, cudaStream_t s, int 
             bool q5 = false;
             if constexpr (VPL <= 8) {
                 if (p.queue_ctas_per_sm >= 5) {
-                    launch_chain(k_reduce_q5<T, A, VPL>, qctas, QUEUE_THREADS, queue_smem<T>(p.dpad), s, p);
+                    launch_chain(k_reduce_q5<T, A, VPL>, qctas, QUEUE_THREADS, queue_smem<T, A>(p.dpad), s, p);
                     q5 = true;
                 }
             }
-            if (!q5) launch_chain(k_reduce<T, A, VPL, OUT_QUEUE>, qctas, QUEUE_THREADS, queue_smem<T>(p.dpad), s, p);
+            if (!q5) launch_chain(k_reduce<T, A, VPL, OUT_QUEUE>, qctas, QUEUE_THREADS, queue_smem<T, A>(p.dpad), s, p);
         } else if (p.out_mode == OUT_RING) {
             if constexpr (sizeof(T) != 8) {
                 // persistent: every CTA resident at once (one per SM at 16 warps)
                 const uint32_t threads = 32 * (p.ring_pw + p.ring_cw);
-                const size_t smem = ring_hdr_bytes() + (size_t)p.ring_slots * ring_slot_bytes<T>(p.dpad);
+                const size_t smem = ring_hdr_bytes() + (size_t)p.ring_slots * ring_slot_bytes<T>(p.dpad) +
+                                    (size_t)p.ring_pw * list_bytes<A>();
                 uint32_t per_sm = 65536u / (threads * 128u);
                 const uint32_t by_smem = (uint32_t)((227u * 1024u) / (smem + 1024u));
                 if (by_smem < per_sm) per_sm = by_smem;
@@ -1151,7 +1270,7 @@ static void red_launch(const ReduceParams& p, uint64_t cap, cudaStream_t s, int 
                 launch_chain(k_reduce<T, A, VPL, OUT_RING>, rctas, threads, smem, s, p);
             }
         }
-        else launch_chain(k_reduce<T, A, VPL, OUT_ADAM>, ctas, RED_THREADS, 0, s, p);
+        else launch_chain(k_reduce<T, A, VPL, OUT_ADAM>, ctas, RED_THREADS, lists, s, p);
     } else {
         uint32_t ctas = std::min<uint32_t>((warps + FIX_THREADS / 32 - 1) / (FIX_THREADS / 32), 152 * 16);
         constexpr int LT = fixl_threads(VPL);
@@ -1175,11 +1294,11 @@ static cudaError_t fixl_setup() {
         e = cudaFuncSetAttribute(k_fixup_long<T, A, VPL, OUT_ADAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_reduce<T, A, VPL, OUT_QUEUE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)queue_smem<T>(VPL * 32));
+                                 (int)queue_smem<T, A>(VPL * 32));
     if constexpr (VPL <= 8) {
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_reduce_q5<T, A, VPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)queue_smem<T>(VPL * 32));
+                                     (int)queue_smem<T, A>(VPL * 32));
     }
     if constexpr (sizeof(T) != 8) {
         if (e == cudaSuccess)
@@ -1195,12 +1314,12 @@ bool ring_supported(int tt, uint32_t dpad, uint32_t pw, uint32_t cw, uint32_t sl
     if (slots % cw) return false;   // each Adam warp owns whole slots (exact parity waits)
     const uint32_t es = tt == TT_BF16 ? 2u : 4u;
     if ((dpad * 4u) % 16u || (dpad * es) % 16u) return false;   // bulk copies move 16-byte multiples
-    return ring_smem_bytes(tt, dpad, slots) <= 227u * 1024u;
+    return ring_smem_bytes(tt, dpad, pw, slots) <= 227u * 1024u;
 }
 
-size_t ring_smem_bytes(int tt, uint32_t dpad, uint32_t slots) {
-    return ring_hdr_bytes() + (size_t)slots * (tt == TT_BF16 ? ring_slot_bytes<__nv_bfloat16>(dpad)
-                                                              : ring_slot_bytes<float>(dpad));
+size_t ring_smem_bytes(int tt, uint32_t dpad, uint32_t pw, uint32_t slots) {
+    return ring_hdr_bytes() + (size_t)pw * list_bytes<float>() +
+           (size_t)slots * (tt == TT_BF16 ? ring_slot_bytes<__nv_bfloat16>(dpad) : ring_slot_bytes<float>(dpad));
 }
 
 template <typename T, typename A>

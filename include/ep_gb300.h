@@ -292,6 +292,14 @@ int ep_ag_forward(ep_ctx* ctx, const ep_batch_samples* samples, int precision,
                   const void* table_dev, void* loss_dev, void* stream);
 int ep_ag_backward(ep_ctx* ctx, const void* dloss_dev, void* grad_dev, void* stream);
 
+/* Self-check (no counterpart in the reference): rounds n element pairs
+ * (hashed from seed, with special values among them) to BF16 both with the
+ * hardware stochastic-rounding conversion the FUSED form's Adam uses and with
+ * the bit rule it stands for (add 16 random bits below the BF16 mantissa,
+ * truncate; NaN and infinities kept), and stores the number of pairs whose
+ * results differ in *mismatches (0 expected). */
+int ep_selftest_stochastic_rounding(int device, uint64_t n, uint64_t seed, uint64_t* mismatches);
+
 /* Blocks until the context's work is done; reports device error flags. */
 int ep_synchronize(ep_ctx* ctx);
 

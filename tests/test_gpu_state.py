@@ -6,7 +6,9 @@
 * table initialisation: rows U(-1, 1)^d, L2-normalised
   (src/algos/ep/mod.rs:100-110, 381-392);
 * the validation loss: the mean over the validation ids of the forward loss
-  with the validation pass's samples (src/algos/ep/mod.rs:267-283).
+  with the validation pass's samples (src/algos/ep/mod.rs:267-283);
+* the FUSED form's BF16 rounding of updated table rows: the hardware
+  stochastic-rounding conversion equals the bit rule it stands for.
 """
 import math
 
@@ -107,3 +109,10 @@ def test_validation_loss_matches_oracle(oracle, sbm10k, form):
     want = float(np.concatenate(losses).sum() / len(valid))
     assert np.isfinite(st["valid_loss"]) and want > 0
     assert abs(st["valid_loss"] - want) <= 1e-4 * abs(want), (st["valid_loss"], want)
+
+
+def test_hardware_stochastic_rounding_matches_the_bit_rule():
+    # 16M element pairs, every 16th from special values (zeros, infinities,
+    # NaNs, subnormals, the largest finite values, BF16 carry boundaries)
+    assert _native.selftest_stochastic_rounding(n=1 << 24, seed=7) == 0
+    assert _native.selftest_stochastic_rounding(n=1 << 20, seed=12345) == 0
