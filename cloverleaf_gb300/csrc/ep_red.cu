@@ -299,15 +299,12 @@ __device__ __forceinline__ void queue_pop(const ReduceParams& p, WarpQueue& q, i
     --q.n;
 }
 
-// Queues a finished (NaN-free) row; updates the oldest slot first when full.
+// Queues a finished (NaN-free) row, then, when every slot is taken, updates
+// the oldest: the new row's copies are issued first, so they are in flight
+// while the oldest row is updated as well as while the next rows reduce.
 template <typename T, typename A, int VPL>
 __device__ __forceinline__ void queue_push(const ReduceParams& p, WarpQueue& q, uint32_t f, const A (&acc)[VPL], int lane,
                                            bool lane_on, const AdamStep& as) {
-    if (q.n == QN) {
-        cp_async_wait<QN - 1>();
-        __syncwarp();
-        queue_pop<T, VPL>(p, q, lane, lane_on, as);
-    }
     uint32_t slot = q.head + q.n;
     if (slot >= QN) slot -= QN;
     float *gs, *ms, *vs;
@@ -326,6 +323,11 @@ __device__ __forceinline__ void queue_push(const ReduceParams& p, WarpQueue& q, 
     cp_async_commit();
     if (lane == 0) q.f[slot] = f;
     ++q.n;
+    if (q.n == QN) {
+        cp_async_wait<QN - 1>();
+        __syncwarp();
+        queue_pop<T, VPL>(p, q, lane, lane_on, as);
+    }
 }
 
 // Updates every queued slot (end of the warp's work).
@@ -566,16 +568,18 @@ __device__ __forceinline__ void prefetch_segment_state(const ReduceParams& p, ui
     }
 }
 
-// k_reduce: one warp per chunk of C sorted items, 32 items (one per lane) at a
-// time.  Per batch the first-occurrence rule is evaluated for all 32 items at
-// once with ballots: group starts (new feature or new anchor), valid roles,
-// and for every item the first valid role of its (feature, anchor) group,
-// carried across batches and, at a chunk start, found by walking back.  The
-// kept items' direction rows are then streamed in item order, several in
-// flight across feature boundaries; a feature is finished when the stream
-// passes the start of the next one.  Item metadata is software-pipelined:
-// while batch b is reduced, the role flags and scales of batch b+1 and the
-// keys of batch b+2 are in flight.
+// k_reduce: one warp per chunk of C sorted items, in windows of RW items.
+// Phase 1 takes the window 32 items (one per lane) at a time: the
+// first-occurrence rule is evaluated for all 32 at once with ballots (group
+// starts: new feature or new anchor; valid roles; for every item the first
+// valid role of its (feature, anchor) group, carried across batches and, at a
+// chunk start, found by walking back), and the kept items and the feature
+// starts are appended to the warp's lists.  Item metadata is
+// software-pipelined: while batch b is examined, the role flags and scales of
+// batch b+1 and the keys of batch b+2 are in flight.  Phase 2 streams the
+// kept items' direction rows in list order, NF in flight across feature
+// boundaries; a feature is finished when the stream reaches the first kept
+// item of the next one.
 // End of an OUT_RING CTA (every warp of both roles): once all warps are
 // here, the bulk copies of each slot's last issued round must have landed
 // before the CTA's shared memory is released.
@@ -916,6 +920,12 @@ __device__ __forceinline__ void reduce_body(const ReduceParams& p) {
 #pragma unroll
                 for (int u = 0; u < NF; ++u)
                     if (k + u < nk) r[u] = IO::load_raw(dir + (uint64_t)src[u] * p.dpad, lane_ld);
+                if (k + NF <= nk && k + NF <= next_b) {   // no feature starts among these NF
+#pragma unroll
+                    for (int u = 0; u < NF; ++u) IO::template fma<A>(acc, wv[u], r[u]);
+                    any_kept = true;
+                    continue;
+                }
 #pragma unroll
                 for (int u = 0; u < NF; ++u) {
                     if (k + u < nk) {
