@@ -788,14 +788,15 @@ static uint32_t kernels_per_batch(const ep_ctx* c, bool fork) {
 
 // Issues one training batch on the context stream; ev (optional) receives an
 // event record after each stage (EP_N_STAGES events).  With fork (graph
-// capture), the items are emitted by k_fwd_emit and sorted on the side stream
-// beside the gathers and the loss (which then skip the emission), and
-// k_batch_end follows the loss there; the reduction waits for the sorted
-// items.  The fix-ups run on the fix stream beside the next batch's
-// k_batch_begin, sampler and scan (which read neither the table nor what the
-// fix-ups read: those use k_reduce's copy of the item count and Adam
-// constants), and that batch's gathers wait for them; the last batch of a
-// capture (last) joins its fix-ups before it ends.
+// capture), the item offsets are scanned, the items emitted by k_fwd_emit and
+// sorted on the side stream beside the gathers and the loss (which then skip
+// the emission and read neither), and k_batch_end follows the loss there; the
+// reduction waits for the sorted items.  The fix-ups run on the fix stream
+// beside the next batch's k_batch_begin, sampler and scan (which read neither
+// the table nor what the fix-ups read: those use k_reduce's copy of the item
+// count and Adam constants), and that batch's gathers and item emission wait
+// for them; the last batch of a capture (last) joins its fix-ups before it
+// ends.
 static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = false, bool last = true) {
     BatchState* st = c->st.as<BatchState>();
     cudaStream_t s = c->stream;
@@ -803,13 +804,15 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = 
                        c->cfg.noise, noise_decay(c), s);
     SampleParams sp = sample_params(c, st, false, false);
     launch_sample(sp, s);
-    launch_scan_occ(st, c->occ.as<uint32_t>(), c->Bcap, c->items_cap, s);
+    if (!fork) launch_scan_occ(st, c->occ.as<uint32_t>(), c->Bcap, c->items_cap, s);
     if (ev) cudaEventRecord(ev[EP_STAGE_SAMPLE], s);
     if (fork) {
-        // side stream: the items (k_fwd_emit) and their sort, beside the
-        // gathers and the loss on the main stream; then k_batch_end
+        // side stream: the item offsets (scan), the items (k_fwd_emit) and
+        // their sort, beside the gathers and the loss on the main stream,
+        // which run with emission off and read neither; then k_batch_end
         cudaEventRecord(c->ev_fork, s);
         cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+        launch_scan_occ(st, c->occ.as<uint32_t>(), c->Bcap, c->items_cap, c->side);
         if (c->fix_pending) {   // the previous batch's fix-ups: the table, and the sorted items they read
             cudaStreamWaitEvent(s, c->ev_fix, 0);
             cudaStreamWaitEvent(c->side, c->ev_fix, 0);

@@ -396,11 +396,16 @@ __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
                 cnt = r;
             } else if (r <= 32) {
                 // Floyd's algorithm: a uniform r-subset of [0, deg); lane i
-                // holds the i-th chosen position.
+                // holds the i-th chosen position.  The draw of step it does
+                // not depend on the set chosen so far, so lane it makes it
+                // up front and the steps only test membership.
                 uint32_t mine = 0xffffffffu;
+                const uint32_t my_draw =
+                    (uint32_t)lane < r ? below(rand_u32(c.seed, v, salt, ST_NBR, (uint32_t)lane), deg - r + (uint32_t)lane + 1)
+                                       : 0u;
                 for (uint32_t it = 0; it < r; ++it) {
                     const uint32_t j = deg - r + it;
-                    const uint32_t tpos = below(rand_u32(c.seed, v, salt, ST_NBR, it), j + 1);
+                    const uint32_t tpos = __shfl_sync(FULL, my_draw, (int)it);
                     const unsigned hit = __ballot_sync(FULL, mine == tpos);
                     const uint32_t pick = hit ? j : tpos;
                     if (lane == (int)it) mine = pick;
@@ -408,10 +413,16 @@ __global__ void __launch_bounds__(256) k_sample(SampleParams p) {
                 if ((uint32_t)lane < r) { out[lane] = p.cols[rs + mine]; outw[lane] = __uint_as_float(mine); }
                 cnt = r;
             } else if (r <= c.Kcap) {
-                // Floyd with the chosen set kept in the output slots.
+                // Floyd with the chosen set kept in the output slots (the
+                // draws made 32 steps at a time, lane i for step it0 + i).
+                uint32_t my_draw = 0;
                 for (uint32_t it = 0; it < r; ++it) {
                     const uint32_t j = deg - r + it;
-                    const uint32_t tpos = below(rand_u32(c.seed, v, salt, ST_NBR, it), j + 1);
+                    if ((it & 31u) == 0) {
+                        const uint32_t q = it + (uint32_t)lane;
+                        my_draw = q < r ? below(rand_u32(c.seed, v, salt, ST_NBR, q), deg - r + q + 1) : 0u;
+                    }
+                    const uint32_t tpos = __shfl_sync(FULL, my_draw, (int)(it & 31u));
                     bool found = false;
                     for (uint32_t b = 0; b < it; b += 32) {
                         const uint32_t q = b + lane;
