@@ -1024,8 +1024,8 @@ static int autotune(ep_ctx* c, uint32_t& n) {
     return EP_OK;
 }
 
-// Captures and instantiates `batches` consecutive training batches as one
-// graph (nothing runs: the capture only records the launches).
+// Captures, instantiates and uploads `batches` consecutive training batches
+// as one graph (nothing runs: the capture only records the launches).
 static int capture_batches(ep_ctx* c, uint32_t batches, cudaGraphExec_t* out) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
@@ -1037,6 +1037,9 @@ static int capture_batches(ep_ctx* c, uint32_t batches, cudaGraphExec_t* out) {
     e = cudaGraphInstantiate(out, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) { *out = nullptr; return c->cuda_fail(e, "graph instantiate"); }
+    // the graph's work goes to the device now, not at its first launch
+    e = cudaGraphUpload(*out, c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "graph upload");
     return EP_OK;
 }
 
