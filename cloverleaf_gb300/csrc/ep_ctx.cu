@@ -825,6 +825,7 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = 
                           c->items_cap, (int)bits_for(c->n_feat), &c->sorted_keys, &c->sorted_vals, c->side);
         cudaEventRecord(c->ev_sorted, c->side);
         ForwardParams fp = forward_params(c, st, c->table.p, false, false);
+        fp.means_dead = 1;
         launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, s);
         cudaEventRecord(c->ev_loss, s);
         cudaStreamWaitEvent(c->side, c->ev_loss, 0);
@@ -834,6 +835,7 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = 
         cudaStreamWaitEvent(s, c->ev_sorted, 0);   // sorted items for the reduction
     } else {
         ForwardParams fp = forward_params(c, st, c->table.p, true, false);
+        fp.means_dead = 1;
         launch_forward(c->tt, (int)c->vpl, fp, c->Bcap, s);
         if (ev) cudaEventRecord(ev[EP_STAGE_FORWARD], s);
         launch_radix_sort(st, c->item_f.as<uint32_t>(), c->key_alt.as<uint32_t>(), c->item_src.as<uint32_t>(),

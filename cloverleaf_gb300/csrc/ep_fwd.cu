@@ -1190,6 +1190,23 @@ __global__ void __launch_bounds__(128) k_fwd_loss(ForwardParams p) {
             for (int k = 0; k < VPL; ++k) x[k] = 0;
         }
     };
+    // Once the anchor's role means are read and its directions written
+    // elsewhere (BF16 directions), nothing reads the means again: their L2
+    // lines are dropped without a write-back (discard.global.L2), which keeps
+    // L2 for the directions the reducer reads next.  Only whole 128-byte
+    // lines of this anchor's rows are dropped.
+    auto drop_means = [&]() {
+        if constexpr (!std::is_same<D, A>::value) {
+            const uint64_t rb = (uint64_t)dpad * sizeof(A);
+            if (p.means_dead && (rb & 127u) == 0) {
+                __syncwarp();
+                const char* base = reinterpret_cast<const char*>(dir + sbase * dpad);
+                const uint32_t lines = (uint32_t)(NR * rb / 128u);
+                for (uint32_t l = lane; l < lines; l += 32)
+                    asm volatile("discard.global.L2 [%0], 128;" ::"l"(base + (uint64_t)l * 128u) : "memory");
+            }
+        }
+    };
 
     A hv[VPL], tv[VPL], u[VPL], un[VPL];
     load_mean(sbase, hv);
@@ -1329,6 +1346,7 @@ __global__ void __launch_bounds__(128) k_fwd_loss(ForwardParams p) {
             if (p.loss_out) ((A*)p.loss_out)[a] = L;
             p.status[a] = is_nan ? 2 : (ok ? 0 : 1);
         }
+        drop_means();
         return;
     }
 
@@ -1469,6 +1487,7 @@ __global__ void __launch_bounds__(128) k_fwd_loss(ForwardParams p) {
         if (!ok) p.valid[src] = 0;
         scale[src] = scale[src] * up * neg_f / wdiv;
     }
+    drop_means();
 }
 
 // ---------------------------------------------------------------------------

@@ -157,6 +157,7 @@ struct ForwardParams {
     void* scale;            // A[n_anchors * NR]
     uint8_t* valid;         // [n_anchors * NR]
     void* loss_out;         // A[n_anchors]
+    int means_dead;         // k_fwd_loss drops the role means from L2 once read (no reader after it)
     int32_t* status;        // [n_anchors]
     uint32_t* item_f;
     uint32_t* item_src;
