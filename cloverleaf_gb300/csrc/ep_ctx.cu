@@ -452,6 +452,17 @@ extern "C" int ep_get_table(ep_ctx* c, float* out) {
     if (!c || !out) return EP_ERR_INVALID_ARG;
     if (!c->table_ok) return c->fail(EP_ERR_STATE, "no table");
     cudaSetDevice(c->device);
+    // page-locked caller memory: the kernel writes the FP32 rows into it
+    // directly (no staging buffer to allocate, no separate copy)
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, out) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer &&
+        launch_table_out(c->tt, c->table.p, static_cast<float*>(pa.devicePointer), c->n_feat, c->dims, c->dpad,
+                         c->stream)) {
+        CK(cudaGetLastError(), "table download");
+        CK(cudaStreamSynchronize(c->stream), "download table");
+        return EP_OK;
+    }
+    cudaGetLastError();   // pageable memory: the attribute query may leave an error behind
     const size_t dense = (size_t)c->n_feat * c->dims * 4;
     if (!c->xfer.ensure(dense)) return c->fail(EP_ERR_OOM, "staging allocation failed");
     launch_convert_table(c->tt, c->table.p, c->xfer.as<float>(), c->n_feat, c->dims, c->dpad, 0, c->stream);

@@ -1601,6 +1601,33 @@ __global__ void k_convert(T* dev, float* host_layout, uint64_t n_feat, uint32_t 
     }
 }
 
+// Device layout [n_feat x dpad] of type T -> dense FP32 [n_feat x dims], four
+// elements per thread (dims and dpad multiples of 4), written straight into
+// page-locked host memory through its device address: the download needs no
+// device staging buffer and no separate copy.
+template <typename T>
+__global__ void k_table_out4(const T* __restrict__ dev, float4* __restrict__ out, uint64_t n_feat, uint32_t dims,
+                             uint32_t dpad) {
+    const uint32_t q = dims / 4;
+    const uint64_t n = n_feat * q;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = i / q;
+        const uint32_t k = (uint32_t)(i - r * q) * 4u;
+        const T* src = dev + r * dpad + k;
+        float4 o;
+        if constexpr (sizeof(T) == 2) {
+            const uint2 w = *reinterpret_cast<const uint2*>(src);
+            o = make_float4(__uint_as_float(w.x << 16), __uint_as_float(w.x & 0xffff0000u), __uint_as_float(w.y << 16),
+                            __uint_as_float(w.y & 0xffff0000u));
+        } else if constexpr (sizeof(T) == 4) {
+            o = *reinterpret_cast<const float4*>(src);
+        } else {
+            o = make_float4((float)src[0], (float)src[1], (float)src[2], (float)src[3]);
+        }
+        out[i] = o;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Set-up kernels.
 // k_node_bound: an upper bound on the items one anchor can emit:
@@ -1738,6 +1765,18 @@ void launch_init_table(int tt, void* table, uint64_t n_feat, uint32_t dims, uint
     else if (tt == TT_BF16)
         k_init_table<__nv_bfloat16><<<(unsigned)blocks, 256, 0, s>>>((__nv_bfloat16*)table, n_feat, dims, dpad, seed);
     else k_init_table<double><<<(unsigned)blocks, 256, 0, s>>>((double*)table, n_feat, dims, dpad, seed);
+}
+
+bool launch_table_out(int tt, const void* table, float* out_dev, uint64_t n_feat, uint32_t dims, uint32_t dpad,
+                      cudaStream_t s) {
+    if ((dims & 3u) || (dpad & 3u) || (reinterpret_cast<uintptr_t>(out_dev) & 15u)) return false;
+    if (!n_feat || !dims) return true;
+    const unsigned blocks = 152 * 16;
+    if (tt == TT_F32) k_table_out4<float><<<blocks, 256, 0, s>>>((const float*)table, (float4*)out_dev, n_feat, dims, dpad);
+    else if (tt == TT_BF16)
+        k_table_out4<__nv_bfloat16><<<blocks, 256, 0, s>>>((const __nv_bfloat16*)table, (float4*)out_dev, n_feat, dims, dpad);
+    else k_table_out4<double><<<blocks, 256, 0, s>>>((const double*)table, (float4*)out_dev, n_feat, dims, dpad);
+    return true;
 }
 
 void launch_convert_table(int tt, void* dst, const float* src, uint64_t n_feat, uint32_t dims, uint32_t dpad,

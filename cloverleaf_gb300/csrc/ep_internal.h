@@ -223,6 +223,11 @@ void launch_batch_end(BatchState* st, const void* loss, const int32_t* status,
                       int eval, int loss_f64, cudaStream_t s);
 void launch_init_table(int tt, void* table, uint64_t n_feat, uint32_t dims, uint32_t dpad,
                        uint64_t seed, cudaStream_t s);
+// Writes the table as dense FP32 [n_feat x dims] to out_dev (device memory,
+// or page-locked host memory through its device address); false when the
+// shape or alignment needs the element-wise conversion instead.
+bool launch_table_out(int tt, const void* table, float* out_dev, uint64_t n_feat, uint32_t dims, uint32_t dpad,
+                      cudaStream_t s);
 void launch_convert_table(int tt_dst, void* dst, const float* src, uint64_t n_feat,
                           uint32_t dims, uint32_t dpad, int to_device_layout, cudaStream_t s);
 void launch_node_bound(const uint64_t* row_ptr, const uint32_t* cols, const uint64_t* fptr, uint32_t n,

@@ -116,3 +116,23 @@ def test_hardware_stochastic_rounding_matches_the_bit_rule():
     # NaNs, subnormals, the largest finite values, BF16 carry boundaries)
     assert _native.selftest_stochastic_rounding(n=1 << 24, seed=7) == 0
     assert _native.selftest_stochastic_rounding(n=1 << 20, seed=12345) == 0
+
+
+@pytest.mark.parametrize("form,dims", [(_native.FORM_FUSED_BF16, 64), (_native.FORM_PLAIN_FP32, 64),
+                                       (_native.FORM_FUSED_BF16, 30)])
+def test_table_download_into_page_locked_memory(sbm10k, form, dims):
+    # page-locked output memory is written by the device directly; the rows
+    # must equal the staged download into ordinary memory bit for bit
+    # (dims 30: not a multiple of 4, the staged path in both cases)
+    torch = pytest.importorskip("torch")
+    w = dict(sbm10k, ep=dict(sbm10k["ep"], dims=dims))
+    ctx = make_ctx(w, form, passes=1)
+    ctx.train(1)
+    n = w["n_feat"]
+    ref = ctx.get_table(n, dims)
+    pin = torch.empty((n, dims), dtype=torch.float32, pin_memory=True).numpy()
+    pin[...] = np.nan
+    got = ctx.get_table(n, dims, out=pin)
+    ctx.close()
+    assert got is pin
+    assert np.array_equal(ref.view(np.uint32), pin.view(np.uint32))
