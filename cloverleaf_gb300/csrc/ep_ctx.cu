@@ -69,7 +69,8 @@ struct ep_ctx {
     cudaEvent_t ev_fork = nullptr, ev_loss = nullptr, ev_join = nullptr, ev_sorted = nullptr;
     // second branch: a batch's fix-ups beside the next batch's sampling
     cudaStream_t fix = nullptr;
-    cudaEvent_t ev_red = nullptr, ev_fix = nullptr;
+    cudaStream_t fix2 = nullptr;   // the long spans' fix-ups, beside the short ones on `fix`
+    cudaEvent_t ev_red = nullptr, ev_fix = nullptr, ev_fix2 = nullptr;
     bool fix_pending = false;   // the last issued fix-ups have not been joined yet
     std::string err;
 
@@ -91,6 +92,7 @@ struct ep_ctx {
     DevBuf item_f, item_src, item_c, key_alt, idx, idx_alt, hist;
     DevBuf carry_head, carry_tail, carry_f, carry_flags, long_list, gdense, touched, n_touched, packed, xfer, bound;
     DevBuf check;   // CSR validation result / bound histogram scratch
+    uint32_t long_cap = 0;   // owner chunks per parity in long_list
     uint64_t items_cap = 0;
     uint32_t buf_B = 0, buf_K = 0, buf_es = 0;
     uint32_t chunk = 128;
@@ -146,7 +148,9 @@ struct ep_ctx {
         if (ev_sorted) cudaEventDestroy(ev_sorted);
         if (ev_red) cudaEventDestroy(ev_red);
         if (ev_fix) cudaEventDestroy(ev_fix);
+        if (ev_fix2) cudaEventDestroy(ev_fix2);
         if (fix) cudaStreamDestroy(fix);
+        if (fix2) cudaStreamDestroy(fix2);
         if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -247,8 +251,10 @@ extern "C" int ep_create(const ep_config* cfg, ep_ctx** out) {
         cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
         cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
         cudaStreamCreateWithPriority(&c->fix, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&c->fix2, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_red, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fix, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fix2, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_loss, cudaEventDisableTiming) != cudaSuccess ||
@@ -501,6 +507,7 @@ static int ensure_bufs(ep_ctx* c, uint32_t B, uint32_t K, uint64_t items, uint32
         if (!ok) return c->fail(EP_ERR_OOM, "batch scratch allocation failed (B=%u K=%u items=%llu)", B, K, (unsigned long long)items);
         c->buf_B = B;
         c->buf_K = K;
+        c->long_cap = nch;
         c->items_cap = items;
         c->buf_es = es;
         c->drop_graph();
@@ -760,6 +767,7 @@ static ReduceParams reduce_params(ep_ctx* c, BatchState* st, int out_mode, void*
     rp.carry_f = c->carry_f.as<uint32_t>();
     rp.carry_flags = c->carry_flags.as<uint32_t>();
     rp.long_list = c->long_list.as<uint32_t>();
+    rp.long_cap = c->long_cap;
     rp.ring_pw = c->ring_pw;
     rp.ring_cw = c->ring_cw;
     rp.ring_slots = c->ring_slots;
@@ -826,7 +834,9 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = 
         launch_scan_occ(st, c->occ.as<uint32_t>(), c->Bcap, c->items_cap, c->side);
         if (c->fix_pending) {   // the previous batch's fix-ups: the table, and the sorted items they read
             cudaStreamWaitEvent(s, c->ev_fix, 0);
+            cudaStreamWaitEvent(s, c->ev_fix2, 0);
             cudaStreamWaitEvent(c->side, c->ev_fix, 0);
+            cudaStreamWaitEvent(c->side, c->ev_fix2, 0);
             c->fix_pending = false;
         }
         ForwardParams fe = forward_params(c, st, c->table.p, true, false);
@@ -862,12 +872,25 @@ static void issue_train_batch(ep_ctx* c, cudaEvent_t* ev = nullptr, bool fork = 
     if (fork && !plain) {
         cudaEventRecord(c->ev_red, s);
         cudaStreamWaitEvent(c->fix, c->ev_red, 0);
-        launch_fixup(c->tt, (int)c->vpl, rp, c->items_cap, c->fix);
+        cudaStreamWaitEvent(c->fix2, c->ev_red, 0);
+        launch_fixup(c->tt, (int)c->vpl, rp, c->items_cap, c->fix, 1);    // short spans
+        launch_fixup(c->tt, (int)c->vpl, rp, c->items_cap, c->fix2, 2);   // long spans, beside them
         cudaEventRecord(c->ev_fix, c->fix);
-        if (last) cudaStreamWaitEvent(s, c->ev_fix, 0);
-        else c->fix_pending = true;
+        cudaEventRecord(c->ev_fix2, c->fix2);
+        if (last) {
+            cudaStreamWaitEvent(s, c->ev_fix, 0);
+            cudaStreamWaitEvent(s, c->ev_fix2, 0);
+        } else {
+            c->fix_pending = true;
+        }
     } else {
-        launch_fixup(c->tt, (int)c->vpl, rp, c->items_cap, s);
+        // the long spans' fix-ups beside the short ones here too
+        cudaEventRecord(c->ev_red, s);
+        cudaStreamWaitEvent(c->fix2, c->ev_red, 0);
+        launch_fixup(c->tt, (int)c->vpl, rp, c->items_cap, s, 1);
+        launch_fixup(c->tt, (int)c->vpl, rp, c->items_cap, c->fix2, 2);
+        cudaEventRecord(c->ev_fix2, c->fix2);
+        cudaStreamWaitEvent(s, c->ev_fix2, 0);
     }
     if (ev) cudaEventRecord(ev[EP_STAGE_FIXUP], s);
     if (plain)

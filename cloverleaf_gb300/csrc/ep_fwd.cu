@@ -180,6 +180,7 @@ __global__ void k_batch_begin(BatchState* st, uint32_t n_order, uint32_t cap, ui
     st->n_items = 0;
     st->fwd_next = 0;
     st->red_next = 0;
+    st->n_long[s & 1u] = 0;
 }
 
 // ---------------------------------------------------------------------------

@@ -62,7 +62,9 @@ struct BatchState {
     // pass accumulators (reset by the host at a pass start)
     double pass_err_sum;
     uint32_t pass_batches;
-    uint32_t n_long;        // long-span fixups queued by k_fixup for k_fixup_long
+    uint32_t n_long[2];     // long spans queued by k_reduce for k_fixup_long, by the step's parity: a
+                            // batch's k_batch_begin zeroes its own while the previous batch's
+                            // k_fixup_long may still read the other
     // the batch's item count and Adam constants as k_reduce found them: the
     // fix-up and dense Adam kernels read these, so that in replayed graphs
     // the next batch's k_batch_begin and sampler may run beside them
@@ -189,7 +191,8 @@ struct ReduceParams {
     void* carry_tail;
     uint32_t* carry_f;
     uint32_t* carry_flags;
-    uint32_t* long_list;    // long spans: (owner chunk, last chunk) pairs [n_chunks][2]
+    uint32_t* long_list;    // owner chunks of long spans [2][long_cap], by step parity
+    uint32_t long_cap;
     // OUT_RING shape: reducing warps, Adam warps and ring slots per CTA
     uint32_t ring_pw, ring_cw, ring_slots;
     // OUT_QUEUE: resident CTAs per SM the reducer is compiled for (4 or 5)
@@ -214,7 +217,9 @@ void launch_radix_sort(BatchState* st, uint32_t* keys, uint32_t* keys_alt, const
                        const float* item_c, uint2* vals, uint2* vals_alt, uint32_t* hist, uint64_t cap,
                        int key_bits, uint32_t** sorted_keys, uint2** sorted_vals, cudaStream_t s);
 void launch_reduce(int tt, int vpl, const ReduceParams& p, uint64_t items_cap, cudaStream_t s);
-void launch_fixup(int tt, int vpl, const ReduceParams& p, uint64_t items_cap, cudaStream_t s);
+// part: 0 both fix-up kernels in order, 1 the short spans (k_fixup), 2 the
+// long spans (k_fixup_long); the two parts are independent
+void launch_fixup(int tt, int vpl, const ReduceParams& p, uint64_t items_cap, cudaStream_t s, int part = 0);
 void launch_adam_dense(int tt, int vpl, BatchState* st, void* table, float* m, float* v,
                        const float* g, const uint32_t* touched, const uint32_t* n_touched,
                        uint32_t dpad, uint32_t max_rows, uint64_t seed, cudaStream_t s);

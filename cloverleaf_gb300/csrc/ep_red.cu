@@ -623,6 +623,14 @@ __host__ __device__ constexpr size_t queue_list_offset(uint32_t dpad, uint32_t w
     return ((size_t)warps * QN * (queue_slot_bytes<T>(dpad) + sizeof(uint32_t)) + 15) & ~(size_t)15;
 }
 
+// A span (owner chunk c, feature f) is long when f still fills the start of
+// chunk c + 1 + FIX_SHORT, i.e. its last chunk is more than FIX_SHORT past c.
+constexpr uint32_t FIX_SHORT = 16;
+__device__ __forceinline__ bool span_is_long(const ReduceParams& p, uint32_t c, uint32_t f, uint32_t M, uint32_t C) {
+    const uint64_t probe = (uint64_t)(c + 1 + FIX_SHORT) * C;
+    return probe < M && p.skey[probe] == f;
+}
+
 template <typename T, typename A, int VPL, int MODE>
 __device__ __forceinline__ void reduce_body(const ReduceParams& p);
 
@@ -690,7 +698,6 @@ __device__ __forceinline__ void reduce_body(const ReduceParams& p) {
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {   // read by k_fixup / k_fixup_long / k_adam_dense
         BatchState* st = p.st;
-        st->n_long = 0;
         st->fx_items = st->n_items;
         st->fx_step = st->step_cur;
         st->fx_lr = st->lr;
@@ -956,6 +963,10 @@ __device__ __forceinline__ void reduce_body(const ReduceParams& p) {
             if (lane_on) store_row<A, VPL, A>((A*)p.carry_tail + (uint64_t)c * p.dpad, lane, acc);
             if (lane == 0) p.carry_f[c] = cur_f;
             flags |= CF_OWNER | (any_kept ? CF_TAIL_KEPT : 0u);
+            if (lane == 0 && span_is_long(p, c, cur_f, M, C)) {
+                const uint32_t par = as.step & 1u;
+                p.long_list[(size_t)par * p.long_cap + atomicAdd(&p.st->n_long[par], 1u)] = c;
+            }
         }
         if (lane == 0) p.carry_flags[c] = flags;
     }
@@ -1001,8 +1012,8 @@ __device__ __forceinline__ uint32_t owner_last(const ReduceParams& p, uint32_t c
 // k_fixup: one warp per owner chunk (a chunk whose last feature continues into
 // later chunks).  Spans of up to FIX_SHORT partials are summed by the warp in
 // chunk order (owner's tail, then the heads of c+1 .. last) and finished;
-// longer spans are queued for k_fixup_long.
-constexpr uint32_t FIX_SHORT = 16;
+// longer spans, which k_reduce queued, are left to k_fixup_long, so that the
+// two kernels can run side by side.
 // k_fixup_long block size: as many warps as the row width leaves registers for
 __host__ __device__ constexpr int fixl_threads(int vpl) { return vpl >= 16 ? 256 : (vpl >= 8 ? 512 : 1024); }
 
@@ -1026,15 +1037,8 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
         if constexpr (MODE == OUT_ADAM && sizeof(T) != 8) {
             if (lane == 0) prefetch_row_state<T>(p, f);
         }
+        if (span_is_long(p, c, f, M, C)) continue;      // k_fixup_long's
         const uint32_t last = owner_last(p, c, f, M, C, lane);
-        if (last - c > FIX_SHORT) {
-            if (lane == 0) {
-                const uint32_t q = atomicAdd(&p.st->n_long, 1u);
-                p.long_list[2 * q] = c;
-                p.long_list[2 * q + 1] = last;
-            }
-            continue;
-        }
         A acc[VPL];
         if (lane_on) RowIO<A, VPL>::load_cg((const A*)p.carry_tail + (uint64_t)c * p.dpad, lane, acc);
         else {
@@ -1068,8 +1072,8 @@ __global__ void __launch_bounds__(FIX_THREADS) k_fixup(ReduceParams p) {
     if (lane == 0 && u_cnt) atomicAdd(&p.st->unique_rows, u_cnt);
 }
 
-// k_fixup_long: one CTA of NWARP warps per queued long span (owner chunk c
-// and the span's last chunk, as k_fixup found them).  Warp w adds
+// k_fixup_long: one CTA of NWARP warps per long span that k_reduce queued
+// (its owner chunk c; warp 0 finds the span's last chunk).  Warp w adds
 // the heads of chunks c+1+w, c+1+w+NWARP, ... in increasing order; warp 0 then
 // adds the owner's tail and the NWARP warp sums in warp order: a fixed order,
 // independent of timing and of the queue order.
@@ -1082,17 +1086,25 @@ __global__ void __launch_bounds__(fixl_threads(VPL)) k_fixup_long(ReduceParams p
     A* wsum = reinterpret_cast<A*>(fixl_smem);          // [NWARP][dpad]
     __shared__ uint32_t s_kept;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const uint32_t n_long = p.st->n_long;
-    const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
     const AdamStep as = AdamStep::load_fx(p.st);
+    const uint32_t par = as.step & 1u;
+    const uint32_t n_long = p.st->n_long[par];
+    const uint32_t* long_list = p.long_list + (size_t)par * p.long_cap;
+    const uint32_t M = p.st->fx_items, C = p.chunk;
+    __shared__ uint32_t s_last;
+    const bool lane_on = (uint32_t)(lane * VPL) < p.dpad;
     unsigned long long u_cnt = 0;
     for (uint32_t q = blockIdx.x; q < n_long; q += gridDim.x) {
-        const uint32_t c = p.long_list[2 * q];
-        const uint32_t last = p.long_list[2 * q + 1];   // found by k_fixup
+        const uint32_t c = long_list[q];
         const uint32_t fl = p.carry_flags[c];
         const uint32_t f = p.carry_f[c];
+        if (w == 0) {
+            const uint32_t l = owner_last(p, c, f, M, C, lane);
+            if (lane == 0) s_last = l;
+        }
         if (threadIdx.x == 0) s_kept = 0;
         __syncthreads();
+        const uint32_t last = s_last;
         A acc[VPL];
 #pragma unroll
         for (int k = 0; k < VPL; ++k) acc[k] = 0;
@@ -1285,12 +1297,14 @@ static void red_launch(const ReduceParams& p, uint64_t cap, cudaStream_t s, int 
         uint32_t ctas = std::min<uint32_t>((warps + FIX_THREADS / 32 - 1) / (FIX_THREADS / 32), 152 * 16);
         constexpr int LT = fixl_threads(VPL);
         const size_t lsmem = (size_t)(LT / 32) * p.dpad * sizeof(A);
+        // which: 1 both kernels, 2 the short spans, 3 the long spans
+        const bool shorts = which != 3, longs = which != 2;
         if (p.out_mode == OUT_DENSE) {
-            launch_chain(k_fixup<T, A, VPL, OUT_DENSE>, ctas, FIX_THREADS, 0, s, p);
-            launch_chain(k_fixup_long<T, A, VPL, OUT_DENSE>, 152, LT, lsmem, s, p);
+            if (shorts) launch_chain(k_fixup<T, A, VPL, OUT_DENSE>, ctas, FIX_THREADS, 0, s, p);
+            if (longs) launch_chain(k_fixup_long<T, A, VPL, OUT_DENSE>, 152, LT, lsmem, s, p);
         } else {
-            launch_chain(k_fixup<T, A, VPL, OUT_ADAM>, ctas, FIX_THREADS, 0, s, p);
-            launch_chain(k_fixup_long<T, A, VPL, OUT_ADAM>, 152, LT, lsmem, s, p);
+            if (shorts) launch_chain(k_fixup<T, A, VPL, OUT_ADAM>, ctas, FIX_THREADS, 0, s, p);
+            if (longs) launch_chain(k_fixup_long<T, A, VPL, OUT_ADAM>, 152, LT, lsmem, s, p);
         }
     }
 }
@@ -1382,8 +1396,8 @@ void launch_reduce(int tt, int vpl, const ReduceParams& p, uint64_t cap, cudaStr
     reduce_or_fixup(tt, vpl, p, cap, s, 0);
 }
 
-void launch_fixup(int tt, int vpl, const ReduceParams& p, uint64_t cap, cudaStream_t s) {
-    reduce_or_fixup(tt, vpl, p, cap, s, 1);
+void launch_fixup(int tt, int vpl, const ReduceParams& p, uint64_t cap, cudaStream_t s, int part) {
+    reduce_or_fixup(tt, vpl, p, cap, s, part == 1 ? 2 : (part == 2 ? 3 : 1));
 }
 
 template <typename T>
