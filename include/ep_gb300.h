@@ -231,7 +231,11 @@ int ep_sample_validation(ep_ctx* ctx, uint32_t first, uint32_t n, uint32_t strid
 int ep_batch_step(ep_ctx* ctx, const ep_batch_samples* samples, float lr, uint32_t pass);
 
 /* Copies the table out as n_feat*dims FP32.  Replaces the EmbeddingStore
- * returned by learn (src/lib.rs:1362-1368). */
+ * returned by learn (src/lib.rs:1362-1368).  When out is page-locked host
+ * memory (cudaHostAlloc / cudaHostRegister, e.g. a pinned torch tensor) and
+ * dims is a multiple of 4, a kernel writes the rows into it directly at the
+ * host link's rate; otherwise the rows go through a device staging buffer
+ * allocated on first use and one copy. */
 int ep_get_table(ep_ctx* ctx, float* out);
 
 /* Launch shapes in use (no counterpart in the reference): the reducer's items
