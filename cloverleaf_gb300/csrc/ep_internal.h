@@ -1,7 +1,9 @@
 // ep_internal.h -- structures shared by the host driver (ep_ctx.cu) and the
 // kernel translation units (ep_fwd.cu, ep_sort.cu, ep_red.cu).
 //
-// Per-batch data flow on the device (one CUDA stream, replayable as a graph):
+// Per-batch data flow on the device (stream launches in this order; replayed
+// graphs run the scan, item emission and sort on a side stream beside the
+// gathers and the loss, and the fix-ups beside the next batch's sampling):
 //   k_batch_begin  -> BatchState (batch range, lr, Adam bias corrections)
 //   k_sample       -> anchors, sampled neighbours, negatives, occurrence counts
 //   k_scan_occ     -> exclusive item offsets per anchor
@@ -11,8 +13,10 @@
 //   radix sort     -> items stably ordered by feature id
 //   k_reduce       -> per-feature gradient = sum over kept items, with the
 //                     first-occurrence rule; fused Adam (FUSED) or a dense
-//                     gradient row + touched list (PLAIN / parity hooks)
-//   k_fixup        -> features whose items span reducer chunks
+//                     gradient row + touched list (PLAIN / parity hooks);
+//                     queues the spans longer than FIX_SHORT later chunks
+//   k_fixup        -> features whose items span up to FIX_SHORT later chunks
+//   k_fixup_long   -> the longer spans (independent of k_fixup)
 //   k_adam         -> (PLAIN) Adam over the touched list
 //   k_batch_end    -> deterministic loss sums, counters, state advance
 #pragma once
@@ -34,7 +38,8 @@ enum : uint32_t {
 // OUT_ADAM: each finished feature row is updated in place by the warp that
 // finished it.  OUT_DENSE: rows go to a dense gradient buffer plus a touched
 // list (a separate Adam kernel, or the caller, consumes them).  OUT_QUEUE:
-// rows are queued in the warp's shared memory and updated four at a time.
+// rows are queued in the warp's shared memory, their Adam state copied in
+// asynchronously, and the oldest updated when the queue is full.
 // OUT_RING: warp-specialised CTAs; reducing warps push finished rows into a
 // CTA-wide shared-memory ring whose slots bulk-copy (TMA) the row's Adam
 // state, and Adam warps pop and update them.
