@@ -568,18 +568,6 @@ __device__ __forceinline__ void prefetch_segment_state(const ReduceParams& p, ui
     }
 }
 
-// k_reduce: one warp per chunk of C sorted items, in windows of RW items.
-// Phase 1 takes the window 32 items (one per lane) at a time: the
-// first-occurrence rule is evaluated for all 32 at once with ballots (group
-// starts: new feature or new anchor; valid roles; for every item the first
-// valid role of its (feature, anchor) group, carried across batches and, at a
-// chunk start, found by walking back), and the kept items and the feature
-// starts are appended to the warp's lists.  Item metadata is
-// software-pipelined: while batch b is examined, the role flags and scales of
-// batch b+1 and the keys of batch b+2 are in flight.  Phase 2 streams the
-// kept items' direction rows in list order, NF in flight across feature
-// boundaries; a feature is finished when the stream reaches the first kept
-// item of the next one.
 // End of an OUT_RING CTA (every warp of both roles): once all warps are
 // here, the bulk copies of each slot's last issued round must have landed
 // before the CTA's shared memory is released.
@@ -634,6 +622,18 @@ __device__ __forceinline__ bool span_is_long(const ReduceParams& p, uint32_t c, 
 template <typename T, typename A, int VPL, int MODE>
 __device__ __forceinline__ void reduce_body(const ReduceParams& p);
 
+// k_reduce: one warp per chunk of C sorted items, in windows of RW items.
+// Phase 1 takes the window 32 items (one per lane) at a time: the
+// first-occurrence rule is evaluated for all 32 at once with ballots (group
+// starts: new feature or new anchor; valid roles; for every item the first
+// valid role of its (feature, anchor) group, carried across batches and, at a
+// chunk start, found by walking back), and the kept items and the feature
+// starts are appended to the warp's lists.  Item metadata is
+// software-pipelined: while batch b is examined, the role flags and scales of
+// batch b+1 and the keys of batch b+2 are in flight.  Phase 2 streams the
+// kept items' direction rows in list order, NF in flight across feature
+// boundaries; a feature is finished when the stream reaches the first kept
+// item of the next one.
 template <typename T, typename A, int VPL, int MODE>
 __global__ void __launch_bounds__(MODE == OUT_RING ? RING_MAX_WARPS * 32 : (MODE == OUT_QUEUE ? QUEUE_THREADS : RED_THREADS),
                                   MODE == OUT_RING ? 1 : (VPL >= 16 ? 1 : (MODE == OUT_DENSE ? 3 : (MODE == OUT_QUEUE ? 4 : 2))))
