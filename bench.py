@@ -8,7 +8,8 @@ dims 256, max_neighbors 25, 10 negatives, StarSpace margin 0.5, batch 8192).
 
 Legs in one run (rank 0, N=1):
   value        fused BF16 form, inputs resident in HBM, CUDA-event time of the
-               timed batches (a CUDA graph replay per batch)
+               timed batches (replays of a CUDA graph of 16 batches, and one
+               graph for a run's remainder, built and uploaded beforehand)
   plain_fp32   the plain FP32 form on the same workload and steps
   cpu_baseline the oracle's CPU restatement of the reference training loop on
                a bounded sample of the same workload, all host threads
