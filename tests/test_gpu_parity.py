@@ -98,14 +98,15 @@ def test_batch_grad_multi_chunk_spans(oracle, monkeypatch, chunk, form):
     check_parity(oracle, prob, smp, ctx, table, grad_tol=TOL if form == 0 else TOL_GRAD_BF16, loss=1, gamma=0.5)
 
 
-@pytest.mark.parametrize("name", ["margin", "starspace"])
+@pytest.mark.parametrize("name", ["margin", "starspace", "contrastive"])
 @pytest.mark.parametrize("form", [0, 1])
 def test_default_losses_known_answers(name, form):
-    # the hand-derived Margin and StarSpace answers of tests/test_oracle.py,
-    # straight through the C ABI (the tables are exact in BF16)
-    from tests.test_oracle import MARGIN_KAT, STARSPACE_KAT
+    # the hand-derived Margin, StarSpace and Contrastive answers of
+    # tests/test_oracle.py, straight through the C ABI (the tables are exact
+    # in BF16)
+    from tests.test_oracle import KATS
 
-    k = MARGIN_KAT if name == "margin" else STARSPACE_KAT
+    k, lid = KATS[name]
     n = len(k["fptr"]) - 1
     prob = dict(rows=np.arange(n + 1, dtype=np.uint64), cols=((np.arange(n) + 1) % n).astype(np.uint32),
                 fptr=np.array(k["fptr"], np.uint64), fids=np.array(k["fids"], np.uint32),
@@ -114,7 +115,7 @@ def test_default_losses_known_answers(name, form):
                nbr=np.array(k["nbr"], np.uint32), nbr_w=np.array(k["nbr_w"], np.float32),
                neg=np.array(k["neg"], np.uint32))
     R = smp["neg"].shape[1]
-    ctx = make_ctx(prob, loss=0 if name == "margin" else 1, gamma=k["gamma"], R=R, form=form)
+    ctx = make_ctx(prob, loss=lid, gamma=k["gamma"], neg_margin=k.get("neg_margin", 0.1), R=R, form=form)
     gl, gst, ids, rows = gpu_batch(ctx, prob, smp)
     assert gst.tolist() == [0]
     assert abs(gl[0] - k["loss"]) < 1e-6

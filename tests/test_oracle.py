@@ -135,6 +135,27 @@ STARSPACE_KAT = dict(
     grad={0: [0.0, -0.1], 1: [-1 / 3, 0.0], 2: [-2 / 3, 0.0], 3: [0.128, -0.096]})
 
 
+# Contrastive, pos_margin (gamma) = 0.875, neg_margin = 0.5 (both exact in
+# f32, as the reference holds them), R = 2 (loss.rs:107-128: mean over the
+# kept terms of (cos(h^,u^) - neg_margin)+ and (pos_margin - cos(t^,h^))+, a
+# term kept when positive):
+#   h = E0 = (3,4): h^ = (.6,.8), |h| = 5;  t = E1 = (0,2) (one neighbour,
+#       weight 1): t^ = (0,1), |t| = 2;  pos term .875 - .8 = .075  (kept)
+#   u1 = E2 = (4,3): u1^ = (.8,.6), |u1| = 5; cos = .96: .96 - .5 = .46 (kept)
+#   u2 = E3 = (-1,0): cos = -.6 -> -1.1                               (dropped)
+#   L = (.46 + .075) / 2 = .2675
+#   dL/dh  = (I - h^h^T)/5 (u1^ - t^)/2     = (0.0704, -0.0528)
+#   dL/dt  = (I - t^t^T)/2 (-h^/2)           = (-0.15, 0)
+#   dL/du1 = (I - u1^u1^T)/5 (h^/2)          = (-0.0168, 0.0224)
+CONTRASTIVE_KAT = dict(
+    table=[[3, 4], [0, 2], [4, 3], [-1, 0]],
+    fptr=[0, 1, 2, 3, 4], fids=[0, 1, 2, 3],
+    nbr_ptr=[0, 1], nbr=[1], nbr_w=[1.0], neg=[[2, 3]], gamma=0.875, neg_margin=0.5, loss=0.2675,
+    grad={0: [0.0704, -0.0528], 1: [-0.15, 0.0], 2: [-0.0168, 0.0224]})
+
+KATS = {"margin": (MARGIN_KAT, 0), "starspace": (STARSPACE_KAT, 1), "contrastive": (CONTRASTIVE_KAT, 2)}
+
+
 def kat_args(k):
     n = len(k["fptr"]) - 1
     rows = np.arange(n + 1, dtype=np.uint64)          # one (unused) edge per node
@@ -142,12 +163,12 @@ def kat_args(k):
             np.array(k["table"], np.float32), rows, [0], k["nbr_ptr"], k["nbr"], k["nbr_w"], k["neg"])
 
 
-@pytest.mark.parametrize("name", ["margin", "starspace"])
+@pytest.mark.parametrize("name", ["margin", "starspace", "contrastive"])
 @pytest.mark.parametrize("prec", ["f64", "f32"])
 def test_default_losses_known_answers(oracle, name, prec):
-    k = MARGIN_KAT if name == "margin" else STARSPACE_KAT
-    lid = oracle.LOSS_MARGIN if name == "margin" else oracle.LOSS_STARSPACE
-    loss, st, g, t = oracle.batch(*kat_args(k), oracle.loss_cfg(loss=lid, gamma=k["gamma"]), prec)
+    k, lid = KATS[name]
+    cfg = oracle.loss_cfg(loss=lid, gamma=k["gamma"], neg_margin=k.get("neg_margin", 0.0))
+    loss, st, g, t = oracle.batch(*kat_args(k), cfg, prec)
     tol = 1e-12 if prec == "f64" else 1e-6
     assert st.tolist() == [0]
     assert abs(loss[0] - k["loss"]) < tol * 10
